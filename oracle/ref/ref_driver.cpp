@@ -1,0 +1,140 @@
+/* C entry points over the reference's own, unmodified classes
+   (CMatrixGenerator, CMatrix, Likelihood, Math::Legendre and the reference's
+   TestLegendre / TestMatrix known-answer subtests).  Test infrastructure: the
+   fixture generator under tests/golden/ calls these through ctypes to pin the
+   oracle restatement to the reference's real code. */
+#include <vector>
+#include <string>
+#include <exception>
+#include <cstring>
+
+#include <c_matrix.hpp>
+#include <c_matrix_generator.hpp>
+#include <likelihood.hpp>
+#include <legendre.hpp>
+#include <utils.hpp>
+#include <test_legendre.hpp>
+#include <test_matrix.hpp>
+
+static std::string g_err;
+
+extern "C" const char* ref_last_error() { return g_err.c_str(); }
+
+static void copy_packed(const CMatrix& m, double* out)
+{
+    const int n = m.getNPix();
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i <= j; ++i)
+            out[(long)j * (j + 1) / 2 + i] = m.element(i, j);
+}
+
+/* CMatrixGenerator::clToCMatrix (source/c_matrix_generator.cpp:164-232);
+   good_nest == NULL means all pixels. */
+extern "C" int ref_cl_to_cmatrix(const double* cl, int lmax, long nside, double fwhm_deg,
+                                 const int* good_nest, int n, double* out_packed)
+{
+    try {
+        std::vector<double> c(cl, cl + lmax + 1);
+        std::vector<int> good;
+        if (good_nest) good.assign(good_nest, good_nest + n);
+        CMatrix* m = CMatrixGenerator::clToCMatrix(c, nside, fwhm_deg, good_nest ? &good : NULL);
+        copy_packed(*m, out_packed);
+        delete m;
+        return 0;
+    } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
+/* The reference's low-l call sequence (source/test_like_low.cpp:183-193):
+   clToCMatrix -> generateNoiseMatrix + maskMatrix -> Likelihood(C, 0, N, good, {})
+   -> calculate(d).  logdet is the reference's value (with its detOffset). */
+extern "C" int ref_likelihood(const double* cl, int lmax, long nside, double fwhm_deg,
+                              const int* good_nest, int n, double noise_sigma, const double* d,
+                              double* chi2, double* logdet, double* like)
+{
+    try {
+        std::vector<double> c(cl, cl + lmax + 1);
+        std::vector<int> good(good_nest, good_nest + n);
+        CMatrix* cm = CMatrixGenerator::clToCMatrix(c, nside, fwhm_deg, &good);
+        CMatrix* noise = CMatrixGenerator::generateNoiseMatrix(nside, noise_sigma);
+        noise->maskMatrix(good);
+        CMatrix fid(n);
+        Likelihood like_obj(*cm, fid, *noise, good, std::vector<double>());
+        std::vector<double> t(d, d + n);
+        *like = like_obj.calculate(t, *chi2, *logdet);
+        delete cm;
+        delete noise;
+        return 0;
+    } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
+/* Likelihood from caller-supplied packed matrices (fiducial may be NULL = 0),
+   with optional foreground marginalisation (source/likelihood.cpp:69-180). */
+extern "C" int ref_likelihood_packed(const double* c_packed, const double* fid_packed, const double* noise_packed,
+                                     int n, const double* d, const double* foreground,
+                                     double* chi2, double* logdet, double* like)
+{
+    try {
+        CMatrix c(n), f(n), nm(n);
+        for (int j = 0; j < n; ++j)
+            for (int i = 0; i <= j; ++i) {
+                const long k = (long)j * (j + 1) / 2 + i;
+                c.element(i, j) = c_packed[k];
+                if (fid_packed) f.element(i, j) = fid_packed[k];
+                nm.element(i, j) = noise_packed[k];
+            }
+        std::vector<int> good(n);
+        for (int i = 0; i < n; ++i) good[i] = i;
+        std::vector<double> fg;
+        if (foreground) fg.assign(foreground, foreground + n);
+        Likelihood like_obj(c, f, nm, good, fg);
+        std::vector<double> t(d, d + n);
+        *like = like_obj.calculate(t, *chi2, *logdet);
+        return 0;
+    } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
+/* CMatrixGenerator::getFiducialMatrix (source/c_matrix_generator.cpp:705-772) */
+extern "C" int ref_fiducial_matrix(const double* cl, int cl_size, long nside, int lmax, double fwhm_deg,
+                                   const int* good_nest, int n, double* out_packed)
+{
+    try {
+        std::vector<double> c(cl, cl + cl_size);
+        std::vector<int> good(good_nest, good_nest + n);
+        CMatrix* m = CMatrixGenerator::getFiducialMatrix(c, nside, lmax, fwhm_deg, &good);
+        copy_packed(*m, out_packed);
+        delete m;
+        return 0;
+    } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
+/* Utils::beamFunction (source/utils.cpp:54-64) and the pixel-window reader
+   with the unit window the shim serves (source/utils.cpp:66-170). */
+extern "C" double ref_beam(int l, double fwhm_deg) { return Utils::beamFunction(l, fwhm_deg); }
+extern "C" int ref_pixel_window(long nside, int lmax, double fwhm_deg, double* out)
+{
+    try {
+        std::vector<double> f;
+        Utils::readPixelWindowFunction(f, nside, lmax, fwhm_deg);
+        for (int l = 0; l <= lmax; ++l) out[l] = f[l];
+        return 0;
+    } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
+/* Math::Legendre::calculate (include/legendre.hpp:26-37) */
+extern "C" double ref_legendre(int l, double x) { Math::Legendre leg; return leg.calculate(l, x); }
+
+/* The reference's own known-answer subtests (source/test_legendre.cpp:27-51,
+   source/test_matrix.cpp:417-488), run through their protected runSubTest. */
+class CgTestLegendre : public TestLegendre { public: using TestLegendre::runSubTest; };
+class CgTestMatrix : public TestMatrix { public: using TestMatrix::runSubTest; };
+
+extern "C" int ref_run_subtest(const char* which, int i, double* res, double* expected)
+{
+    try {
+        std::string name;
+        if (std::strcmp(which, "legendre") == 0) { CgTestLegendre t; t.runSubTest(i, *res, *expected, name); }
+        else if (std::strcmp(which, "matrix") == 0) { CgTestMatrix t; t.runSubTest(i, *res, *expected, name); }
+        else return 2;
+        return 0;
+    } catch (std::exception& e) { g_err = e.what(); return 1; }
+}

@@ -1,0 +1,118 @@
+"""Generate the golden fixtures in this folder from the reference's own code.
+
+Runs here, where the reference sources exist: ``make -C oracle/ref`` compiles
+the reference's unmodified translation units into oracle/_ref/libcg_ref.so
+(project-written HEALPix / cfitsio / LAPACK shims), and this script calls
+them through ctypes.  Every number stored below comes from the reference:
+
+* Legendre and symmetric-matrix known-answer subtests (source/test_legendre.cpp,
+  source/test_matrix.cpp), as (result, expected) pairs;
+* clToCMatrix covariance matrices (full packed for small cases, SHA-256 plus
+  samples for larger ones);
+* Likelihood(C, 0, N, goodPixels).calculate(d) chi2 / logDet / -2lnL for the
+  fiducial and a few lognormal-perturbed C_l vectors;
+* central finite differences (step 1e-4 C_l) of the reference's -2lnL, which
+  pin the adjoint gradient the reference does not have.
+
+Usage:  python tests/golden/make_golden.py
+"""
+import ctypes
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+from cosmopp_gb300 import workload as W  # noqa: E402
+
+dp = ctypes.POINTER(ctypes.c_double)
+ip = ctypes.POINTER(ctypes.c_int)
+DET_OFFSET = 29677.0566  # source/likelihood.cpp:127-128 (logDet -= -29677.0566)
+
+CASES = [
+    # name, nside, lmax, fwhm_arcmin, keep, sigma, n_perturbed, fd_ells, store_full_c
+    ("nside1", 1, 4, 440.0, 1.0, 1.0, 2, "all", True),
+    ("nside2", 2, 8, 440.0, 0.8, 1.0, 2, "all", True),
+    ("nside4", 4, 16, 440.0, 0.8, 1.0, 2, "all", True),
+    ("nside8_lmax24", 8, 24, 440.0, 0.8, 1.0, 3, [2, 3, 10, 17, 24], False),
+    ("nside16_lmax47", 16, 47, 220.0, 0.8, 1.0, 2, [2, 30, 47], False),
+]
+
+
+def ref_cmatrix(R, cl, nside, fwhm, nest):
+    n = len(nest)
+    out = np.zeros(n * (n + 1) // 2)
+    rc = R.ref_cl_to_cmatrix(cl.ctypes.data_as(dp), len(cl) - 1, nside, fwhm, nest.ctypes.data_as(ip), n,
+                             out.ctypes.data_as(dp))
+    assert rc == 0, R.ref_last_error()
+    return out
+
+
+def ref_like(R, cl, nside, fwhm, nest, sigma, d):
+    chi2, ld, lk = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    rc = R.ref_likelihood(cl.ctypes.data_as(dp), len(cl) - 1, nside, fwhm, nest.ctypes.data_as(ip), len(nest),
+                          sigma, d.ctypes.data_as(dp), ctypes.byref(chi2), ctypes.byref(ld), ctypes.byref(lk))
+    assert rc == 0, R.ref_last_error()
+    return chi2.value, ld.value, lk.value
+
+
+def main():
+    if not O.ref_available():
+        raise SystemExit("build the reference first: make -C oracle/ref")
+    R = O.ref()
+    os.makedirs(os.path.join(HERE, "_kat", "test_files"), exist_ok=True)
+    cwd = os.getcwd()
+    os.chdir(os.path.join(HERE, "_kat"))  # the matrix subtests write text files under test_files/
+    kat = []
+    res, exp = ctypes.c_double(), ctypes.c_double()
+    for which, idx in [("legendre", i) for i in range(5)] + [("matrix", 18), ("matrix", 19)]:
+        rc = R.ref_run_subtest(which.encode(), idx, ctypes.byref(res), ctypes.byref(exp))
+        assert rc == 0
+        kat.append((which, idx, res.value, exp.value))
+    os.chdir(cwd)
+    np.savez(os.path.join(HERE, "kat_reference.npz"),
+             which=np.array([k[0] for k in kat]), index=np.array([k[1] for k in kat]),
+             result=np.array([k[2] for k in kat]), expected=np.array([k[3] for k in kat]))
+
+    for name, nside, lmax, fwhm_am, keep, sigma, npert, fd_ells, store_full in CASES:
+        fwhm = fwhm_am / 60.0
+        ring = W.bernoulli_mask(nside, keep, 1234) if keep < 1 else np.arange(12 * nside * nside, dtype=np.int32)
+        nest = O.ring2nest(nside, ring)
+        n = len(nest)
+        cl_fid = W.fiducial_cl(lmax)
+        cls = np.vstack([cl_fid, W.lognormal_batch(cl_fid, npert, 7)])
+        c_fid = ref_cmatrix(R, cl_fid, nside, fwhm, nest)
+        z = np.random.default_rng(0).standard_normal(n)
+        full = W.packed_to_full(c_fid, n) + sigma ** 2 * np.eye(n)
+        d = W.draw_data(full, z)
+        rows = []
+        for cl in cls:
+            rows.append(ref_like(R, cl, nside, fwhm, nest, sigma, d))
+        rows = np.array(rows)
+        ells = list(range(2, lmax + 1)) if fd_ells == "all" else list(fd_ells)
+        fd = []
+        for ell in ells:
+            h = 1e-4 * cl_fid[ell]
+            cp = cl_fid.copy(); cp[ell] += h
+            cm = cl_fid.copy(); cm[ell] -= h
+            fd.append((ref_like(R, cp, nside, fwhm, nest, sigma, d)[2] - ref_like(R, cm, nside, fwhm, nest, sigma, d)[2]) / (2 * h))
+        out = dict(nside=nside, lmax=lmax, fwhm_deg=fwhm, sigma=sigma, ring_kept=ring, nest_good=nest,
+                   cls=cls, d=d, chi2=rows[:, 0], logdet_ref=rows[:, 1], like_ref=rows[:, 2],
+                   logdet_raw=rows[:, 1] - DET_OFFSET, m2lnl=rows[:, 0] + (rows[:, 1] - DET_OFFSET),
+                   fd_ells=np.array(ells), fd_grad=np.array(fd),
+                   c_sha256=np.array(hashlib.sha256(c_fid.tobytes()).hexdigest()),
+                   c_diag=np.array([c_fid[j * (j + 1) // 2 + j] for j in range(n)]),
+                   c_head=c_fid[:4096].copy())
+        if store_full:
+            out["c_packed"] = c_fid
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print(name, "n", n, "m2lnl", out["m2lnl"][0], "chi2", rows[0, 0])
+
+
+if __name__ == "__main__":
+    main()

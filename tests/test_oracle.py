@@ -1,0 +1,101 @@
+"""The oracle restatement pinned to the reference's own outputs (golden
+fixtures made by tests/golden/make_golden.py from the reference compiled from
+its sources) and to the reference's known-answer tests."""
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from cosmopp_gb300 import workload as W
+
+DET_OFFSET = 29677.0566
+
+
+def test_reference_kats_legendre_and_matrix(oracle_mod):
+    kat = load_golden("kat_reference")
+    for which, idx, res, exp in zip(kat["which"], kat["index"], kat["result"], kat["expected"]):
+        # the reference's own tests pass at its default precision (rel 1e-5)
+        assert abs(res - exp) <= 1e-5 * max(1.0, abs(exp)), (which, idx)
+    # the oracle's Legendre reproduces the reference's results exactly
+    legendre_args = [(4, 2.0), (10, 0.5), (64, 0.1), (1000, -0.25), (10000, -0.5)]
+    for (l, x), res in zip(legendre_args, kat["result"][:5]):
+        assert oracle_mod.legendre(l, x) == res
+
+
+def test_oracle_2x2_cholesky_invert_and_determinant(oracle_mod):
+    # source/test_matrix.cpp:417-488: [[2,1],[1,3]] invert, [[3,2],[2,4]] determinant
+    ap = np.array([2.0, 1.0, 3.0])
+    u, info = oracle_mod.dpptrf(ap)
+    assert info == 0
+    inv, info = oracle_mod.dpptri(u)
+    assert info == 0
+    full = W.packed_to_full(inv, 2)
+    assert np.allclose(full @ np.array([[2, 1], [1, 3.0]]), np.eye(2), atol=1e-12)
+    u2, _ = oracle_mod.dpptrf(np.array([3.0, 2.0, 4.0]))
+    sign = np.array([0], dtype=np.int32)
+    ld = oracle_mod.lib().orc_logdet_from_chol(2, u2.ctypes.data_as(oracle_mod._dp),
+                                               sign.ctypes.data_as(oracle_mod._ip))
+    assert abs(np.exp(ld) - 8.0) < 1e-12
+
+
+def test_oracle_not_positive_definite_reports_info(oracle_mod):
+    _, info = oracle_mod.dpptrf(np.array([1.0, 2.0, 1.0]))  # [[1,2],[2,1]] is indefinite
+    assert info == 2
+
+
+@pytest.mark.parametrize("name", ["nside1", "nside2", "nside4", "nside8_lmax24", "nside16_lmax47"])
+def test_oracle_cmatrix_matches_reference_bitwise(oracle_mod, name):
+    g = load_golden(name)
+    xyz = oracle_mod.unit_vectors(int(g["nside"]), g["nest_good"], "NEST")
+    c = oracle_mod.cl_to_cmatrix(g["cls"][0], xyz, float(g["fwhm_deg"]))
+    assert hashlib.sha256(c.tobytes()).hexdigest() == str(g["c_sha256"])
+    if "c_packed" in g:
+        assert np.array_equal(c, g["c_packed"])
+    # RING indices give the same directions as their NEST images
+    xyz_r = oracle_mod.unit_vectors(int(g["nside"]), g["ring_kept"], "RING")
+    assert np.array_equal(xyz, xyz_r)
+
+
+@pytest.mark.parametrize("name", ["nside1", "nside2", "nside4", "nside8_lmax24"])
+def test_oracle_likelihood_matches_reference(oracle_mod, name):
+    g = load_golden(name)
+    xyz = oracle_mod.unit_vectors(int(g["nside"]), g["nest_good"], "NEST")
+    for k, cl in enumerate(g["cls"]):
+        e = oracle_mod.evaluate(cl, xyz, float(g["fwhm_deg"]), float(g["sigma"]) ** 2, g["d"], grad=False)
+        assert e["status"] == 0
+        assert abs(e["logdet"] - g["logdet_raw"][k]) <= 1e-9 * abs(g["logdet_raw"][k])
+        assert abs(e["chi2"] - g["chi2"][k]) <= 1e-9 * abs(g["chi2"][k])
+        assert abs((e["logdet"] + DET_OFFSET) - g["logdet_ref"][k]) <= 1e-8
+
+
+@pytest.mark.parametrize("name", ["nside1", "nside2", "nside4", "nside8_lmax24"])
+def test_oracle_adjoint_gradient_matches_reference_fd(oracle_mod, name):
+    g = load_golden(name)
+    xyz = oracle_mod.unit_vectors(int(g["nside"]), g["nest_good"], "NEST")
+    e = oracle_mod.evaluate(g["cls"][0], xyz, float(g["fwhm_deg"]), float(g["sigma"]) ** 2, g["d"], grad=True)
+    scale = np.abs(g["fd_grad"]).max()
+    for ell, fd in zip(g["fd_ells"], g["fd_grad"]):
+        # central differences at step 1e-4 C_l carry O(h^2) truncation + roundoff of the reference
+        assert abs(e["grad"][ell] - fd) <= 1e-5 * abs(fd) + 1e-7 * scale, (ell, e["grad"][ell], fd)
+
+
+def test_single_pass_recurrence_equals_reference_restart(oracle_mod):
+    g = load_golden("nside4")
+    xyz = oracle_mod.unit_vectors(4, g["nest_good"], "NEST")
+    a = oracle_mod.cl_to_cmatrix(g["cls"][1], xyz, float(g["fwhm_deg"]), restart=True)
+    b = oracle_mod.cl_to_cmatrix(g["cls"][1], xyz, float(g["fwhm_deg"]), restart=False)
+    assert np.array_equal(a, b)
+
+
+def test_healpix_ring_nest_roundtrip(oracle_mod):
+    for ns in (1, 2, 4, 8, 16):
+        npix = 12 * ns * ns
+        r = np.arange(npix)
+        nest = oracle_mod.ring2nest(ns, r)
+        assert sorted(nest.tolist()) == list(range(npix))
+        assert np.array_equal(oracle_mod.nest2ring(ns, nest), r)
+    # nside 1 base pixels: rings at z = 2/3, 0, -2/3 (Gorski et al. 2005, fig. 3)
+    xyz = oracle_mod.unit_vectors(1, None, "RING")
+    assert np.allclose(xyz[:4, 2], 2 / 3) and np.allclose(xyz[4:8, 2], 0) and np.allclose(xyz[8:, 2], -2 / 3)
+    assert np.allclose(np.arctan2(xyz[4:8, 1], xyz[4:8, 0]) % (2 * np.pi), [0, np.pi / 2, np.pi, 3 * np.pi / 2])
