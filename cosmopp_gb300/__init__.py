@@ -1,0 +1,372 @@
+"""cosmopp_gb300: GB300-native pixel-space CMB covariance and low-l TT likelihood.
+
+Python front end over the C ABI (include/cosmopp_gb300.h) of the in-tree
+library cosmopp_gb300/_lib/libcosmopp_gb300.so.  The Python names mirror the
+reference's call surface:
+
+* ``Context.build_cmatrix``  -- CMatrixGenerator::clToCMatrix
+  (include/c_matrix_generator.hpp:53);
+* ``Context.loglike``        -- Likelihood(C, 0, N, goodPixels).calculate(d)
+  for a batch of C_l vectors, plus d(-2lnL)/dC_l (new);
+* ``Likelihood``             -- the Likelihood class itself
+  (include/likelihood.hpp:36-132) built from packed matrices;
+* ``LikelihoodWithDerivs``   -- the Math::LikelihoodWithDerivs interface the
+  reference's HMC consumes (include/likelihood_function.hpp:30-47).
+
+There is no CPU fallback: if the library is missing, importing the compute
+entry points raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+__all__ = ["Context", "Likelihood", "LikelihoodWithDerivs", "CGError", "library", "DET_OFFSET",
+           "ring2nest", "nest2ring", "pix2vec", "beam"]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libcosmopp_gb300.so")
+
+# source/likelihood.cpp:127-128: the reference subtracts detOffset = -29677.0566 from ln det C
+DET_OFFSET = 29677.0566
+
+CG_OK, CG_ERR_BAD_ARG, CG_ERR_NOT_PD, CG_ERR_NONFINITE, CG_ERR_TIMEOUT, CG_ERR_CUDA, CG_ERR_NO_DEVICE, \
+    CG_ERR_ALLOC = range(8)
+_STATUS_NAMES = {0: "OK", 1: "BAD_ARG", 2: "NOT_PD", 3: "NONFINITE", 4: "TIMEOUT", 5: "CUDA", 6: "NO_DEVICE",
+                 7: "ALLOC"}
+SCHEME = {"RING": 0, "NEST": 1}
+PRECISION = {"fp64": 0, "mixed": 1}
+RECENTER = {"fixed": 0, "batch": 1, "auto": 2}
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+class CGError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("cosmopp_gb300 error %s (%d): %s" % (_STATUS_NAMES.get(code, "?"), code, msg))
+        self.code = code
+
+
+class _Config(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_int), ("nside", ctypes.c_long), ("scheme", ctypes.c_int),
+                ("good_pixels", _ip), ("n", ctypes.c_int), ("dirs", _dp), ("lmax", ctypes.c_int),
+                ("fwhm_deg", ctypes.c_double), ("beam", _dp), ("noise_sigma", ctypes.c_double),
+                ("noise_var", _dp), ("max_batch", ctypes.c_int), ("precision", ctypes.c_int),
+                ("device", ctypes.c_int), ("cl_ref", _dp), ("recenter", ctypes.c_int),
+                ("recenter_radius", ctypes.c_double)]
+
+
+_lib = None
+
+
+def library():
+    """Load the shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("cosmopp_gb300 native library not built (%s); run `python -m cosmopp_gb300.build`"
+                          % LIB_PATH)
+    L = ctypes.CDLL(LIB_PATH)
+    L.cg_config_init.argtypes = [ctypes.POINTER(_Config)]
+    L.cg_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(_Config)]
+    L.cg_destroy.argtypes = [ctypes.c_void_p]
+    L.cg_last_error.restype = ctypes.c_char_p
+    L.cg_last_error.argtypes = [ctypes.c_void_p]
+    L.cg_get_n.argtypes = [ctypes.c_void_p]
+    L.cg_unit_vectors.argtypes = [ctypes.c_void_p, _dp]
+    L.cg_build_cmatrix.argtypes = [ctypes.c_void_p, _dp, _dp]
+    L.cg_build_cmatrix_batched.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
+    L.cg_loglike.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, ctypes.c_int, _dp, _dp, _dp, _dp, _ip]
+    L.cg_loglike_device.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p, ctypes.c_void_p]
+    L.cg_set_reference.argtypes = [ctypes.c_void_p, _dp]
+    L.cg_reference_count.argtypes = [ctypes.c_void_p]
+    L.cg_likelihood_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_int]
+    L.cg_likelihood_calculate.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+    L.cg_likelihood_logdet.restype = ctypes.c_double
+    L.cg_likelihood_logdet.argtypes = [ctypes.c_void_p]
+    L.cg_likelihood_destroy.argtypes = [ctypes.c_void_p]
+    L.cg_likelihood_last_error.restype = ctypes.c_char_p
+    L.cg_likelihood_last_error.argtypes = [ctypes.c_void_p]
+    L.cg_nside2npix.restype = ctypes.c_long
+    L.cg_nside2npix.argtypes = [ctypes.c_long]
+    L.cg_ring2nest.restype = ctypes.c_long
+    L.cg_ring2nest.argtypes = [ctypes.c_long, ctypes.c_long]
+    L.cg_nest2ring.restype = ctypes.c_long
+    L.cg_nest2ring.argtypes = [ctypes.c_long, ctypes.c_long]
+    L.cg_pix2vec.argtypes = [ctypes.c_long, ctypes.c_int, _ip, ctypes.c_int, _dp]
+    L.cg_beam.restype = ctypes.c_double
+    L.cg_beam.argtypes = [ctypes.c_int, ctypes.c_double]
+    _lib = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+# ---- HEALPix host helpers ---------------------------------------------------
+
+def ring2nest(nside, ring):
+    L = library()
+    return np.array([L.cg_ring2nest(nside, int(r)) for r in np.atleast_1d(ring)], dtype=np.int32)
+
+
+def nest2ring(nside, nest):
+    L = library()
+    return np.array([L.cg_nest2ring(nside, int(p)) for p in np.atleast_1d(nest)], dtype=np.int32)
+
+
+def pix2vec(nside, pix=None, scheme="NEST"):
+    L = library()
+    if pix is None:
+        n, pp = 12 * nside * nside, None
+    else:
+        pp = np.ascontiguousarray(pix, dtype=np.int32)
+        n = len(pp)
+    out = np.zeros((n, 3))
+    rc = L.cg_pix2vec(nside, SCHEME[scheme.upper()], None if pp is None else pp.ctypes.data_as(_ip), n, _p(out))
+    if rc:
+        raise CGError(rc, "cg_pix2vec")
+    return out
+
+
+def beam(l, fwhm_deg):
+    return library().cg_beam(int(l), float(fwhm_deg))
+
+
+# ---- context ------------------------------------------------------------------
+
+class Context:
+    """One GPU context for a fixed pixel set, l range, beam and noise.
+
+    precision="fp64": the plain FP64 path (bit-identical covariance, FP64
+    Cholesky).  precision="mixed": the batched mixed path (FP64 reference
+    factorisation, FP32 whitened factors, FP64 log-det and refinement).
+    """
+
+    def __init__(self, lmax, fwhm_deg, nside=None, good_pixels=None, scheme="NEST", dirs=None, beam=None,
+                 noise_sigma=1e-3, noise_var=None, max_batch=1, precision="fp64", device=0, cl_ref=None,
+                 recenter="auto", recenter_radius=1.0):
+        L = library()
+        cfg = _Config()
+        L.cg_config_init(ctypes.byref(cfg))
+        keep = []
+        if dirs is not None:
+            d = _f64(dirs).reshape(-1, 3)
+            keep.append(d)
+            cfg.dirs = _p(d)
+            cfg.n = d.shape[0]
+        else:
+            cfg.nside = int(nside)
+            cfg.scheme = SCHEME[scheme.upper()]
+            if good_pixels is not None:
+                g = np.ascontiguousarray(good_pixels, dtype=np.int32)
+                keep.append(g)
+                cfg.good_pixels = g.ctypes.data_as(_ip)
+                cfg.n = len(g)
+        cfg.lmax = int(lmax)
+        cfg.fwhm_deg = float(fwhm_deg)
+        if beam is not None:
+            b = _f64(beam)
+            keep.append(b)
+            cfg.beam = _p(b)
+        cfg.noise_sigma = float(noise_sigma)
+        if noise_var is not None:
+            nv = _f64(noise_var)
+            keep.append(nv)
+            cfg.noise_var = _p(nv)
+        cfg.max_batch = int(max_batch)
+        cfg.precision = PRECISION[precision]
+        cfg.device = int(device)
+        if cl_ref is not None:
+            cr = _f64(cl_ref)
+            keep.append(cr)
+            cfg.cl_ref = _p(cr)
+        cfg.recenter = RECENTER[recenter]
+        cfg.recenter_radius = float(recenter_radius)
+        h = ctypes.c_void_p()
+        rc = L.cg_create(ctypes.byref(h), ctypes.byref(cfg))
+        if rc:
+            raise CGError(rc, L.cg_last_error(None).decode())
+        self._h = h
+        self._L = L
+        self.lmax = int(lmax)
+        self.n = L.cg_get_n(h)
+        self.max_batch = int(max_batch)
+        self.precision = precision
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.cg_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, rc):
+        if rc:
+            raise CGError(rc, self._L.cg_last_error(self._h).decode())
+
+    @property
+    def handle(self):
+        return self._h
+
+    def unit_vectors(self):
+        out = np.zeros((self.n, 3))
+        self._check(self._L.cg_unit_vectors(self._h, _p(out)))
+        return out
+
+    def build_cmatrix(self, cl):
+        """Packed C (i <= j at j(j+1)/2 + i) for one C_l vector or a batch [B, lmax+1]."""
+        cl = _f64(cl)
+        single = cl.ndim == 1
+        cl2 = cl.reshape(-1, self.lmax + 1)
+        B = cl2.shape[0]
+        out = np.zeros((B, self.n * (self.n + 1) // 2))
+        self._check(self._L.cg_build_cmatrix_batched(self._h, B, _p(cl2), _p(out)))
+        return out[0] if single else out
+
+    def loglike(self, cl, d, grad=False):
+        """-2lnL for a batch of C_l vectors on one map d [n] or B maps [B, n].
+
+        Returns dict(m2lnl, chi2, logdet (raw ln det C), grad (d(-2lnL)/dC_l), status)."""
+        cl = _f64(cl)
+        single = cl.ndim == 1
+        cl2 = cl.reshape(-1, self.lmax + 1)
+        B = cl2.shape[0]
+        d = _f64(d)
+        stride = 0 if d.ndim == 1 else d.shape[1]
+        m2 = np.zeros(B)
+        chi2 = np.zeros(B)
+        ld = np.zeros(B)
+        st = np.zeros(B, dtype=np.int32)
+        g = np.zeros((B, self.lmax + 1)) if grad else None
+        self._check(self._L.cg_loglike(self._h, B, _p(cl2), _p(d), stride, _p(m2), _p(chi2), _p(ld), _p(g),
+                                       st.ctypes.data_as(_ip)))
+        out = dict(m2lnl=m2, chi2=chi2, logdet=ld, grad=g, status=st)
+        if single:
+            out = {k: (v[0] if v is not None else None) for k, v in out.items()}
+        return out
+
+    def loglike_device(self, B, cl_ptr, d_ptr, d_stride, m2lnl_ptr, chi2_ptr=None, logdet_ptr=None,
+                       grad_ptr=None, status_ptr=None, stream=0):
+        """Asynchronous device-pointer entry point (raw CUDA addresses, e.g. torch .data_ptr())."""
+        self._check(self._L.cg_loglike_device(self._h, int(B), cl_ptr, d_ptr, int(d_stride), m2lnl_ptr, chi2_ptr,
+                                              logdet_ptr, grad_ptr, status_ptr, stream))
+
+    def set_reference(self, cl_ref):
+        self._check(self._L.cg_set_reference(self._h, _p(_f64(cl_ref))))
+
+    def reference_count(self):
+        return self._L.cg_reference_count(self._h)
+
+
+class Likelihood:
+    """Drop-in for the reference's Likelihood (source/likelihood.cpp:38-41,69-180):
+    constructed from packed C, fiducial and noise matrices plus an optional
+    foreground map; ``calculate(t)`` returns (like, chi2, logdet) with the
+    reference's detOffset applied exactly as the reference does."""
+
+    def __init__(self, c_packed, fid_packed, noise_packed, good_pixels=None, foreground=None, device=0):
+        L = library()
+        c = _f64(c_packed)
+        n = int(round((np.sqrt(8 * len(c) + 1) - 1) / 2))
+        if good_pixels is not None and len(good_pixels) != n:
+            raise CGError(CG_ERR_BAD_ARG, "There are %d unmasked pixels, however the covariance matrix corresponds "
+                                          "to %d." % (len(good_pixels), n))
+        f = None if fid_packed is None else _f64(fid_packed)
+        nz = _f64(noise_packed)
+        for m in (f, nz):
+            if m is not None and len(m) != len(c):
+                raise CGError(CG_ERR_BAD_ARG, "matrix sizes differ")
+        fg = None if foreground is None or len(foreground) == 0 else _f64(foreground)
+        h = ctypes.c_void_p()
+        rc = L.cg_likelihood_create(ctypes.byref(h), n, _p(c), _p(f), _p(nz), _p(fg), int(device))
+        if rc:
+            raise CGError(rc, L.cg_likelihood_last_error(None).decode())
+        self._h, self._L, self.n = h, L, n
+        self.logdet_raw = L.cg_likelihood_logdet(h)
+
+    def calculate(self, t):
+        chi2 = ctypes.c_double()
+        ld = ctypes.c_double()
+        t = _f64(t)
+        rc = self._L.cg_likelihood_calculate(self._h, _p(t), ctypes.byref(chi2), ctypes.byref(ld))
+        if rc:
+            raise CGError(rc, self._L.cg_likelihood_last_error(self._h).decode())
+        logdet = ld.value - (-DET_OFFSET)  # logDet_ -= detOffset (source/likelihood.cpp:127-128)
+        return chi2.value + logdet, chi2.value, logdet
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.cg_likelihood_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class LikelihoodWithDerivs:
+    """The Math::LikelihoodWithDerivs interface (include/likelihood_function.hpp:30-47)
+    over one data map: parameters are C_l for l = lmin..lmax (or ln C_l with
+    log_params=True); ``calculate`` returns -2lnL and ``calculateDeriv(x, i)``
+    the derivative of -2lnL w.r.t. parameter i, from one cached gradient per x
+    (the reference's HMC asks for the n_par components one by one,
+    source/hmc.cpp:158-163)."""
+
+    def __init__(self, ctx, d, cl_template, lmin=2, log_params=True):
+        self.ctx = ctx
+        self.d = _f64(d)
+        self.template = _f64(cl_template).copy()
+        self.lmin = lmin
+        self.log = log_params
+        self._x = None
+        self._val = None
+        self._grad = None
+
+    def _cl(self, x):
+        cl = self.template.copy()
+        x = np.asarray(x, dtype=np.float64)
+        cl[self.lmin:self.lmin + len(x)] = np.exp(x) if self.log else x
+        return cl
+
+    def _eval(self, x):
+        x = np.array(x, dtype=np.float64)
+        if self._x is not None and np.array_equal(x, self._x):
+            return
+        cl = self._cl(x)
+        r = self.ctx.loglike(cl, self.d, grad=True)
+        if r["status"] != 0:
+            raise CGError(int(r["status"]), "likelihood evaluation failed")
+        g = r["grad"][self.lmin:self.lmin + len(x)]
+        if self.log:
+            g = g * cl[self.lmin:self.lmin + len(x)]
+        self._x, self._val, self._grad = x, r["m2lnl"], g
+
+    def calculate(self, params, nParams=None):
+        self._eval(params)
+        return self._val
+
+    def calculateDeriv(self, params, nParams, i):
+        self._eval(params)
+        return self._grad[i]

@@ -1,0 +1,418 @@
+// C ABI of cosmopp_gb300: context set-up, staging of host buffers, dispatch
+// to the plain FP64 and mixed paths, and the Likelihood drop-in.
+//
+// Entry points and the reference interfaces they replace are declared in
+// include/cosmopp_gb300.h.
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <new>
+
+#include "cg_internal.h"
+
+namespace {
+
+thread_local std::string g_create_error;
+
+bool device_ok(int device, int* sm_count, std::string& why)
+{
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        why = "no CUDA device available";
+        return false;
+    }
+    if (device < 0 || device >= count) {
+        why = "device ordinal out of range";
+        return false;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
+        why = "cudaGetDeviceProperties failed";
+        return false;
+    }
+    if (prop.major != 10 || prop.minor != 3) {
+        why = std::string("cosmopp_gb300 is built for sm_103 (GB300); device is ") + prop.name + " sm_" +
+              std::to_string(prop.major) + std::to_string(prop.minor);
+        return false;
+    }
+    *sm_count = prop.multiProcessorCount;
+    return true;
+}
+
+template <typename T>
+bool dalloc(T** p, size_t count)
+{
+    if (count == 0) count = 1;
+    if (cudaMalloc((void**)p, sizeof(T) * count) != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return false;
+    }
+    return true;
+}
+
+}  // namespace
+
+extern "C" void cg_config_init(cg_config* cfg)
+{
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->struct_size = (int)sizeof(cg_config);
+    cfg->scheme = CG_SCHEME_NEST;
+    cfg->noise_sigma = 1e-3;  // CMatrixGenerator::generateNoiseMatrix default (include/c_matrix_generator.hpp:147)
+    cfg->max_batch = 1;
+    cfg->precision = CG_PREC_FP64;
+    cfg->recenter = CG_RECENTER_AUTO;
+}
+
+extern "C" const char* cg_last_error(const cg_ctx* ctx) { return ctx ? ctx->err.c_str() : g_create_error.c_str(); }
+extern "C" int cg_get_n(const cg_ctx* ctx) { return ctx ? ctx->n : 0; }
+
+extern "C" int cg_unit_vectors(const cg_ctx* ctx, double* xyz)
+{
+    if (!ctx || !xyz) return CG_ERR_BAD_ARG;
+    std::memcpy(xyz, ctx->xyz.data(), sizeof(double) * ctx->xyz.size());
+    return CG_OK;
+}
+
+extern "C" void cg_destroy(cg_ctx* ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    cg::fp64_free(ctx);
+    cg::mixed_free(ctx);
+    cudaFree(ctx->d_xyz); cudaFree(ctx->d_noise); cudaFree(ctx->d_lega); cudaFree(ctx->d_legb);
+    cudaFree(ctx->d_beam); cudaFree(ctx->d_cl); cudaFree(ctx->d_out);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+extern "C" int cg_create(cg_ctx** out, const cg_config* cfg)
+{
+    g_create_error.clear();
+    if (!out || !cfg) { g_create_error = "NULL argument"; return CG_ERR_BAD_ARG; }
+    *out = nullptr;
+    if (cfg->struct_size != (int)sizeof(cg_config)) { g_create_error = "cg_config.struct_size mismatch"; return CG_ERR_BAD_ARG; }
+    if (cfg->lmax < 2 || cfg->lmax > 255) { g_create_error = "lmax must be in [2, 255]"; return CG_ERR_BAD_ARG; }
+    if (cfg->max_batch < 1) { g_create_error = "max_batch must be >= 1"; return CG_ERR_BAD_ARG; }
+    if (cfg->precision != CG_PREC_FP64 && cfg->precision != CG_PREC_MIXED) { g_create_error = "unknown precision"; return CG_ERR_BAD_ARG; }
+    std::unique_ptr<cg_ctx> ctx(new (std::nothrow) cg_ctx());
+    if (!ctx) { g_create_error = "out of host memory"; return CG_ERR_ALLOC; }
+
+    // pixel directions
+    if (cfg->dirs) {
+        if (cfg->n <= 0) { g_create_error = "n must be > 0 with dirs"; return CG_ERR_BAD_ARG; }
+        ctx->n = cfg->n;
+        ctx->xyz.assign(cfg->dirs, cfg->dirs + 3 * (size_t)cfg->n);
+    } else {
+        if (cfg->nside <= 0 || cfg->nside > 8192) { g_create_error = "invalid nside"; return CG_ERR_BAD_ARG; }
+        const long npix = cg_nside2npix(cfg->nside);
+        ctx->n = cfg->good_pixels ? cfg->n : (int)npix;
+        if (ctx->n <= 0 || ctx->n > npix) { g_create_error = "invalid number of kept pixels"; return CG_ERR_BAD_ARG; }
+        ctx->xyz.resize(3 * (size_t)ctx->n);
+        if (cg_pix2vec(cfg->nside, cfg->scheme, cfg->good_pixels, ctx->n, ctx->xyz.data()) != CG_OK) {
+            g_create_error = "invalid pixel index or scheme";
+            return CG_ERR_BAD_ARG;
+        }
+    }
+    for (double v : ctx->xyz)
+        if (!std::isfinite(v)) { g_create_error = "non-finite direction"; return CG_ERR_NONFINITE; }
+    ctx->lmax = cfg->lmax;
+    ctx->nt = (ctx->n + cg::TS - 1) / cg::TS;
+    ctx->N = ctx->nt * cg::TS;
+    ctx->max_batch = cfg->max_batch;
+    ctx->precision = cfg->precision;
+    ctx->recenter = cfg->recenter;
+    ctx->recenter_radius = cfg->recenter_radius > 0 ? cfg->recenter_radius : 1.0;
+    ctx->device = cfg->device;
+
+    // beam: Utils::readPixelWindowFunction with a unit window (f[l] = 1, f[l] *= B_l)
+    ctx->leg.beam.resize(ctx->lmax + 1);
+    ctx->leg.a.assign(ctx->lmax + 1, 0.0);
+    ctx->leg.b.assign(ctx->lmax + 1, 0.0);
+    for (int l = 0; l <= ctx->lmax; ++l) {
+        if (cfg->beam) ctx->leg.beam[l] = cfg->beam[l];
+        else {
+            double f = 1.0;
+            f *= cg_beam(l, cfg->fwhm_deg);
+            ctx->leg.beam[l] = f;
+        }
+        if (l >= 1) {
+            ctx->leg.a[l] = 2 - 1.0 / l;  // include/legendre.hpp:34
+            ctx->leg.b[l] = 1 - 1.0 / l;
+        }
+    }
+    if (cfg->fwhm_deg < 0 && !cfg->beam) { g_create_error = "invalid fwhm"; return CG_ERR_BAD_ARG; }
+    // noise: generateNoiseMatrix puts noise * noise on the diagonal (source/c_matrix_generator.cpp:774-787)
+    ctx->noise.resize(ctx->n);
+    for (int i = 0; i < ctx->n; ++i) {
+        ctx->noise[i] = cfg->noise_var ? cfg->noise_var[i] : cfg->noise_sigma * cfg->noise_sigma;
+        if (!std::isfinite(ctx->noise[i])) { g_create_error = "non-finite noise"; return CG_ERR_NONFINITE; }
+    }
+
+    std::string why;
+    if (!device_ok(ctx->device, &ctx->sm_count, why)) { g_create_error = why; return CG_ERR_NO_DEVICE; }
+    if (cudaSetDevice(ctx->device) != cudaSuccess) { g_create_error = "cudaSetDevice failed"; return CG_ERR_CUDA; }
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        g_create_error = "cudaStreamCreate failed";
+        return CG_ERR_CUDA;
+    }
+    const int N = ctx->N, L1 = ctx->lmax + 1, Bm = ctx->max_batch;
+    std::vector<double> soa(3 * (size_t)N, 0.0), nz(N, 0.0);
+    for (int i = 0; i < ctx->n; ++i) {
+        for (int c = 0; c < 3; ++c) soa[(size_t)c * N + i] = ctx->xyz[3 * (size_t)i + c];
+        nz[i] = ctx->noise[i];
+    }
+    // staging: cl [Bm][L1], then outputs m2lnl, chi2, logdet [Bm], grad [Bm][L1], data [Bm][N], status
+    ctx->d_out_bytes = sizeof(double) * ((size_t)Bm * (3 + L1) + (size_t)Bm * N) + sizeof(int) * Bm;
+    if (!dalloc(&ctx->d_xyz, soa.size()) || !dalloc(&ctx->d_noise, (size_t)N) || !dalloc(&ctx->d_lega, (size_t)L1) ||
+        !dalloc(&ctx->d_legb, (size_t)L1) || !dalloc(&ctx->d_beam, (size_t)L1) || !dalloc(&ctx->d_cl, (size_t)Bm * L1) ||
+        !dalloc((unsigned char**)&ctx->d_out, ctx->d_out_bytes)) {
+        g_create_error = "device allocation failed";
+        cg_destroy(ctx.release());
+        return CG_ERR_ALLOC;
+    }
+    cudaMemcpy(ctx->d_xyz, soa.data(), sizeof(double) * soa.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->d_noise, nz.data(), sizeof(double) * N, cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->d_lega, ctx->leg.a.data(), sizeof(double) * L1, cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->d_legb, ctx->leg.b.data(), sizeof(double) * L1, cudaMemcpyHostToDevice);
+    cudaMemcpy(ctx->d_beam, ctx->leg.beam.data(), sizeof(double) * L1, cudaMemcpyHostToDevice);
+    if (cudaGetLastError() != cudaSuccess) { g_create_error = "upload failed"; cg_destroy(ctx.release()); return CG_ERR_CUDA; }
+    if (ctx->precision == CG_PREC_MIXED && cfg->cl_ref) {
+        const int rc = cg::mixed_prepare_reference(ctx.get(), cfg->cl_ref);
+        if (rc) { g_create_error = ctx->err; cg_destroy(ctx.release()); return rc; }
+    }
+    *out = ctx.release();
+    return CG_OK;
+}
+
+// ---- covariance build ------------------------------------------------------
+
+extern "C" int cg_build_cmatrix_batched(cg_ctx* ctx, int B, const double* cl, double* out_packed)
+{
+    if (!ctx || !cl || !out_packed || B < 1 || B > ctx->max_batch) {
+        if (ctx) ctx->err = "bad arguments to cg_build_cmatrix_batched";
+        return CG_ERR_BAD_ARG;
+    }
+    for (size_t k = 0; k < (size_t)B * (ctx->lmax + 1); ++k)
+        if (!std::isfinite(cl[k])) { ctx->err = "non-finite C_l"; return CG_ERR_NONFINITE; }
+    CG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const size_t np = (size_t)ctx->n * (ctx->n + 1) / 2;
+    double* d_out = nullptr;
+    CG_CUDA_TRY(ctx, cudaMalloc((void**)&d_out, sizeof(double) * np * B));
+    cudaMemcpyAsync(ctx->d_cl, cl, sizeof(double) * B * (ctx->lmax + 1), cudaMemcpyHostToDevice, ctx->stream);
+    int rc = cg::fp64_build_packed(ctx, B, ctx->d_cl, d_out, ctx->stream);
+    if (rc == CG_OK) {
+        cudaMemcpyAsync(out_packed, d_out, sizeof(double) * np * B, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = CG_ERR_CUDA; }
+    }
+    cudaFree(d_out);
+    return rc;
+}
+
+extern "C" int cg_build_cmatrix(cg_ctx* ctx, const double* cl, double* out_packed)
+{
+    return cg_build_cmatrix_batched(ctx, 1, cl, out_packed);
+}
+
+// ---- likelihood ------------------------------------------------------------
+
+extern "C" int cg_loglike_device(cg_ctx* ctx, int B, const double* d_cl, const double* d_d, int d_stride,
+                                 double* d_m2lnl, double* d_chi2, double* d_logdet, double* d_grad, int* d_status,
+                                 void* stream)
+{
+    if (!ctx) return CG_ERR_BAD_ARG;
+    if (B < 1 || B > ctx->max_batch || !d_cl || !d_d || !d_m2lnl || (d_stride != 0 && d_stride < ctx->n)) {
+        ctx->err = "bad arguments to cg_loglike";
+        return CG_ERR_BAD_ARG;
+    }
+    CG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    if (ctx->precision == CG_PREC_MIXED)
+        return cg::mixed_loglike(ctx, B, d_cl, nullptr, d_d, d_stride, d_m2lnl, d_chi2, d_logdet, d_grad, d_status, s);
+    return cg::fp64_loglike(ctx, B, d_cl, d_d, d_stride, d_m2lnl, d_chi2, d_logdet, d_grad, d_status, s);
+}
+
+extern "C" int cg_loglike(cg_ctx* ctx, int B, const double* cl, const double* d, int d_stride, double* m2lnl,
+                          double* chi2, double* logdet, double* grad, int* status)
+{
+    if (!ctx) return CG_ERR_BAD_ARG;
+    if (B < 1 || B > ctx->max_batch || !cl || !d || !m2lnl || (d_stride != 0 && d_stride < ctx->n)) {
+        ctx->err = "bad arguments to cg_loglike";
+        return CG_ERR_BAD_ARG;
+    }
+    CG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const int L1 = ctx->lmax + 1, n = ctx->n, Bm = ctx->max_batch;
+    double* o_m2 = ctx->d_out;
+    double* o_chi2 = o_m2 + Bm;
+    double* o_ld = o_chi2 + Bm;
+    double* o_grad = o_ld + Bm;
+    double* o_d = o_grad + (size_t)Bm * L1;
+    int* o_st = (int*)(o_d + (size_t)Bm * ctx->N);
+    cudaStream_t s = ctx->stream;
+    CG_CUDA_TRY(ctx, cudaMemcpyAsync(ctx->d_cl, cl, sizeof(double) * B * L1, cudaMemcpyHostToDevice, s));
+    const int nmaps = d_stride ? B : 1;
+    if (d_stride == 0 || d_stride == n) {
+        CG_CUDA_TRY(ctx, cudaMemcpyAsync(o_d, d, sizeof(double) * (size_t)nmaps * n, cudaMemcpyHostToDevice, s));
+    } else {
+        CG_CUDA_TRY(ctx, cudaMemcpy2DAsync(o_d, sizeof(double) * n, d, sizeof(double) * d_stride, sizeof(double) * n,
+                                           nmaps, cudaMemcpyHostToDevice, s));
+    }
+    int rc = cg_loglike_device(ctx, B, ctx->d_cl, o_d, d_stride ? n : 0, o_m2, o_chi2, o_ld, grad ? o_grad : nullptr,
+                               o_st, s);
+    if (rc) return rc;
+    CG_CUDA_TRY(ctx, cudaMemcpyAsync(m2lnl, o_m2, sizeof(double) * B, cudaMemcpyDeviceToHost, s));
+    if (chi2) CG_CUDA_TRY(ctx, cudaMemcpyAsync(chi2, o_chi2, sizeof(double) * B, cudaMemcpyDeviceToHost, s));
+    if (logdet) CG_CUDA_TRY(ctx, cudaMemcpyAsync(logdet, o_ld, sizeof(double) * B, cudaMemcpyDeviceToHost, s));
+    if (grad) CG_CUDA_TRY(ctx, cudaMemcpyAsync(grad, o_grad, sizeof(double) * B * L1, cudaMemcpyDeviceToHost, s));
+    if (status) CG_CUDA_TRY(ctx, cudaMemcpyAsync(status, o_st, sizeof(int) * B, cudaMemcpyDeviceToHost, s));
+    CG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+    return CG_OK;
+}
+
+extern "C" int cg_set_reference(cg_ctx* ctx, const double* cl_ref)
+{
+    if (!ctx || !cl_ref) return CG_ERR_BAD_ARG;
+    if (ctx->precision != CG_PREC_MIXED) { ctx->err = "cg_set_reference needs a CG_PREC_MIXED context"; return CG_ERR_BAD_ARG; }
+    CG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    return cg::mixed_prepare_reference(ctx, cl_ref);
+}
+
+extern "C" int cg_reference_count(const cg_ctx* ctx) { return ctx ? ctx->wmx.ref_count : 0; }
+
+// ---- Likelihood drop-in ------------------------------------------------------
+
+struct cg_lik {
+    cg_ctx ctx;                  // device, sizes, stream and error text
+    double* A = nullptr;         // tiled C + F + N, then L, then C^-1
+    double* M = nullptr;
+    double* Dinv = nullptr;
+    double* diag = nullptr;
+    double* tmp = nullptr;       // [4][N] vectors + scalars
+    int* st = nullptr;
+    double logdet = 0;
+    std::vector<double> fg;
+};
+
+extern "C" void cg_likelihood_destroy(cg_lik* lik)
+{
+    if (!lik) return;
+    cudaSetDevice(lik->ctx.device);
+    if (lik->ctx.stream) cudaStreamSynchronize(lik->ctx.stream);
+    cudaFree(lik->A); cudaFree(lik->M); cudaFree(lik->Dinv); cudaFree(lik->diag); cudaFree(lik->tmp); cudaFree(lik->st);
+    if (lik->ctx.stream) cudaStreamDestroy(lik->ctx.stream);
+    delete lik;
+}
+
+extern "C" const char* cg_likelihood_last_error(const cg_lik* lik) { return lik ? lik->ctx.err.c_str() : g_create_error.c_str(); }
+extern "C" double cg_likelihood_logdet(const cg_lik* lik) { return lik ? lik->logdet : 0.0; }
+
+extern "C" int cg_likelihood_create(cg_lik** out, int n, const double* c_packed, const double* fid_packed,
+                                    const double* noise_packed, const double* foreground, int device)
+{
+    g_create_error.clear();
+    if (!out || n <= 0 || !c_packed || !noise_packed) { g_create_error = "bad arguments to cg_likelihood_create"; return CG_ERR_BAD_ARG; }
+    *out = nullptr;
+    std::unique_ptr<cg_lik> lik(new (std::nothrow) cg_lik());
+    if (!lik) return CG_ERR_ALLOC;
+    cg_ctx& ctx = lik->ctx;
+    std::string why;
+    if (!device_ok(device, &ctx.sm_count, why)) { g_create_error = why; return CG_ERR_NO_DEVICE; }
+    ctx.device = device;
+    ctx.n = n;
+    ctx.nt = (n + cg::TS - 1) / cg::TS;
+    ctx.N = ctx.nt * cg::TS;
+    cudaSetDevice(device);
+    if (cudaStreamCreateWithFlags(&ctx.stream, cudaStreamNonBlocking) != cudaSuccess) { g_create_error = "stream"; return CG_ERR_CUDA; }
+    const size_t np = (size_t)n * (n + 1) / 2, tiled = cg::tiled_elems(ctx.nt);
+    double* dpk = nullptr;
+    if (!dalloc(&lik->A, tiled) || !dalloc(&lik->M, tiled) || !dalloc(&lik->Dinv, (size_t)ctx.nt * cg::TILE_ELEMS) ||
+        !dalloc(&lik->diag, (size_t)ctx.N) || !dalloc(&lik->tmp, 4 * (size_t)ctx.N + 8) || !dalloc(&lik->st, 1) ||
+        !dalloc(&dpk, 3 * np)) {
+        cudaFree(dpk);
+        g_create_error = "device allocation failed";
+        cg_likelihood_destroy(lik.release());
+        return CG_ERR_ALLOC;
+    }
+    for (size_t k = 0; k < np; ++k)
+        if (!std::isfinite(c_packed[k]) || !std::isfinite(noise_packed[k]) || (fid_packed && !std::isfinite(fid_packed[k]))) {
+            cudaFree(dpk);
+            g_create_error = "non-finite matrix entry";
+            cg_likelihood_destroy(lik.release());
+            return CG_ERR_NONFINITE;
+        }
+    cudaStream_t s = ctx.stream;
+    cudaMemcpyAsync(dpk, c_packed, sizeof(double) * np, cudaMemcpyHostToDevice, s);
+    if (fid_packed) cudaMemcpyAsync(dpk + np, fid_packed, sizeof(double) * np, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(dpk + 2 * np, noise_packed, sizeof(double) * np, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(lik->st, 0, sizeof(int), s);
+    cg::fp64_packed_to_tiled(n, ctx.nt, dpk, fid_packed ? dpk + np : nullptr, dpk + 2 * np, lik->A, s);
+    int rc = cg::tiled_cholesky<double>(&ctx, 1, ctx.nt, lik->A, lik->Dinv, lik->diag, lik->st, tiled, s);
+    if (!rc) {
+        cg::fp64_logdet(1, n, ctx.N, lik->diag, lik->tmp + 4 * (size_t)ctx.N, s);
+        rc = cg::tiled_trtri<double>(&ctx, 1, ctx.nt, lik->A, lik->Dinv, lik->M, tiled, s);
+    }
+    if (!rc) rc = cg::tiled_lauum<double>(&ctx, 1, ctx.nt, lik->M, lik->A, tiled, s);
+    int st = 0;
+    if (!rc) {
+        cudaMemcpyAsync(&lik->logdet, lik->tmp + 4 * (size_t)ctx.N, sizeof(double), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(&st, lik->st, sizeof(int), cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) { ctx.err = cudaGetErrorString(e); rc = CG_ERR_CUDA; }
+    }
+    cudaFree(dpk);
+    if (!rc && st) {
+        // source/likelihood.cpp:120-125: "The covariance matrix must be positive definite."
+        ctx.err = "The covariance matrix is not positive definite.";
+        rc = CG_ERR_NOT_PD;
+    }
+    if (rc) {
+        g_create_error = ctx.err;
+        cg_likelihood_destroy(lik.release());
+        return rc;
+    }
+    if (foreground) lik->fg.assign(foreground, foreground + n);
+    *out = lik.release();
+    return CG_OK;
+}
+
+extern "C" int cg_likelihood_calculate(cg_lik* lik, const double* t, double* chi2, double* logdet)
+{
+    if (!lik || !t || !chi2 || !logdet) return CG_ERR_BAD_ARG;
+    cg_ctx& ctx = lik->ctx;
+    const int n = ctx.n, N = ctx.N;
+    for (int i = 0; i < n; ++i)
+        if (!std::isfinite(t[i])) { ctx.err = "non-finite map value"; return CG_ERR_NONFINITE; }
+    CG_CUDA_TRY(&ctx, cudaSetDevice(ctx.device));
+    cudaStream_t s = ctx.stream;
+    double* tv = lik->tmp;          // padded t
+    double* ta = tv + N;            // C^-1 t
+    double* fv = ta + N;            // padded f
+    double* fa = fv + N;            // C^-1 f
+    double* sc = fa + N;            // scalars
+    cudaMemsetAsync(tv, 0, sizeof(double) * 4 * N, s);
+    cudaMemcpyAsync(tv, t, sizeof(double) * n, cudaMemcpyHostToDevice, s);
+    cg::fp64_symv(1, ctx.nt, N, lik->A, tv, ta, s);
+    cg::fp64_dot(n, tv, ta, sc + 1, s);  // chi2 = t^T C^-1 t (Likelihood::vmv, source/likelihood.cpp:137-152)
+    const bool fgm = !lik->fg.empty();
+    if (fgm) {
+        cudaMemcpyAsync(fv, lik->fg.data(), sizeof(double) * n, cudaMemcpyHostToDevice, s);
+        cg::fp64_symv(1, ctx.nt, N, lik->A, fv, fa, s);
+        cg::fp64_dot(n, tv, fa, sc + 2, s);
+        cg::fp64_dot(n, fv, fa, sc + 3, s);
+    }
+    double h[4] = {0, 0, 0, 0};
+    cudaMemcpyAsync(h, sc, sizeof(double) * 4, cudaMemcpyDeviceToHost, s);
+    CG_CUDA_TRY(&ctx, cudaStreamSynchronize(s));
+    *chi2 = h[1];
+    *logdet = lik->logdet;
+    if (fgm) {
+        // foreground marginalisation, source/likelihood.cpp:171-177
+        const double tCinvf = h[2], fCinvf = h[3];
+        *logdet += std::log(fCinvf / n);
+        *chi2 -= tCinvf * tCinvf / fCinvf;
+    }
+    return CG_OK;
+}

@@ -1,0 +1,161 @@
+// Internal declarations shared by the cosmopp_gb300 translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/cosmopp_gb300.h"
+
+namespace cg {
+
+// ---- tiled symmetric layout ---------------------------------------------
+// An N x N symmetric matrix (N = nt * TS) is kept as its lower-triangular
+// tiles: tile (I, J), J <= I, at tile index I(I+1)/2 + J, each tile TS x TS
+// column-major (element (r, c) at r + c*TS).  Padding rows/columns n..N-1 hold
+// the identity, which changes neither ln det nor any solve.
+constexpr int TS = 64;
+constexpr int TILE_ELEMS = TS * TS;
+
+__host__ __device__ inline int tile_index(int I, int J) { return I * (I + 1) / 2 + J; }
+__host__ __device__ inline int ntiles_lower(int nt) { return nt * (nt + 1) / 2; }
+inline size_t tiled_elems(int nt) { return (size_t)ntiles_lower(nt) * TILE_ELEMS; }
+
+// inverse of tile_index for the lower triangle: t -> (I, J)
+__host__ __device__ inline void tile_coords(int t, int& I, int& J)
+{
+    int i = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+    while (i * (i + 1) / 2 > t) --i;
+    while ((i + 1) * (i + 2) / 2 <= t) ++i;
+    I = i;
+    J = t - i * (i + 1) / 2;
+}
+
+// ---- constants uploaded per context --------------------------------------
+struct LegConsts {
+    // Bonnet recurrence coefficients exactly as include/legendre.hpp:34 forms
+    // them: a_l = 2 - 1.0/l, b_l = 1 - 1.0/l
+    std::vector<double> a, b;
+    std::vector<double> beam;   // B_l (pixel window x beam), source/utils.cpp:149-158
+};
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+// ---- plain FP64 path workspace -------------------------------------------
+struct Fp64Work {
+    int cap = 0;                 // batch capacity
+    double* A = nullptr;         // [cap][tiled]  C, then L, then C^-1
+    double* M = nullptr;         // [cap][tiled]  L^-1
+    double* Dinv = nullptr;      // [cap][nt][TS*TS] inverses of the diagonal L tiles
+    double* diag = nullptr;      // [cap][N] diagonal of L
+    double* clc = nullptr;       // [cap][lmax+1] cl_l (2l+1)/(4 pi)
+    double* dvec = nullptr;      // [cap][N] data maps (padded)
+    double* alpha = nullptr;     // [cap][N]
+    double* gpart = nullptr;     // [cap][nblk][lmax+1] adjoint partial sums
+    int* st = nullptr;           // [cap] status
+    double* ld = nullptr;        // [cap] ln det
+};
+
+// ---- mixed path workspace ------------------------------------------------
+struct MixedWork {
+    int cap = 0;
+    bool have_ref = false;
+    std::vector<double> cl_ref;  // current reference C_l (host copy)
+    int ref_count = 0;
+    int lpad = 0;                // l extent of the table rows (lmax + 1 rounded up to 16)
+    // reference point, FP64
+    double* Lref = nullptr;      // [tiled] Cholesky factor of C_ref
+    double* Mref = nullptr;      // [tiled] L_ref^-1
+    double* Dinv_ref = nullptr;  // [nt][TS*TS]
+    double* diag_ref = nullptr;  // [N]
+    double* cref = nullptr;      // [lmax+1] reference C_l on the device
+    double* ldref = nullptr;     // [1] ln det C_ref
+    double* Y = nullptr;         // [nharm_pad][N] real spherical harmonics x B_l at the pixels
+    double* Z = nullptr;         // [nharm_pad][N] L_ref^-1 Y
+    float* U = nullptr;          // [tiles][TS*TS][lpad] whitened Legendre table
+    // per batch element
+    float* A = nullptr;          // [cap][tiled] I + K_b, then L_b, then V_b = (I + K_b)^-1
+    float* Acopy = nullptr;      // [cap][tiled] I + K_b kept for the refinement residual
+    float* M = nullptr;          // [cap][tiled] L_b^-1
+    float* Dinv = nullptr;       // [cap][nt][TS*TS]
+    float* diag = nullptr;       // [cap][N]
+    float* eps = nullptr;        // [cap][lpad] C_l / Cref_l - 1
+    double* y = nullptr;         // [cap][N] L_ref^-1 d
+    double* x = nullptr;         // [cap][N] (I+K)^-1 y
+    double* r = nullptr;         // [cap][N] refinement residual
+    double* part = nullptr;      // [cap][tiles][2][TS] matvec partials
+    float* gpart = nullptr;      // [tiles][cap][lpad] adjoint partials
+    double* ld = nullptr;        // [cap] ln det C_b
+    int* st = nullptr;           // [cap]
+};
+
+}  // namespace cg
+
+struct cg_ctx {
+    int device = 0;
+    int n = 0, nt = 0, N = 0;    // kept pixels, tiles per side, padded size
+    int lmax = 0;
+    int max_batch = 1;
+    int precision = CG_PREC_FP64;
+    int recenter = CG_RECENTER_AUTO;
+    double recenter_radius = 1.0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    std::vector<double> xyz;     // [n][3]
+    std::vector<double> noise;   // [n]
+    cg::LegConsts leg;
+    double* d_xyz = nullptr;     // [3][N] SoA, padding rows = 0
+    double* d_noise = nullptr;   // [N]
+    double* d_lega = nullptr;    // [lmax+1]
+    double* d_legb = nullptr;
+    double* d_beam = nullptr;
+    double* d_cl = nullptr;      // staging [max_batch][lmax+1]
+    double* d_out = nullptr;     // staging for outputs
+    size_t d_out_bytes = 0;
+    cg::Fp64Work w64;
+    cg::MixedWork wmx;
+    std::string err;
+};
+
+// helpers shared by the translation units
+#define CG_CUDA_TRY(ctx, expr)                                                           \
+    do {                                                                                 \
+        cudaError_t e_ = (expr);                                                         \
+        if (e_ != cudaSuccess) {                                                         \
+            (ctx)->err = std::string(#expr) + ": " + cudaGetErrorString(e_);            \
+            return CG_ERR_CUDA;                                                          \
+        }                                                                                \
+    } while (0)
+
+namespace cg {
+// plain FP64 path (k_fp64.cu)
+int fp64_ensure(cg_ctx* ctx, int B);
+int fp64_build_tiled(cg_ctx* ctx, int B, const double* d_cl, bool add_noise, cudaStream_t s);
+int fp64_build_tiled_into(cg_ctx* ctx, int B, const double* d_cl, bool add_noise, double* A, cudaStream_t s);
+int fp64_build_packed(cg_ctx* ctx, int B, const double* d_cl, double* d_out, cudaStream_t s);
+int fp64_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* d_d, int d_stride, double* d_m2lnl,
+                 double* d_chi2, double* d_logdet, double* d_grad, int* d_status, cudaStream_t s);
+// generic tiled FP64 / FP32 factorisation entry points (k_chol.cu)
+template <typename T>
+int tiled_cholesky(cg_ctx* ctx, int B, int nt, T* A, T* Dinv, T* diag, int* status, size_t strideA, cudaStream_t s);
+template <typename T>
+int tiled_trtri(cg_ctx* ctx, int B, int nt, const T* L, const T* Dinv, T* M, size_t strideA, cudaStream_t s);
+template <typename T>
+int tiled_lauum(cg_ctx* ctx, int B, int nt, const T* M, T* V, size_t strideA, cudaStream_t s);
+// mixed path (k_mixed.cu)
+int mixed_prepare_reference(cg_ctx* ctx, const double* cl_ref_host);
+int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, const double* d_d, int d_stride,
+                  double* d_m2lnl, double* d_chi2, double* d_logdet, double* d_grad, int* d_status, cudaStream_t s);
+void mixed_free(cg_ctx* ctx);
+void fp64_free(cg_ctx* ctx);
+// small FP64 launchers used by the Likelihood drop-in (k_fp64.cu)
+void fp64_packed_to_tiled(int n, int nt, const double* c, const double* f, const double* nz, double* A, cudaStream_t s);
+void fp64_symv(int B, int nt, int N, const double* V, const double* dv, double* alpha, cudaStream_t s);
+void fp64_logdet(int B, int n, int N, const double* diag, double* out, cudaStream_t s);
+void fp64_dot(int n, const double* a, const double* b, double* out, cudaStream_t s);
+}  // namespace cg

@@ -1,0 +1,125 @@
+// Shared 64x64 tile helpers for the tiled kernels (k_chol.cu, k_mixed.cu).
+// A tile in global memory is column-major, element (r, c) at r + TS*c; in
+// shared memory an operand is kept as s[m * SmemLd + row] so that a 256-thread
+// block can run 4x4 register micro-tiles over the m (reduction) index.
+#pragma once
+
+#include "cg_internal.h"
+
+namespace cg {
+namespace tile {
+
+constexpr int NT_THREADS = 256;
+
+// smem tile stored as s[m * SLD + row]
+template <typename T>
+struct SmemLd {
+    static constexpr int v = TS + (sizeof(T) == 4 ? 4 : 2);
+};
+
+// sX[m][r] = G(r, m) with G column-major (r + TS*m): contiguous copy
+template <typename T>
+__device__ __forceinline__ void load_direct(T* s, const T* __restrict__ g)
+{
+    constexpr int L = SmemLd<T>::v;
+    for (int e = threadIdx.x; e < TILE_ELEMS; e += blockDim.x) {
+        const int r = e % TS, m = e / TS;
+        s[m * L + r] = g[e];
+    }
+}
+
+// sX[m][r] = G(m, r): transposed copy
+template <typename T>
+__device__ __forceinline__ void load_trans(T* s, const T* __restrict__ g)
+{
+    constexpr int L = SmemLd<T>::v;
+    for (int e = threadIdx.x; e < TILE_ELEMS; e += blockDim.x) {
+        const int m = e % TS, r = e / TS;  // G(m, r) at m + TS*r = e
+        s[m * L + r] = g[e];
+    }
+}
+
+// acc(r0+a, c0+b) += sum_m X(r0+a, m) Y(c0+b, m), sX[m][r], sY[m][c]
+template <typename T>
+__device__ __forceinline__ void tile_mma(const T* sX, const T* sY, T acc[4][4], int r0, int c0)
+{
+    constexpr int L = SmemLd<T>::v;
+#pragma unroll 8
+    for (int m = 0; m < TS; ++m) {
+        T x[4], y[4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a) x[a] = sX[m * L + r0 + a];
+#pragma unroll
+        for (int b = 0; b < 4; ++b) y[b] = sY[m * L + c0 + b];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) acc[a][b] = fma(x[a], y[b], acc[a][b]);
+    }
+}
+
+__device__ __forceinline__ void micro_coords(int& r0, int& c0)
+{
+    r0 = (threadIdx.x % 16) * 4;
+    c0 = (threadIdx.x / 16) * 4;
+}
+
+}  // namespace tile
+}  // namespace cg
+
+namespace cg {
+namespace tile {
+
+// Symmetric matvec on the tiled lower storage, two deterministic passes:
+// symv_partials: per lower tile (I, J): part[t][0][r] = (V_IJ v_J)[r],
+//                part[t][1][c] = (V_IJ^T v_I)[c] (I != J);
+// symv_reduce:   out_I = sum_J (row-I pieces) in a fixed order.
+template <typename T>
+__global__ void __launch_bounds__(256) symv_partials(int nt, const T* __restrict__ V, size_t strideA,
+                                                     const double* __restrict__ v, int vstride,
+                                                     double* __restrict__ part)
+{
+    __shared__ T s[TS][TS + 1];
+    __shared__ double sv[2][TS];
+    __shared__ double red[4][2][TS];
+    int I, J;
+    tile_coords(blockIdx.x, I, J);
+    const int b = blockIdx.y, ntile = ntiles_lower(nt);
+    const T* tile = V + (size_t)b * strideA + (size_t)blockIdx.x * TILE_ELEMS;
+    for (int e = threadIdx.x; e < TILE_ELEMS; e += blockDim.x) s[e / TS][e % TS] = tile[e];  // s[c][r]
+    if (threadIdx.x < TS) {
+        sv[0][threadIdx.x] = v[(size_t)b * vstride + J * TS + threadIdx.x];
+        sv[1][threadIdx.x] = v[(size_t)b * vstride + I * TS + threadIdx.x];
+    }
+    __syncthreads();
+    const int r = threadIdx.x % TS, q = threadIdx.x / TS;
+    double a = 0.0, t = 0.0;
+    for (int c = q; c < TS; c += 4) {
+        a += (double)s[c][r] * sv[0][c];  // (V v_J)[r]
+        t += (double)s[r][c] * sv[1][c];  // (V^T v_I)[r] = sum_c V(c, r) v_I[c]
+    }
+    red[q][0][r] = a;
+    red[q][1][r] = t;
+    __syncthreads();
+    if (q == 0) {
+        double* p = part + ((size_t)b * ntile + blockIdx.x) * 2 * TS;
+        p[r] = ((red[0][0][r] + red[1][0][r]) + red[2][0][r]) + red[3][0][r];
+        p[TS + r] = (I != J) ? ((red[0][1][r] + red[1][1][r]) + red[2][1][r]) + red[3][1][r] : 0.0;
+    }
+}
+
+// out[b][I*TS + r] = scale_out * sum + add[b][..] (add nullable)
+static __global__ void __launch_bounds__(64) symv_reduce(int nt, const double* __restrict__ part, double* __restrict__ out,
+                                                  int ostride, const double* __restrict__ add, double sign)
+{
+    const int I = blockIdx.x, b = blockIdx.y, r = threadIdx.x, ntile = ntiles_lower(nt);
+    const double* pb = part + (size_t)b * ntile * 2 * TS;
+    double s = 0.0;
+    for (int J = 0; J <= I; ++J) s += pb[(size_t)tile_index(I, J) * 2 * TS + r];
+    for (int J = I + 1; J < nt; ++J) s += pb[(size_t)tile_index(J, I) * 2 * TS + TS + r];
+    const size_t o = (size_t)b * ostride + I * TS + r;
+    out[o] = (add ? add[o] : 0.0) + sign * s;
+}
+
+}  // namespace tile
+}  // namespace cg

@@ -1,0 +1,625 @@
+// Batched mixed-precision path: -2lnL and d(-2lnL)/dC_l for many C_l vectors.
+//
+// The reference evaluates one C_l at a time: clToCMatrix, then Likelihood's
+// dpptrf/dpptri in FP64 (source/c_matrix_generator.cpp:164-232,
+// source/likelihood.cpp:69-180).  On GB300 FP64 runs at ~1/64 of FP32, so
+// this path keeps FP64 only where the ill-conditioning of C needs it:
+//
+//   reference point (FP64, once per re-centre):
+//     Cref = C(cl_ref) + N = Lref Lref^T,  Mref = Lref^-1,  ln det Cref
+//     Y    = real spherical harmonics x B_l at the pixels (sum_m Y_lm Y_lm^T
+//            = (2l+1)/(4pi) B_l^2 P_l(x), the addition theorem)
+//     Z    = Mref Y,  Ubar_l = cref_l Z_l Z_l^T   (whitened Legendre table,
+//            stored FP32 as [tile][entry][l])
+//     y    = Mref d
+//   per batch element b (FP32 O(n^3), FP64 accumulations):
+//     eps_bl = C_bl / cref_l - 1
+//     A_b = I + K_b,  K_b = sum_l eps_bl Ubar_l   (= Lref^-1 (C_b - Cref) Lref^-T)
+//         -- the [pairs x l] x [l x batch] contraction
+//     A_b = L_b L_b^T (FP32), V_b = A_b^-1 (FP32)
+//     ln det C_b = ln det Cref + 2 sum ln diag(L_b)           (FP64 sum)
+//     x_b = V_b y, one refinement step r = y - A_b x_b, x_b += V_b r (FP64)
+//     chi2_b = y^T x_b
+//     d(-2lnL)/dC_l = sum_ij (V_b - x_b x_b^T)_ij Ubar_l,ij / cref_l
+//         -- the transposed contraction against the same table.
+// A_b is well conditioned (eigenvalues in [min_l C_bl/cref_l, max_l C_bl/cref_l]),
+// which is what makes FP32 factors accurate to ~1e-6 in -2lnL.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "cg_internal.h"
+#include "cg_tile.cuh"
+
+namespace cg {
+
+using namespace tile;
+
+namespace {
+
+constexpr double kPi = 3.141592653589793;
+
+inline int lpad_of(int lmax) { return ((lmax + 1 + 15) / 16) * 16; }
+inline int nharm_of(int lmax) { return (lmax + 1) * (lmax + 1) - 4; }  // l = 2..lmax
+inline int nharm_pad(int lmax) { return ((nharm_of(lmax) + TS - 1) / TS) * TS; }
+
+// Real orthonormal spherical harmonics times B_l at every pixel, rows h =
+// (l^2 - 4) + {0: m=0, 2m-1: cos, 2m: sin}; normalised associated Legendre
+// functions by the standard three-term recurrence in l at fixed m.
+__global__ void ylm_basis(int n, int N, int lmax, const double* __restrict__ xyz, const double* __restrict__ beam,
+                          double* __restrict__ Y)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int m = blockIdx.y;
+    if (i >= N) return;
+    const bool real = i < n;
+    double x = 0, sth = 0, phi = 0;
+    if (real) {
+        const double px = xyz[i], py = xyz[N + i], pz = xyz[2 * N + i];
+        x = pz;
+        sth = sqrt(px * px + py * py);
+        phi = atan2(py, px);
+    }
+    double pmm = 1.0 / sqrt(4.0 * kPi);  // Pbar_0^0
+    for (int k = 1; k <= m; ++k) pmm *= -sqrt((2.0 * k + 1.0) / (2.0 * k)) * sth;
+    double sm, cm;
+    sincos((double)m * phi, &sm, &cm);
+    const double fac = (m == 0) ? 1.0 : sqrt(2.0);
+    double p2 = 0.0, p1 = pmm;  // P_{l-2}, P_{l-1}
+    for (int l = m; l <= lmax; ++l) {
+        double p;
+        if (l == m) p = pmm;
+        else if (l == m + 1) p = sqrt(2.0 * m + 3.0) * x * pmm;
+        else {
+            const double a = sqrt((4.0 * l * l - 1.0) / ((double)l * l - (double)m * m));
+            const double bb = sqrt(((double)(l - 1) * (l - 1) - (double)m * m) / (4.0 * (l - 1) * (l - 1) - 1.0));
+            p = a * (x * p1 - bb * p2);
+        }
+        if (l > m) { p2 = p1; p1 = p; }
+        if (l >= 2) {
+            const int base = l * l - 4;
+            const double v = real ? fac * p * beam[l] : 0.0;
+            if (m == 0) Y[(size_t)base * N + i] = v;
+            else {
+                Y[(size_t)(base + 2 * m - 1) * N + i] = v * cm;
+                Y[(size_t)(base + 2 * m) * N + i] = v * sm;
+            }
+        }
+    }
+}
+
+// Z[h][I-block] = sum_{J <= I} Mref_IJ Y[h][J-block]; grid (nt, nharm_pad / TS)
+__global__ void __launch_bounds__(256) whiten_basis(int nt, int N, const double* __restrict__ Mref,
+                                                    const double* __restrict__ Y, double* __restrict__ Z)
+{
+    extern __shared__ unsigned char smem_raw[];
+    constexpr int L = SmemLd<double>::v;
+    double* sX = reinterpret_cast<double*>(smem_raw);
+    double* sY = sX + TS * L;
+    const int I = blockIdx.x, H = blockIdx.y;
+    int r0, c0;
+    micro_coords(r0, c0);
+    double acc[4][4] = {};
+    for (int J = 0; J <= I; ++J) {
+        load_direct(sX, Mref + (size_t)tile_index(I, J) * TILE_ELEMS);
+        for (int e = threadIdx.x; e < TILE_ELEMS; e += blockDim.x) {
+            const int m = e % TS, c = e / TS;  // sY[m][c] = Y[H*TS + c][J*TS + m]
+            sY[m * L + c] = Y[(size_t)(H * TS + c) * N + J * TS + m];
+        }
+        __syncthreads();
+        tile_mma(sX, sY, acc, r0, c0);
+        __syncthreads();
+    }
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) Z[(size_t)(H * TS + c0 + q) * N + I * TS + r0 + a] = acc[a][q];
+}
+
+// Ubar[t][e][l] = cref_l sum_{h in l} Z[h][i] Z[h][j] (FP64 sums, FP32 store);
+// grid (tiles, TS / CC): each block covers CC columns (CC*TS entries) of one tile.
+template <int CC>
+__global__ void __launch_bounds__(256) build_ubar(int N, int lmax, int lp, const double* __restrict__ Z,
+                                                  const double* __restrict__ cref, float* __restrict__ U)
+{
+    extern __shared__ unsigned char smem_raw[];
+    constexpr int HB = 32;                                   // harmonics per sub-batch
+    double* zi = reinterpret_cast<double*>(smem_raw);        // [HB][TS]
+    double* zj = zi + HB * TS;                               // [HB][CC]
+    float* out = reinterpret_cast<float*>(zj + HB * CC);     // [CC*TS][lp]
+    int I, J;
+    tile_coords(blockIdx.x, I, J);
+    const int c_begin = blockIdx.y * CC;
+    constexpr int NE = CC * TS;                              // entries in this block
+    constexpr int PER = NE / 256;                            // entries per thread
+    for (int k = threadIdx.x; k < NE * lp; k += blockDim.x) out[k] = 0.f;
+    __syncthreads();
+    for (int l = 2; l <= lmax; ++l) {
+        const int h0 = l * l - 4, h1 = (l + 1) * (l + 1) - 4;
+        double acc[PER];
+#pragma unroll
+        for (int p = 0; p < PER; ++p) acc[p] = 0.0;
+        for (int hb = h0; hb < h1; hb += HB) {
+            const int nh = min(HB, h1 - hb);
+            for (int k = threadIdx.x; k < nh * TS; k += blockDim.x)
+                zi[k] = Z[(size_t)(hb + k / TS) * N + I * TS + k % TS];
+            for (int k = threadIdx.x; k < nh * CC; k += blockDim.x)
+                zj[k] = Z[(size_t)(hb + k / CC) * N + J * TS + c_begin + k % CC];
+            __syncthreads();
+#pragma unroll
+            for (int p = 0; p < PER; ++p) {
+                const int e = threadIdx.x + 256 * p;  // e = r + TS * cc
+                const int r = e % TS, cc = e / TS;
+                double s = acc[p];
+                for (int h = 0; h < nh; ++h) s += zi[h * TS + r] * zj[h * CC + cc];
+                acc[p] = s;
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int p = 0; p < PER; ++p) out[(threadIdx.x + 256 * p) * lp + l] = (float)(cref[l] * acc[p]);
+    }
+    __syncthreads();
+    float* dst = U + ((size_t)blockIdx.x * TILE_ELEMS + (size_t)c_begin * TS) * lp;
+    for (int k = threadIdx.x; k < NE * lp; k += blockDim.x) dst[k] = out[k];
+}
+
+// y[b][I-block] = sum_{J <= I} Mref_IJ d_b[J-block]; grid (nt, maps), 256 threads
+__global__ void __launch_bounds__(256) trmv_lower(int nt, int n, int N, const double* __restrict__ M,
+                                                  const double* __restrict__ d, int d_stride,
+                                                  double* __restrict__ y)
+{
+    __shared__ double part[4][TS];
+    const int I = blockIdx.x, b = blockIdx.y;
+    const int r = threadIdx.x % TS, q = threadIdx.x / TS;
+    const double* db = d + (size_t)b * d_stride;
+    double s = 0.0;
+    for (int J = 0; J <= I; ++J) {
+        const double* t = M + (size_t)tile_index(I, J) * TILE_ELEMS;
+        for (int c = q; c < TS; c += 4) {
+            const int j = J * TS + c;
+            if (j < n) s += t[r + TS * c] * db[j];
+        }
+    }
+    part[q][r] = s;
+    __syncthreads();
+    if (q == 0) y[(size_t)b * N + I * TS + r] = ((part[0][r] + part[1][r]) + part[2][r]) + part[3][r];
+}
+
+// eps[b][l] = C_bl / cref_l - 1 (0 for l < 2 and padding)
+__global__ void make_eps(int B, int lmax, int lp, const double* __restrict__ cl, const double* __restrict__ cref,
+                         float* __restrict__ eps)
+{
+    const int b = blockIdx.x;
+    for (int l = threadIdx.x; l < lp; l += blockDim.x) {
+        float v = 0.f;
+        if (l >= 2 && l <= lmax) {
+            const double c = cl[(size_t)b * (lmax + 1) + l];
+            v = (float)(c / cref[l] - 1.0);
+        }
+        eps[(size_t)b * lp + l] = v;
+    }
+}
+
+__global__ void init_status(int B, const double* __restrict__ cl, int lmax, int* __restrict__ status)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= B) return;
+    int st = CG_OK;
+    for (int l = 0; l <= lmax; ++l)
+        if (!isfinite(cl[(size_t)b * (lmax + 1) + l])) st = CG_ERR_NONFINITE;
+    status[b] = st;
+}
+
+// Forward contraction: A_b[t][e] = [e on the diagonal] + sum_l Ubar[t][e][l] eps[b][l],
+// written to A (factorised in place) and Acopy (kept for the refinement residual).
+// grid (tiles * TILE_ELEMS / 128, ceil(B / 128)); 256 threads, 8 entries x 8 batch each.
+__global__ void __launch_bounds__(256) contract_fwd(int B, int lp, const float* __restrict__ U,
+                                                    const float* __restrict__ eps, float* __restrict__ A,
+                                                    float* __restrict__ Acopy, size_t strideA)
+{
+    extern __shared__ float fsm[];
+    float* sU = fsm;             // [lp][128]
+    float* sE = fsm + lp * 128;  // [lp][128]
+    const size_t e_begin = (size_t)blockIdx.x * 128;  // global entry index over all tiles
+    const int b_begin = blockIdx.y * 128;
+    const float* ublk = U + e_begin * lp;
+    for (int k = threadIdx.x; k < 128 * lp; k += 256) {
+        const int e = k % 128, l = k / 128;  // e fastest: conflict-free smem stores
+        sU[l * 128 + e] = ublk[(size_t)e * lp + l];
+        const int bb = b_begin + e;
+        sE[l * 128 + e] = (bb < B) ? eps[(size_t)bb * lp + l] : 0.f;
+    }
+    __syncthreads();
+    const int te = threadIdx.x % 16, tb = threadIdx.x / 16;
+    const int e0 = te * 8, b0 = tb * 8;
+    float acc[8][8];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) acc[a][q] = 0.f;
+    for (int l = 0; l < lp; ++l) {
+        const float4 u0 = *reinterpret_cast<const float4*>(&sU[l * 128 + e0]);
+        const float4 u1 = *reinterpret_cast<const float4*>(&sU[l * 128 + e0 + 4]);
+        const float4 w0 = *reinterpret_cast<const float4*>(&sE[l * 128 + b0]);
+        const float4 w1 = *reinterpret_cast<const float4*>(&sE[l * 128 + b0 + 4]);
+        const float u[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+        const float w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int q = 0; q < 8; ++q) acc[a][q] = fmaf(u[a], w[q], acc[a][q]);
+    }
+    const size_t tile_id = e_begin / TILE_ELEMS;
+    int I, J;
+    tile_coords((int)tile_id, I, J);
+    const int ein = (int)(e_begin % TILE_ELEMS) + e0;  // entry offset within the tile
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        const int bb = b_begin + b0 + q;
+        if (bb >= B) continue;
+        float v[8];
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+            const int e = ein + a;
+            const bool dg = (I == J) && (e % TS == e / TS);
+            v[a] = acc[a][q] + (dg ? 1.f : 0.f);
+        }
+        const size_t off = (size_t)bb * strideA + e_begin + e0;
+        float4* pa = reinterpret_cast<float4*>(A + off);
+        float4* pc = reinterpret_cast<float4*>(Acopy + off);
+        const float4 v0 = make_float4(v[0], v[1], v[2], v[3]), v1 = make_float4(v[4], v[5], v[6], v[7]);
+        pa[0] = v0; pa[1] = v1;
+        pc[0] = v0; pc[1] = v1;
+    }
+}
+
+// ln det C_b = ln det Cref + 2 sum ln diag(L_b), FP64 sums; grid B
+__global__ void __launch_bounds__(256) logdet_mixed(int n, int N, const float* __restrict__ diag,
+                                                    const double* __restrict__ logdet_ref, double* __restrict__ out)
+{
+    __shared__ double red[256];
+    const int b = blockIdx.x;
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += 256) s += log((double)diag[(size_t)b * N + i]);
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[b] = *logdet_ref + 2.0 * red[0];
+}
+
+// chi2_b = y_b . x_b, m2lnl_b = chi2_b + logdet_b; grid B
+__global__ void __launch_bounds__(256) chi2_mixed(int n, int N, int ystride, const double* __restrict__ y,
+                                                  const double* __restrict__ x, const double* __restrict__ logdet,
+                                                  double* __restrict__ m2lnl, double* __restrict__ chi2,
+                                                  double* __restrict__ logdet_out)
+{
+    __shared__ double red[256];
+    const int b = blockIdx.x;
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += 256) s += y[(size_t)b * ystride + i] * x[(size_t)b * N + i];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        if (chi2) chi2[b] = red[0];
+        if (logdet_out) logdet_out[b] = logdet[b];
+        m2lnl[b] = red[0] + logdet[b];
+    }
+}
+
+// broadcast y (one map) to every batch element: yb[b][i] = y[i]
+__global__ void broadcast_vec(int B, int N, const double* __restrict__ y, double* __restrict__ yb)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x, b = blockIdx.y;
+    if (i < N && b < B) yb[(size_t)b * N + i] = y[i];
+}
+
+// Adjoint contraction partials: part[t][b][l] = sum_{e in tile t (lower)} w_e W_b[t][e] Ubar[t][e][l],
+// W_b = V_b - x_b x_b^T; grid (tiles, ceil(B / 64)); thread -> 4 batch x 3 l.
+__global__ void __launch_bounds__(256) contract_adj(int B, int N, int lp, const float* __restrict__ U,
+                                                    const float* __restrict__ V, size_t strideA,
+                                                    const double* __restrict__ x, float* __restrict__ part)
+{
+    extern __shared__ float asm_[];
+    float (*sU)[49] = reinterpret_cast<float (*)[49]>(asm_);              // [entry][l], 48 l per pass
+    float (*sW)[65] = reinterpret_cast<float (*)[65]>(asm_ + 64 * 49);    // [b][entry]
+    float (*sxi)[64] = reinterpret_cast<float (*)[64]>(asm_ + 64 * 49 + 64 * 65);
+    float (*sxj)[64] = reinterpret_cast<float (*)[64]>(asm_ + 64 * 49 + 64 * 65 + 64 * 64);  // x_b at rows / cols
+    const int t = blockIdx.x, b_begin = blockIdx.y * 64;
+    int I, J;
+    tile_coords(t, I, J);
+    for (int k = threadIdx.x; k < 64 * 64; k += 256) {
+        const int bb = k / 64, r = k % 64, b = b_begin + bb;
+        sxi[bb][r] = (b < B) ? (float)x[(size_t)b * N + I * TS + r] : 0.f;
+        sxj[bb][r] = (b < B) ? (float)x[(size_t)b * N + J * TS + r] : 0.f;
+    }
+    const int tb = threadIdx.x / 16, tl = threadIdx.x % 16;  // b0 = 4 tb, l0 = 3 tl
+    for (int lbase = 0; lbase < lp; lbase += 48) {
+        float acc[4][3] = {};
+        for (int e0 = 0; e0 < TILE_ELEMS; e0 += 64) {
+            __syncthreads();
+            for (int k = threadIdx.x; k < 64 * 48; k += 256) {
+                const int e = k / 48, l = k % 48;
+                sU[e][l] = (lbase + l < lp) ? U[((size_t)t * TILE_ELEMS + e0 + e) * lp + lbase + l] : 0.f;
+            }
+            for (int k = threadIdx.x; k < 64 * 64; k += 256) {
+                const int bb = k / 64, e = k % 64, b = b_begin + bb;
+                const int ee = e0 + e, r = ee % TS, c = ee / TS;
+                float w = 0.f;
+                if (b < B && (I != J || r >= c)) {
+                    const float wt = (I == J && r == c) ? 1.f : 2.f;
+                    w = wt * (V[(size_t)b * strideA + (size_t)t * TILE_ELEMS + ee] - sxi[bb][r] * sxj[bb][c]);
+                }
+                sW[bb][e] = w;
+            }
+            __syncthreads();
+#pragma unroll 4
+            for (int e = 0; e < 64; ++e) {
+                float u[3], w[4];
+#pragma unroll
+                for (int q = 0; q < 3; ++q) u[q] = sU[e][tl * 3 + q];
+#pragma unroll
+                for (int a = 0; a < 4; ++a) w[a] = sW[tb * 4 + a][e];
+#pragma unroll
+                for (int a = 0; a < 4; ++a)
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) acc[a][q] = fmaf(w[a], u[q], acc[a][q]);
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int b = b_begin + tb * 4 + a;
+            if (b >= B) continue;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                const int l = lbase + tl * 3 + q;
+                if (l < lp) part[((size_t)t * B + b) * lp + l] = acc[a][q];
+            }
+        }
+    }
+}
+
+// grad[b][l] = (sum_t part[t][b][l]) / cref_l, FP64 in tile order; grid B
+__global__ void adj_finish(int B, int ntile, int lmax, int lp, const float* __restrict__ part,
+                           const double* __restrict__ cref, double* __restrict__ grad)
+{
+    const int b = blockIdx.x;
+    for (int l = threadIdx.x; l <= lmax; l += blockDim.x) {
+        double s = 0.0;
+        if (l >= 2)
+            for (int t = 0; t < ntile; ++t) s += (double)part[((size_t)t * B + b) * lp + l];
+        grad[(size_t)b * (lmax + 1) + l] = (l >= 2) ? s / cref[l] : 0.0;
+    }
+}
+
+template <typename T>
+int dalloc(cg_ctx* ctx, T** p, size_t count)
+{
+    if (cudaMalloc((void**)p, sizeof(T) * std::max<size_t>(count, 1)) != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        ctx->err = "device allocation failed (mixed path workspace)";
+        return CG_ERR_ALLOC;
+    }
+    return CG_OK;
+}
+
+}  // namespace
+
+void mixed_free(cg_ctx* ctx)
+{
+    MixedWork& w = ctx->wmx;
+    cudaFree(w.Lref); cudaFree(w.Mref); cudaFree(w.Dinv_ref); cudaFree(w.diag_ref); cudaFree(w.Y); cudaFree(w.Z);
+    cudaFree(w.U); cudaFree(w.A); cudaFree(w.M); cudaFree(w.Dinv); cudaFree(w.diag); cudaFree(w.eps); cudaFree(w.y);
+    cudaFree(w.x); cudaFree(w.r); cudaFree(w.gpart); cudaFree(w.st); cudaFree(w.Acopy); cudaFree(w.cref);
+    cudaFree(w.ldref); cudaFree(w.part); cudaFree(w.ld);
+    w = MixedWork();
+}
+
+static int ensure_ref_bufs(cg_ctx* ctx)
+{
+    MixedWork& w = ctx->wmx;
+    if (w.Lref) return CG_OK;
+    const size_t tiled = tiled_elems(ctx->nt);
+    const int N = ctx->N, nt = ctx->nt, lp = lpad_of(ctx->lmax), nhp = nharm_pad(ctx->lmax);
+    int rc = dalloc(ctx, &w.Lref, tiled);
+    if (!rc) rc = dalloc(ctx, &w.Mref, tiled);
+    if (!rc) rc = dalloc(ctx, &w.Dinv_ref, (size_t)nt * TILE_ELEMS);
+    if (!rc) rc = dalloc(ctx, &w.diag_ref, (size_t)N);
+    if (!rc) rc = dalloc(ctx, &w.Y, (size_t)nhp * N);
+    if (!rc) rc = dalloc(ctx, &w.Z, (size_t)nhp * N);
+    if (!rc) rc = dalloc(ctx, &w.U, tiled * lp);
+    if (!rc) rc = dalloc(ctx, &w.cref, (size_t)ctx->lmax + 1);
+    if (!rc) rc = dalloc(ctx, &w.ldref, 1);
+    if (rc) { mixed_free(ctx); return rc; }
+    w.lpad = lp;
+    return CG_OK;
+}
+
+static int ensure_batch_bufs(cg_ctx* ctx, int B)
+{
+    MixedWork& w = ctx->wmx;
+    if (w.cap >= B) return CG_OK;
+    cudaFree(w.A); cudaFree(w.Acopy); cudaFree(w.M); cudaFree(w.Dinv); cudaFree(w.diag); cudaFree(w.eps);
+    cudaFree(w.y); cudaFree(w.x); cudaFree(w.r); cudaFree(w.part); cudaFree(w.gpart); cudaFree(w.st); cudaFree(w.ld);
+    w.A = w.Acopy = w.M = w.Dinv = w.diag = w.eps = w.gpart = nullptr;
+    w.y = w.x = w.r = w.part = w.ld = nullptr;
+    w.st = nullptr;
+    w.cap = 0;
+    const size_t tiled = tiled_elems(ctx->nt);
+    const int N = ctx->N, nt = ctx->nt, lp = lpad_of(ctx->lmax), ntile = ntiles_lower(nt);
+    int rc = dalloc(ctx, &w.A, tiled * B);
+    if (!rc) rc = dalloc(ctx, &w.Acopy, tiled * B);
+    if (!rc) rc = dalloc(ctx, &w.M, tiled * B);
+    if (!rc) rc = dalloc(ctx, &w.Dinv, (size_t)B * nt * TILE_ELEMS);
+    if (!rc) rc = dalloc(ctx, &w.diag, (size_t)B * N);
+    if (!rc) rc = dalloc(ctx, &w.eps, (size_t)B * lp);
+    if (!rc) rc = dalloc(ctx, &w.y, (size_t)B * N);
+    if (!rc) rc = dalloc(ctx, &w.x, (size_t)B * N);
+    if (!rc) rc = dalloc(ctx, &w.r, (size_t)B * N);
+    if (!rc) rc = dalloc(ctx, &w.part, (size_t)B * ntile * 2 * TS);
+    if (!rc) rc = dalloc(ctx, &w.gpart, (size_t)ntile * B * lp);
+    if (!rc) rc = dalloc(ctx, &w.st, (size_t)B);
+    if (!rc) rc = dalloc(ctx, &w.ld, (size_t)B);
+    if (rc) return rc;
+    w.cap = B;
+    return CG_OK;
+}
+
+int mixed_prepare_reference(cg_ctx* ctx, const double* cl_ref_host)
+{
+    int rc = ensure_ref_bufs(ctx);
+    if (rc) return rc;
+    MixedWork& w = ctx->wmx;
+    const int nt = ctx->nt, N = ctx->N, n = ctx->n, lmax = ctx->lmax, lp = w.lpad;
+    const size_t tiled = tiled_elems(nt);
+    for (int l = 2; l <= lmax; ++l)
+        if (!(cl_ref_host[l] > 0) || !std::isfinite(cl_ref_host[l])) {
+            ctx->err = "reference C_l must be positive and finite for l >= 2";
+            return CG_ERR_BAD_ARG;
+        }
+    cudaStream_t s = ctx->stream;
+    w.cl_ref.assign(cl_ref_host, cl_ref_host + lmax + 1);
+    CG_CUDA_TRY(ctx, cudaMemcpyAsync(w.cref, cl_ref_host, sizeof(double) * (lmax + 1), cudaMemcpyHostToDevice, s));
+    // Cref = C(cl_ref) + N in FP64, factor and invert the factor
+    if ((rc = fp64_build_tiled_into(ctx, 1, w.cref, true, w.Lref, s))) return rc;
+    int* st = nullptr;
+    if ((rc = dalloc(ctx, &st, 1))) return rc;
+    cudaMemsetAsync(st, 0, sizeof(int), s);
+    rc = tiled_cholesky<double>(ctx, 1, nt, w.Lref, w.Dinv_ref, w.diag_ref, st, tiled, s);
+    if (!rc) rc = tiled_trtri<double>(ctx, 1, nt, w.Lref, w.Dinv_ref, w.Mref, tiled, s);
+    int hst = 0;
+    if (!rc) {
+        fp64_logdet(1, n, N, w.diag_ref, w.ldref, s);
+        cudaMemcpyAsync(&hst, st, sizeof(int), cudaMemcpyDeviceToHost, s);
+    }
+    // whitened harmonic basis and table
+    const int nhp = nharm_pad(lmax);
+    if (!rc) {
+        CG_CUDA_TRY(ctx, cudaMemsetAsync(w.Y, 0, sizeof(double) * (size_t)nhp * N, s));
+        ylm_basis<<<dim3((N + 127) / 128, lmax + 1), 128, 0, s>>>(n, N, lmax, ctx->d_xyz, ctx->d_beam, w.Y);
+        const size_t smz = 2 * (size_t)TS * SmemLd<double>::v * sizeof(double);
+        cudaFuncSetAttribute(whiten_basis, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
+        whiten_basis<<<dim3(nt, nhp / TS), 256, smz, s>>>(nt, N, w.Mref, w.Y, w.Z);
+        if (lp <= 48) {
+            constexpr int CC = 8;
+            const size_t smu = sizeof(double) * 32 * (TS + CC) + sizeof(float) * (size_t)CC * TS * lp;
+            cudaFuncSetAttribute(build_ubar<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smu);
+            build_ubar<CC><<<dim3(ntiles_lower(nt), TS / CC), 256, smu, s>>>(N, lmax, lp, w.Z, w.cref, w.U);
+        } else {
+            constexpr int CC = 4;
+            const size_t smu = sizeof(double) * 32 * (TS + CC) + sizeof(float) * (size_t)CC * TS * lp;
+            cudaFuncSetAttribute(build_ubar<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smu);
+            build_ubar<CC><<<dim3(ntiles_lower(nt), TS / CC), 256, smu, s>>>(N, lmax, lp, w.Z, w.cref, w.U);
+        }
+        CG_CUDA_TRY(ctx, cudaGetLastError());
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = CG_ERR_CUDA; }
+    }
+    cudaFree(st);
+    if (!rc && hst) {
+        ctx->err = "reference covariance is not positive definite";
+        rc = CG_ERR_NOT_PD;
+    }
+    if (rc) { w.have_ref = false; return rc; }
+    w.have_ref = true;
+    ++w.ref_count;
+    return CG_OK;
+}
+
+static void geometric_mean(int B, int lmax, const double* cl, std::vector<double>& out)
+{
+    out.assign(lmax + 1, 0.0);
+    for (int l = 2; l <= lmax; ++l) {
+        double s = 0.0;
+        int cnt = 0;
+        for (int b = 0; b < B; ++b) {
+            const double v = cl[(size_t)b * (lmax + 1) + l];
+            if (v > 0 && std::isfinite(v)) { s += std::log(v); ++cnt; }
+        }
+        out[l] = cnt ? std::exp(s / cnt) : 1.0;
+    }
+}
+
+int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, const double* d_d, int d_stride,
+                  double* d_m2lnl, double* d_chi2, double* d_logdet, double* d_grad, int* d_status, cudaStream_t s)
+{
+    MixedWork& w = ctx->wmx;
+    const int nt = ctx->nt, N = ctx->N, n = ctx->n, lmax = ctx->lmax;
+    int rc = ensure_batch_bufs(ctx, B);
+    if (rc) return rc;
+    // decide the reference point on the host
+    std::vector<double> hcl;
+    const bool need_host = !w.have_ref || ctx->recenter != CG_RECENTER_FIXED;
+    if (need_host && !h_cl) {
+        hcl.resize((size_t)B * (lmax + 1));
+        CG_CUDA_TRY(ctx, cudaMemcpyAsync(hcl.data(), d_cl, sizeof(double) * hcl.size(), cudaMemcpyDeviceToHost, s));
+        CG_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+        h_cl = hcl.data();
+    }
+    if (need_host) {
+        bool recentre = !w.have_ref || ctx->recenter == CG_RECENTER_BATCH;
+        if (!recentre) {
+            double dev = 0.0;
+            for (int b = 0; b < B; ++b)
+                for (int l = 2; l <= lmax; ++l) {
+                    const double v = h_cl[(size_t)b * (lmax + 1) + l];
+                    if (v > 0 && std::isfinite(v)) dev = std::max(dev, std::fabs(std::log(v / w.cl_ref[l])));
+                }
+            recentre = dev > ctx->recenter_radius;
+        }
+        if (recentre) {
+            std::vector<double> gm;
+            geometric_mean(B, lmax, h_cl, gm);
+            if ((rc = mixed_prepare_reference(ctx, gm.data()))) return rc;
+        }
+    }
+    const int lp = w.lpad, ntile = ntiles_lower(nt);
+    const size_t tiled = tiled_elems(nt);
+    init_status<<<(B + 127) / 128, 128, 0, s>>>(B, d_cl, lmax, w.st);
+    make_eps<<<B, 64, 0, s>>>(B, lmax, lp, d_cl, w.cref, w.eps);
+    // y = Mref d: one map (broadcast) or one per element
+    if (d_stride == 0) {
+        trmv_lower<<<dim3(nt, 1), 256, 0, s>>>(nt, n, N, w.Mref, d_d, 0, w.r);
+        broadcast_vec<<<dim3((N + 255) / 256, B), 256, 0, s>>>(B, N, w.r, w.y);
+    } else {
+        trmv_lower<<<dim3(nt, B), 256, 0, s>>>(nt, n, N, w.Mref, d_d, d_stride, w.y);
+    }
+    // A_b = I + sum_l eps_bl Ubar_l
+    {
+        const size_t smem = sizeof(float) * 2 * 128 * lp;
+        cudaFuncSetAttribute(contract_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        contract_fwd<<<dim3((unsigned)(tiled / 128), (B + 127) / 128), 256, smem, s>>>(B, lp, w.U, w.eps, w.A,
+                                                                                        w.Acopy, tiled);
+    }
+    if ((rc = tiled_cholesky<float>(ctx, B, nt, w.A, w.Dinv, w.diag, w.st, tiled, s))) return rc;
+    logdet_mixed<<<B, 256, 0, s>>>(n, N, w.diag, w.ldref, w.ld);
+    if ((rc = tiled_trtri<float>(ctx, B, nt, w.A, w.Dinv, w.M, tiled, s))) return rc;
+    if ((rc = tiled_lauum<float>(ctx, B, nt, w.M, w.A, tiled, s))) return rc;
+    // x = V y; r = y - A x; x += V r
+    symv_partials<float><<<dim3(ntile, B), 256, 0, s>>>(nt, w.A, tiled, w.y, N, w.part);
+    symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, w.part, w.x, N, nullptr, 1.0);
+    symv_partials<float><<<dim3(ntile, B), 256, 0, s>>>(nt, w.Acopy, tiled, w.x, N, w.part);
+    symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, w.part, w.r, N, w.y, -1.0);
+    symv_partials<float><<<dim3(ntile, B), 256, 0, s>>>(nt, w.A, tiled, w.r, N, w.part);
+    symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, w.part, w.x, N, w.x, 1.0);
+    chi2_mixed<<<B, 256, 0, s>>>(n, N, N, w.y, w.x, w.ld, d_m2lnl, d_chi2, d_logdet);
+    if (d_grad) {
+        const size_t sma = sizeof(float) * (64 * 49 + 64 * 65 + 2 * 64 * 64);
+        cudaFuncSetAttribute(contract_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma);
+        contract_adj<<<dim3(ntile, (B + 63) / 64), 256, sma, s>>>(B, N, lp, w.U, w.A, tiled, w.x, w.gpart);
+        adj_finish<<<B, 64, 0, s>>>(B, ntile, lmax, lp, w.gpart, w.cref, d_grad);
+    }
+    if (d_status) CG_CUDA_TRY(ctx, cudaMemcpyAsync(d_status, w.st, sizeof(int) * B, cudaMemcpyDeviceToDevice, s));
+    CG_CUDA_TRY(ctx, cudaGetLastError());
+    return CG_OK;
+}
+
+}  // namespace cg

@@ -1,0 +1,130 @@
+/* cosmopp_gb300 -- GB300-native pixel-space CMB covariance and low-l TT
+ * likelihood, the drop-in for Cosmo++'s CMatrixGenerator / CMatrix /
+ * Likelihood path (plus the adjoint gradient that path lacks).
+ *
+ * C ABI: plain pointers and sizes, every call returns an int status
+ * (CG_OK = 0), cg_last_error() gives the text.  One context per host thread;
+ * calls on one context are serialised.  Host-pointer entry points block until
+ * the result is on the host; *_device entry points take device pointers and
+ * run asynchronously on the given CUDA stream.
+ *
+ * Packed storage is the reference's CMatrix layout: element (i, j), i <= j,
+ * at j*(j+1)/2 + i (include/c_matrix.hpp:10-83, source/c_matrix.cpp:28-39),
+ * identical to LAPACK 'U' packed.
+ */
+#ifndef COSMOPP_GB300_H
+#define COSMOPP_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define CG_OK              0
+#define CG_ERR_BAD_ARG     1  /* invalid argument (size, NULL, range) */
+#define CG_ERR_NOT_PD      2  /* covariance not positive definite (per-element status) */
+#define CG_ERR_NONFINITE   3  /* NaN / Inf in an input */
+#define CG_ERR_TIMEOUT     4  /* a bounded device wait gave up */
+#define CG_ERR_CUDA        5  /* CUDA runtime error */
+#define CG_ERR_NO_DEVICE   6  /* no usable sm_103 device */
+#define CG_ERR_ALLOC       7  /* device allocation failed */
+
+#define CG_SCHEME_RING 0
+#define CG_SCHEME_NEST 1      /* the reference's ordering (source/c_matrix_generator.cpp:182) */
+
+#define CG_PREC_FP64   0      /* plain FP64 path */
+#define CG_PREC_MIXED  1      /* batched mixed path: FP64 reference factor + FP32 whitened factors */
+
+#define CG_RECENTER_FIXED 0   /* keep the reference point until cg_set_reference */
+#define CG_RECENTER_BATCH 1   /* re-centre on every batch's geometric-mean C_l */
+#define CG_RECENTER_AUTO  2   /* re-centre when a batch strays beyond recenter_radius */
+
+typedef struct cg_ctx cg_ctx;
+typedef struct cg_lik cg_lik;
+
+typedef struct cg_config {
+    int struct_size;           /* sizeof(cg_config) */
+    /* pixels: either HEALPix (nside, scheme, good_pixels[n] or NULL = all) or dirs[n][3] */
+    long nside;
+    int scheme;
+    const int* good_pixels;
+    int n;
+    const double* dirs;
+    /* harmonic range and beam */
+    int lmax;                  /* C_l vectors have lmax + 1 entries; l = 0, 1 are ignored */
+    double fwhm_deg;           /* Gaussian beam FWHM in degrees (source/utils.cpp:54-64) */
+    const double* beam;        /* optional B_l[lmax + 1] (e.g. pixel window x beam); overrides fwhm */
+    /* white noise on the kept pixels: noise_var[n] or sigma^2 on every pixel */
+    double noise_sigma;
+    const double* noise_var;
+    /* execution */
+    int max_batch;             /* largest B a call may pass */
+    int precision;             /* CG_PREC_FP64 or CG_PREC_MIXED */
+    int device;                /* CUDA device ordinal */
+    /* mixed path reference point */
+    const double* cl_ref;      /* optional initial reference C_l[lmax + 1] */
+    int recenter;              /* CG_RECENTER_* */
+    double recenter_radius;    /* max |ln(C_l / Cref_l)| before an automatic re-centre (0 = 1.0) */
+} cg_config;
+
+/* ---- context ----------------------------------------------------------- */
+void cg_config_init(cg_config* cfg);
+int cg_create(cg_ctx** ctx, const cg_config* cfg);
+void cg_destroy(cg_ctx* ctx);
+const char* cg_last_error(const cg_ctx* ctx);   /* ctx may be NULL: last create error */
+int cg_get_n(const cg_ctx* ctx);
+int cg_unit_vectors(const cg_ctx* ctx, double* xyz);             /* [n][3] */
+
+/* ---- covariance build --------------------------------------------------- */
+/* CMatrixGenerator::clToCMatrix (include/c_matrix_generator.hpp:53,
+   source/c_matrix_generator.cpp:164-232): packed C for one C_l vector, no noise.
+   Same rounding order as the reference, so the result is bit-identical. */
+int cg_build_cmatrix(cg_ctx* ctx, const double* cl, double* out_packed);
+/* the same for B C_l vectors ([B][lmax+1] -> [B][n(n+1)/2]) */
+int cg_build_cmatrix_batched(cg_ctx* ctx, int B, const double* cl, double* out_packed);
+
+/* ---- likelihood + gradient ---------------------------------------------- */
+/* -2lnL = d^T C^-1 d + ln det C for B C_l vectors, C = C(cl_b) + noise
+   (the reference's Likelihood(C, 0, N, goodPixels).calculate(d),
+   include/likelihood.hpp:58,88; source/likelihood.cpp:69-180, without its
+   hard-coded detOffset: logdet is the raw ln det C).
+   d: one map (d_stride = 0) or B maps at stride d_stride (>= n).
+   grad (nullable): [B][lmax+1] d(-2lnL)/dC_l (l < 2 are 0) -- new, no reference counterpart.
+   chi2 / logdet / status nullable; status[b] = CG_OK or CG_ERR_NOT_PD / CG_ERR_NONFINITE.
+   Returns CG_OK when the call ran, even if some elements carry a bad status. */
+int cg_loglike(cg_ctx* ctx, int B, const double* cl, const double* d, int d_stride,
+               double* m2lnl, double* chi2, double* logdet, double* grad, int* status);
+/* device-pointer variant, asynchronous on `stream` (cudaStream_t, 0 = the context's stream) */
+int cg_loglike_device(cg_ctx* ctx, int B, const double* d_cl, const double* d_d, int d_stride,
+                      double* d_m2lnl, double* d_chi2, double* d_logdet, double* d_grad, int* d_status,
+                      void* stream);
+/* mixed path: set the reference point explicitly (C_l[lmax + 1]) */
+int cg_set_reference(cg_ctx* ctx, const double* cl_ref);
+/* number of reference (re)factorisations so far (mixed path) */
+int cg_reference_count(const cg_ctx* ctx);
+
+/* ---- Likelihood drop-in (source/likelihood.cpp:38-41,69-180) ------------- */
+/* construct from packed C, fiducial (nullable = 0) and noise, with optional
+   foreground marginalisation; all host pointers, n(n+1)/2 doubles each */
+int cg_likelihood_create(cg_lik** lik, int n, const double* c_packed, const double* fid_packed,
+                         const double* noise_packed, const double* foreground, int device);
+/* chi2 and logdet as the reference's calculate (logdet without detOffset) */
+int cg_likelihood_calculate(cg_lik* lik, const double* t, double* chi2, double* logdet);
+double cg_likelihood_logdet(const cg_lik* lik);
+void cg_likelihood_destroy(cg_lik* lik);
+const char* cg_likelihood_last_error(const cg_lik* lik);
+
+/* ---- HEALPix geometry (host; Gorski et al. 2005) ------------------------ */
+long cg_nside2npix(long nside);
+long cg_ring2nest(long nside, long ipring);
+long cg_nest2ring(long nside, long ipnest);
+int cg_pix2vec(long nside, int scheme, const int* pix, int n, double* xyz);
+/* Utils::beamFunction (source/utils.cpp:54-64), fwhm in degrees */
+double cg_beam(int l, double fwhm_deg);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
