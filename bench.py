@@ -1,0 +1,382 @@
+"""Benchmark: -2lnL + gradient evaluations per second at nside 16, lmax 47.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--path mixed|fp64] [--batch B] [--no-cpu-baseline]
+
+A step is one batched evaluation of B C_l vectors (lognormal 10% per-l
+perturbations of C_l = 1e3 2pi/(l(l+1))) on one seeded synthetic map, returning
+-2lnL and d(-2lnL)/dC_l for each vector.  ``value`` is evaluations/s with
+inputs resident in HBM (device-pointer entry point); ``e2e`` is the same
+through the host-pointer C ABI from pinned buffers, copies included.
+Multi-GPU: one process per GPU, each with its own batch (replicas: batch
+elements are independent), max-over-ranks time, value summed over ranks.
+
+``--impl reference`` times the reference algorithm on the host cores: the
+oracle restatement of clToCMatrix + Likelihood (dpptrf/dpptri) + calculate,
+plus the FP64 adjoint gradient, at the same configuration.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "nside16_lmax47_b256"
+METRIC = "lnL+grad evals/sec at nside16 lmax47, batched mixed vs plain FP64 GPU, |delta|<=1e-3"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--path", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--batch", type=int, default=None)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--fp64-compare-batch", type=int, default=16)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons, power = [], None, set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": max(power) if power else None}
+
+
+def make_inputs(wl, cg):
+    """Seeded data map d = L z, L from the FP64 covariance built by the library (input generation)."""
+    from cosmopp_gb300 import workload as W
+    ctx = cg.Context(lmax=wl.lmax, fwhm_deg=wl.fwhm_deg, nside=wl.nside, good_pixels=wl.ring_kept, scheme="RING",
+                     noise_sigma=wl.sigma, max_batch=1, precision="fp64")
+    c = ctx.build_cmatrix(wl.cl_fid)
+    ctx.close()
+    full = W.packed_to_full(c, wl.n) + wl.sigma ** 2 * np.eye(wl.n)
+    return W.draw_data(full, wl.z)
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def cpu_baseline(wl, d, seconds_budget=20.0):
+    """The reference algorithm (oracle restatement, O(lmax^2) Legendre restarts as the
+    reference does) on this host's cores, for a bounded sample of the batch."""
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    nest = np.array([int(x) for x in __import__("cosmopp_gb300").ring2nest(wl.nside, wl.ring_kept)], dtype=np.int32)
+    xyz = O.unit_vectors(wl.nside, nest, "NEST")
+    t0 = time.perf_counter()
+    done = 0
+    while True:
+        O.evaluate(wl.cl_batch[done % len(wl.cl_batch)], xyz, wl.fwhm_deg, wl.sigma ** 2, d, grad=True, restart=True)
+        done += 1
+        if time.perf_counter() - t0 > seconds_budget or done >= 4:
+            break
+    el = time.perf_counter() - t0
+    return {"value": done / el, "unit": "evals/s", "cores": cores, "kind": "port",
+            "sample": "%d evaluation(s) of the %d-vector batch (clToCMatrix with per-l Legendre restarts + "
+                      "dpptrf/dpptri Likelihood + calculate + FP64 adjoint), %.1f s" % (done, len(wl.cl_batch), el)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import cosmopp_gb300 as cg
+    from cosmopp_gb300 import workload as W
+    from oracle import oracle as O
+    wl = W.make(WORKLOAD, batch=args.batch)
+    # data map from the oracle's own FP64 covariance (no GPU on this arm)
+    O.build()
+    nest = cg.ring2nest(wl.nside, wl.ring_kept)
+    xyz = O.unit_vectors(wl.nside, nest, "NEST")
+    c = O.cl_to_cmatrix(wl.cl_fid, xyz, wl.fwhm_deg)
+    d = W.draw_data(W.packed_to_full(c, wl.n) + wl.sigma ** 2 * np.eye(wl.n), wl.z)
+    cores = os.cpu_count() or 1
+    O.set_threads(cores)
+    for k in range(args.warmup):
+        O.evaluate(wl.cl_batch[k % len(wl.cl_batch)], xyz, wl.fwhm_deg, wl.sigma ** 2, d, grad=True, restart=True)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        O.evaluate(wl.cl_batch[k % len(wl.cl_batch)], xyz, wl.fwhm_deg, wl.sigma ** 2, d, grad=True, restart=True)
+    el = time.perf_counter() - t0
+    v = args.steps / el
+    out = {"metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": args.gpus, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1000.0 * el / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+           "config": {"workload": WORKLOAD, "nside": wl.nside, "lmax": wl.lmax, "n_pixels": wl.n,
+                      "sample": "one C_l vector per step"},
+           "cpu_baseline": {"value": v, "unit": "evals/s", "cores": cores, "kind": "port",
+                            "sample": "%d steps x 1 evaluation (clToCMatrix with per-l Legendre restarts, "
+                                      "dpptrf/dpptri, calculate, FP64 adjoint)" % args.steps},
+           "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    import cosmopp_gb300 as cg
+    from cosmopp_gb300 import workload as W
+    wl = W.make(WORKLOAD, batch=args.batch, batch_seed=7 + rank)
+    B = len(wl.cl_batch)
+    d = make_inputs(wl, cg)
+    path = args.path
+    ctx = cg.Context(lmax=wl.lmax, fwhm_deg=wl.fwhm_deg, nside=wl.nside, good_pixels=wl.ring_kept, scheme="RING",
+                     noise_sigma=wl.sigma, max_batch=B, precision=path, device=local,
+                     cl_ref=wl.cl_fid if path == "mixed" else None, recenter="fixed")
+    L1 = wl.lmax + 1
+    dev = torch.device("cuda", local)
+    # a few distinct batches, cycled so that no two consecutive steps see the same inputs
+    nb = 4
+    cls = torch.tensor(np.stack([W.lognormal_batch(wl.cl_fid, B, 100 + 17 * rank + k) for k in range(nb)]),
+                       dtype=torch.float64, device=dev)
+    dd = torch.tensor(d, dtype=torch.float64, device=dev)
+    m2 = torch.empty(B, dtype=torch.float64, device=dev)
+    chi2 = torch.empty_like(m2)
+    ld = torch.empty_like(m2)
+    grad = torch.empty(B, L1, dtype=torch.float64, device=dev)
+    st = torch.empty(B, dtype=torch.int32, device=dev)
+    # an explicit stream: the library launches there and the events bracket exactly that work
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.set_stream(stream)
+    sp = stream.cuda_stream
+    assert sp != 0
+
+    def step(k):
+        ctx.loglike_device(B, cls[k % nb].data_ptr(), dd.data_ptr(), 0, m2.data_ptr(), chi2.data_ptr(),
+                           ld.data_ptr(), grad.data_ptr(), st.data_ptr(), sp)
+
+    for k in range(max(3, args.warmup)):
+        step(k)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = ctx.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for k in range(args.steps):
+        step(k)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = (ctx.launch_count() - launches0) // args.steps
+    clk = clocks.stop()
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = B * world / (ms / 1000.0)
+    assert int(st.sum().item()) == 0, "non-OK element status in the timed batch"
+
+    # end to end through the host-pointer C ABI from pinned buffers
+    cl_h = torch.empty(nb, B, L1, dtype=torch.float64).pin_memory()
+    cl_h.copy_(cls.cpu())
+    d_h = torch.empty(wl.n, dtype=torch.float64).pin_memory()
+    d_h.copy_(dd.cpu())
+    outs = [torch.empty(B, dtype=torch.float64).pin_memory() for _ in range(3)]
+    g_h = torch.empty(B, L1, dtype=torch.float64).pin_memory()
+    st_h = torch.empty(B, dtype=torch.int32).pin_memory()
+    L = cg.library()
+    import ctypes
+
+    def e2e_step(k):
+        rc = L.cg_loglike(ctx.handle, B, ctypes.cast(cl_h[k % nb].data_ptr(), cg._dp),
+                          ctypes.cast(d_h.data_ptr(), cg._dp), 0, ctypes.cast(outs[0].data_ptr(), cg._dp),
+                          ctypes.cast(outs[1].data_ptr(), cg._dp), ctypes.cast(outs[2].data_ptr(), cg._dp),
+                          ctypes.cast(g_h.data_ptr(), cg._dp), ctypes.cast(st_h.data_ptr(), cg._ip))
+        assert rc == 0
+    for k in range(2):
+        e2e_step(k)
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        e2e_step(k)
+    e2e_ms = (time.perf_counter() - t0) * 1000.0 / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_ms], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    h2d = B * L1 * 8 + wl.n * 8
+    d2h = B * (3 * 8 + L1 * 8 + 4)
+
+    # per-stage times (profiled pass after the timed region) and the roofline of the top stage
+    ctx.set_profiling(True)
+    stages = {}
+    nprof = 3
+    for k in range(nprof):
+        step(k)
+        for nm, v in ctx.stage_times().items():
+            stages[nm] = stages.get(nm, 0.0) + v / nprof
+    ctx.set_profiling(False)
+    torch.cuda.synchronize()
+    peaks, peak_kind = load_peaks()
+    n, N = wl.n, ((wl.n + 63) // 64) * 64
+    pairs = n * (n + 1) // 2
+    if path == "mixed":
+        # contraction: reads the FP32 table once (tiles x 4096 x lpad x 4 B), writes A and its copy (FP32)
+        nt = N // 64
+        tiled = nt * (nt + 1) // 2 * 4096
+        lpad = ((L1 + 15) // 16) * 16
+        build_bytes = tiled * lpad * 4 + 2 * B * tiled * 4
+        fac_flops = B * (N ** 3 / 3.0) * 2 / 2  # n^3/3 multiply-adds -> 2 flops each, Cholesky only
+        top = max(("cholesky", "trtri", "lauum"), key=lambda s: stages.get(s, 0))
+        roof = {"kernel": "contraction (K_b = sum_l eps_bl Ubar_l, FP32 out)", "bound": "hbm",
+                "achieved": build_bytes / (stages["build"] * 1e-3) / 1e9, "peak": peaks["hbm_gbs"],
+                "unit": "GB/s", "traffic": None, "algorithmic_bytes": build_bytes}
+        roof["frac"] = roof["achieved"] / roof["peak"]
+        fp32_peak = 70.06  # TFLOP/s, FFMA probe on this machine's GB300 (no FP32 figure in the peaks file)
+        chol_flops = B * (N ** 3) / 3.0
+        roof_chol = {"kernel": "tiled FP32 Cholesky (chol_diag/panel/update)", "bound": "fp32_cuda_core",
+                     "achieved": chol_flops / (stages["cholesky"] * 1e-3) / 1e12, "peak": fp32_peak,
+                     "unit": "TFLOP/s"}
+        roof_chol["frac"] = roof_chol["achieved"] / fp32_peak
+        del fac_flops, top
+    else:
+        roof = {"kernel": "FP64 tiled Cholesky", "bound": "fp64", "achieved": B * (N ** 3) / 3.0 /
+                (stages["cholesky"] * 1e-3) / 1e12, "peak": 1.20, "unit": "TFLOP/s", "traffic": None}
+        roof["frac"] = roof["achieved"] / roof["peak"]
+        roof_chol = None
+
+    out = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+           "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+f64" if path == "mixed" else "f64", "data": "synthetic",
+           "config": {"workload": WORKLOAD, "path": path, "nside": wl.nside, "lmax": wl.lmax, "n_pixels": wl.n,
+                      "batch_per_gpu": B, "fwhm_arcmin": wl.meta["fwhm_arcmin"], "noise_sigma": wl.sigma,
+                      "mask_keep": wl.meta["keep"], "reference_point": "fiducial C_l, factorised at set-up",
+                      "l2": "per-step working set %.1f GB > 129 MB L2" % (B * 3 * (N * N / 2) * 4 / 1e9),
+                      "parallelism": "replicas x%d" % world},
+           "clocks": clk, "gpu_launches": int(launches),
+           "e2e": {"value": B * world / (e2e_ms / 1000.0), "unit": "evals/s", "ms_per_step": e2e_ms,
+                   "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+           "stages_ms": {k: round(v, 4) for k, v in stages.items() if k != "end"},
+           "roofline": roof}
+    if roof_chol:
+        out["roofline_factor"] = roof_chol
+    out["roofline"]["peak_source"] = peak_kind
+    if rank == 0 and path == "mixed" and args.fp64_compare_batch > 0:
+        # the plain FP64 GPU path on the same workload, for the mixed-vs-FP64 ratio and the error bar
+        Bf = min(args.fp64_compare_batch, B)
+        c64 = cg.Context(lmax=wl.lmax, fwhm_deg=wl.fwhm_deg, nside=wl.nside, good_pixels=wl.ring_kept,
+                         scheme="RING", noise_sigma=wl.sigma, max_batch=Bf, precision="fp64", device=local)
+        clsf = cls[0, :Bf].contiguous()
+        m64 = torch.empty(Bf, dtype=torch.float64, device=dev)
+        g64 = torch.empty(Bf, L1, dtype=torch.float64, device=dev)
+        c64.loglike_device(Bf, clsf.data_ptr(), dd.data_ptr(), 0, m64.data_ptr(), None, None, g64.data_ptr(),
+                           None, sp)
+        torch.cuda.synchronize()
+        step(0)
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        c64.loglike_device(Bf, clsf.data_ptr(), dd.data_ptr(), 0, m64.data_ptr(), None, None, g64.data_ptr(),
+                           None, sp)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = f0.elapsed_time(f1)
+        err = (m2[:Bf] - m64).abs().max().item()
+        gerr = ((grad[:Bf] - g64).abs().max(dim=1).values / g64.abs().max(dim=1).values).max().item()
+        out["plain_fp64_gpu"] = {"value": Bf / (ms64 / 1000.0), "unit": "evals/s", "batch": Bf,
+                                 "mixed_over_fp64": value / world / (Bf / (ms64 / 1000.0)),
+                                 "max_abs_delta_m2lnl": err, "max_rel_delta_grad": gerr}
+        c64.close()
+    if rank == 0 and not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(wl, d)
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -84,6 +84,10 @@ def library():
                                     ctypes.c_void_p, ctypes.c_void_p]
     L.cg_set_reference.argtypes = [ctypes.c_void_p, _dp]
     L.cg_reference_count.argtypes = [ctypes.c_void_p]
+    L.cg_launch_count.restype = ctypes.c_longlong
+    L.cg_launch_count.argtypes = [ctypes.c_void_p]
+    L.cg_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.cg_stage_times.argtypes = [ctypes.c_void_p, _dp]
     L.cg_likelihood_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_int]
     L.cg_likelihood_calculate.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
     L.cg_likelihood_logdet.restype = ctypes.c_double
@@ -276,6 +280,21 @@ class Context:
 
     def reference_count(self):
         return self._L.cg_reference_count(self._h)
+
+    def launch_count(self):
+        """Kernels this context has launched so far."""
+        return int(self._L.cg_launch_count(self._h))
+
+    def set_profiling(self, enable=True):
+        self._check(self._L.cg_set_profiling(self._h, int(bool(enable))))
+
+    STAGES = ("build", "cholesky", "trtri", "lauum", "solve", "adjoint", "end")
+
+    def stage_times(self):
+        """Per-stage device ms of the last profiled call (syncs on its last event)."""
+        ms = np.zeros(7)
+        self._check(self._L.cg_stage_times(self._h, _p(ms)))
+        return dict(zip(self.STAGES, ms))
 
 
 class Likelihood:

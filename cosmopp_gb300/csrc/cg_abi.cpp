@@ -84,6 +84,8 @@ extern "C" void cg_destroy(cg_ctx* ctx)
     cg::mixed_free(ctx);
     cudaFree(ctx->d_xyz); cudaFree(ctx->d_noise); cudaFree(ctx->d_lega); cudaFree(ctx->d_legb);
     cudaFree(ctx->d_beam); cudaFree(ctx->d_cl); cudaFree(ctx->d_out);
+    for (cudaEvent_t e : ctx->marks)
+        if (e) cudaEventDestroy(e);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -230,6 +232,7 @@ extern "C" int cg_loglike_device(cg_ctx* ctx, int B, const double* d_cl, const d
     }
     CG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    ctx->nmarks = 0;
     if (ctx->precision == CG_PREC_MIXED)
         return cg::mixed_loglike(ctx, B, d_cl, nullptr, d_d, d_stride, d_m2lnl, d_chi2, d_logdet, d_grad, d_status, s);
     return cg::fp64_loglike(ctx, B, d_cl, d_d, d_stride, d_m2lnl, d_chi2, d_logdet, d_grad, d_status, s);
@@ -281,6 +284,29 @@ extern "C" int cg_set_reference(cg_ctx* ctx, const double* cl_ref)
 }
 
 extern "C" int cg_reference_count(const cg_ctx* ctx) { return ctx ? ctx->wmx.ref_count : 0; }
+
+extern "C" long long cg_launch_count(const cg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+extern "C" int cg_set_profiling(cg_ctx* ctx, int enable)
+{
+    if (!ctx) return CG_ERR_BAD_ARG;
+    ctx->profiling = enable != 0;
+    return CG_OK;
+}
+
+extern "C" int cg_stage_times(cg_ctx* ctx, double* ms)
+{
+    if (!ctx || !ms) return CG_ERR_BAD_ARG;
+    for (int k = 0; k < cg::ST_COUNT; ++k) ms[k] = 0.0;
+    if (ctx->nmarks > 0) CG_CUDA_TRY(ctx, cudaEventSynchronize(ctx->marks[ctx->nmarks - 1]));
+    for (int k = 0; k + 1 < ctx->nmarks; ++k) {
+        float t = 0.f;
+        CG_CUDA_TRY(ctx, cudaEventElapsedTime(&t, ctx->marks[k], ctx->marks[k + 1]));
+        ms[ctx->mark_stage[k]] += t;
+    }
+    ctx->nmarks = 0;
+    return CG_OK;
+}
 
 // ---- Likelihood drop-in ------------------------------------------------------
 

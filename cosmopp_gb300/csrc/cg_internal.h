@@ -120,6 +120,12 @@ struct cg_ctx {
     cg::Fp64Work w64;
     cg::MixedWork wmx;
     std::string err;
+    // instrumentation: kernel launch counter and optional per-stage CUDA events
+    long long launches = 0;
+    bool profiling = false;
+    int nmarks = 0;
+    cudaEvent_t marks[16] = {};
+    int mark_stage[16] = {};
 };
 
 // helpers shared by the translation units
@@ -133,6 +139,17 @@ struct cg_ctx {
     } while (0)
 
 namespace cg {
+// stage ids reported by cg_stage_times
+enum Stage { ST_BUILD = 0, ST_CHOL, ST_TRTRI, ST_LAUUM, ST_SOLVE, ST_ADJOINT, ST_END, ST_COUNT };
+inline void stage_mark(cg_ctx* ctx, int stage, cudaStream_t s)
+{
+    if (!ctx->profiling || ctx->nmarks >= 16) return;
+    if (!ctx->marks[ctx->nmarks]) cudaEventCreate(&ctx->marks[ctx->nmarks]);
+    ctx->mark_stage[ctx->nmarks] = stage;
+    cudaEventRecord(ctx->marks[ctx->nmarks], s);
+    ++ctx->nmarks;
+}
+inline void count_launch(cg_ctx* ctx, long long k = 1) { ctx->launches += k; }
 // plain FP64 path (k_fp64.cu)
 int fp64_ensure(cg_ctx* ctx, int B);
 int fp64_build_tiled(cg_ctx* ctx, int B, const double* d_cl, bool add_noise, cudaStream_t s);

@@ -73,33 +73,59 @@ namespace tile {
 // Symmetric matvec on the tiled lower storage, two deterministic passes:
 // symv_partials: per lower tile (I, J): part[t][0][r] = (V_IJ v_J)[r],
 //                part[t][1][c] = (V_IJ^T v_I)[c] (I != J);
-// symv_reduce:   out_I = sum_J (row-I pieces) in a fixed order.
-template <typename T>
-__global__ void __launch_bounds__(256) symv_partials(int nt, const T* __restrict__ V, size_t strideA,
+// symv_reduce:   out_I = sum_J (row-I pieces) in a fixed order, in FP64.
+// DF = false: FP32 products and in-tile sums (a solve, whose error is then
+// refined away).  DF = true: the vector is split into two FP32 words
+// (hi + lo) and every product is formed exactly with an FMA, the in-tile sums
+// carried as double-float pairs (Dekker / Knuth error-free transformations) --
+// ~44-bit residuals y - A x at FP32 issue rate instead of the 1/64-rate FP64 pipe.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float v)
+{
+    const float t = hi + v;
+    const float z = t - hi;
+    lo += (hi - (t - z)) + (v - z);
+    hi = t;
+}
+
+template <bool DF>
+__global__ void __launch_bounds__(256) symv_partials(int nt, const float* __restrict__ V, size_t strideA,
                                                      const double* __restrict__ v, int vstride,
                                                      double* __restrict__ part)
 {
-    __shared__ T s[TS][TS + 1];
-    __shared__ double sv[2][TS];
+    __shared__ float s[TS][TS + 1];
+    __shared__ float svh[2][TS], svl[2][TS];
     __shared__ double red[4][2][TS];
     int I, J;
     tile_coords(blockIdx.x, I, J);
     const int b = blockIdx.y, ntile = ntiles_lower(nt);
-    const T* tile = V + (size_t)b * strideA + (size_t)blockIdx.x * TILE_ELEMS;
+    const float* tile = V + (size_t)b * strideA + (size_t)blockIdx.x * TILE_ELEMS;
     for (int e = threadIdx.x; e < TILE_ELEMS; e += blockDim.x) s[e / TS][e % TS] = tile[e];  // s[c][r]
-    if (threadIdx.x < TS) {
-        sv[0][threadIdx.x] = v[(size_t)b * vstride + J * TS + threadIdx.x];
-        sv[1][threadIdx.x] = v[(size_t)b * vstride + I * TS + threadIdx.x];
+    if (threadIdx.x < 2 * TS) {
+        const int w = threadIdx.x / TS, k = threadIdx.x % TS;
+        const double x = v[(size_t)b * vstride + (w == 0 ? J : I) * TS + k];
+        const float h = (float)x;
+        svh[w][k] = h;
+        svl[w][k] = (float)(x - (double)h);
     }
     __syncthreads();
     const int r = threadIdx.x % TS, q = threadIdx.x / TS;
-    double a = 0.0, t = 0.0;
+    float ah = 0.f, al = 0.f, th = 0.f, tl = 0.f;
     for (int c = q; c < TS; c += 4) {
-        a += (double)s[c][r] * sv[0][c];  // (V v_J)[r]
-        t += (double)s[r][c] * sv[1][c];  // (V^T v_I)[r] = sum_c V(c, r) v_I[c]
+        const float va = s[c][r], vt = s[r][c];
+        if (DF) {
+            const float p = va * svh[0][c];
+            df_add(ah, al, p);
+            al += fmaf(va, svh[0][c], -p) + va * svl[0][c];
+            const float pt = vt * svh[1][c];
+            df_add(th, tl, pt);
+            tl += fmaf(vt, svh[1][c], -pt) + vt * svl[1][c];
+        } else {
+            ah = fmaf(va, svh[0][c], ah);
+            th = fmaf(vt, svh[1][c], th);
+        }
     }
-    red[q][0][r] = a;
-    red[q][1][r] = t;
+    red[q][0][r] = (double)ah + (double)al;
+    red[q][1][r] = (double)th + (double)tl;
     __syncthreads();
     if (q == 0) {
         double* p = part + ((size_t)b * ntile + blockIdx.x) * 2 * TS;

@@ -258,6 +258,7 @@ int tiled_cholesky(cg_ctx* ctx, int B, int nt, T* A, T* Dinv, T* diag, int* stat
     for (int k = 0; k < nt; ++k) {
         chol_diag<T><<<B, NT_THREADS, diag_smem<T>(), s>>>(k, nt, A, strideA, Dinv, diag, status);
         const int m = nt - k - 1;
+        count_launch(ctx, m > 0 ? 3 : 1);
         if (m > 0) {
             chol_panel<T><<<dim3(m, B), NT_THREADS, sm, s>>>(k, nt, A, strideA, Dinv);
             chol_update<T><<<dim3(m * (m + 1) / 2, B), NT_THREADS, sm, s>>>(k, nt, A, strideA);
@@ -276,6 +277,7 @@ int tiled_trtri(cg_ctx* ctx, int B, int nt, const T* Lm, const T* Dinv, T* M, si
     CG_CUDA_TRY(ctx, cudaMemsetAsync(M, 0, sizeof(T) * strideA * B, s));
     for (int i = 0; i < nt; ++i) {
         trtri_finish<T><<<dim3(i + 1, B), NT_THREADS, sm, s>>>(i, nt, Dinv, M, strideA);
+        count_launch(ctx, i + 1 < nt ? 2 : 1);
         if (i + 1 < nt) trtri_update<T><<<dim3((nt - i - 1) * (i + 1), B), NT_THREADS, sm, s>>>(i, nt, Lm, M, strideA);
     }
     CG_CUDA_TRY(ctx, cudaGetLastError());
@@ -288,6 +290,7 @@ int tiled_lauum(cg_ctx* ctx, int B, int nt, const T* M, T* V, size_t strideA, cu
     int rc = set_smem_attrs<T>(ctx);
     if (rc) return rc;
     lauum_tiles<T><<<dim3(ntiles_lower(nt), B), NT_THREADS, pair_smem<T>(), s>>>(nt, M, V, strideA);
+    count_launch(ctx);
     CG_CUDA_TRY(ctx, cudaGetLastError());
     return CG_OK;
 }

@@ -414,6 +414,7 @@ int fp64_build_tiled_into(cg_ctx* ctx, int B, const double* d_cl, bool add_noise
     build_c_tiled<<<dim3(ntile, B), kThreads, const_smem(ctx->lmax), s>>>(
         ctx->n, ctx->N, ctx->lmax, ctx->d_xyz, ctx->d_noise, ctx->d_lega, ctx->d_legb, ctx->d_beam, d_cl,
         add_noise ? 1 : 0, A, tiled_elems(ctx->nt));
+    count_launch(ctx);
     CG_CUDA_TRY(ctx, cudaGetLastError());
     return CG_OK;
 }
@@ -428,6 +429,7 @@ int fp64_build_packed(cg_ctx* ctx, int B, const double* d_cl, double* d_out, cud
     const long np = (long)ctx->n * (ctx->n + 1) / 2;
     build_c_packed<<<dim3((unsigned)((np + 4 * kThreads - 1) / (4 * kThreads)), B), kThreads, const_smem(ctx->lmax), s>>>(
         ctx->n, ctx->N, ctx->lmax, ctx->d_xyz, ctx->d_lega, ctx->d_legb, ctx->d_beam, d_cl, d_out);
+    count_launch(ctx);
     CG_CUDA_TRY(ctx, cudaGetLastError());
     return CG_OK;
 }
@@ -441,25 +443,37 @@ int fp64_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* d_d, int 
     const int nt = ctx->nt, N = ctx->N, n = ctx->n, lmax = ctx->lmax;
     const size_t strideA = tiled_elems(nt);
     const int ntile = ntiles_lower(nt);
+    stage_mark(ctx, ST_BUILD, s);
     check_inputs<<<(B + 127) / 128, 128, 0, s>>>(B, lmax, d_cl, w.st);
+    count_launch(ctx);
     if ((rc = fp64_build_tiled(ctx, B, d_cl, true, s))) return rc;
+    stage_mark(ctx, ST_CHOL, s);
     if ((rc = tiled_cholesky<double>(ctx, B, nt, w.A, w.Dinv, w.diag, w.st, strideA, s))) return rc;
     logdet_reduce<<<B, kThreads, 0, s>>>(n, N, w.diag, w.ld);
+    count_launch(ctx);
+    stage_mark(ctx, ST_TRTRI, s);
     if ((rc = tiled_trtri<double>(ctx, B, nt, w.A, w.Dinv, w.M, strideA, s))) return rc;
+    stage_mark(ctx, ST_LAUUM, s);
     if ((rc = tiled_lauum<double>(ctx, B, nt, w.M, w.A, strideA, s))) return rc;
+    stage_mark(ctx, ST_SOLVE, s);
     pad_data<<<dim3((N + 255) / 256, B), 256, 0, s>>>(n, N, B, d_d, d_stride, w.dvec);
     symv_tiled<double><<<dim3(nt, B), kThreads, 0, s>>>(nt, N, w.A, strideA, w.dvec, w.alpha);
     chi2_finish<<<B, kThreads, 0, s>>>(n, N, w.dvec, w.alpha, w.ld, d_m2lnl, d_chi2);
+    count_launch(ctx, 3);
+    stage_mark(ctx, ST_ADJOINT, s);
     if (d_logdet) CG_CUDA_TRY(ctx, cudaMemcpyAsync(d_logdet, w.ld, sizeof(double) * B, cudaMemcpyDeviceToDevice, s));
     if (d_grad) {
         for (int l0 = 2; l0 <= lmax; l0 += kAdjChunk) {
             const int l1 = (l0 + kAdjChunk <= lmax + 1) ? l0 + kAdjChunk : lmax + 1;
             adjoint_tiles<<<dim3(ntile, B), kThreads, 0, s>>>(n, N, l0, l1, ctx->d_xyz, ctx->d_lega, ctx->d_legb, w.A,
                                                               strideA, w.alpha, w.gpart, ntile, lmax + 1);
+            count_launch(ctx);
         }
         adjoint_finish<<<B, 64, 0, s>>>(lmax, ntile, w.gpart, ctx->d_beam, d_grad);
+        count_launch(ctx);
     }
-    if (d_status) copy_status<<<(B + 127) / 128, 128, 0, s>>>(B, w.st, d_status);
+    if (d_status) { copy_status<<<(B + 127) / 128, 128, 0, s>>>(B, w.st, d_status); count_launch(ctx); }
+    stage_mark(ctx, ST_END, s);
     CG_CUDA_TRY(ctx, cudaGetLastError());
     return CG_OK;
 }

@@ -583,8 +583,10 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
     }
     const int lp = w.lpad, ntile = ntiles_lower(nt);
     const size_t tiled = tiled_elems(nt);
+    stage_mark(ctx, ST_BUILD, s);
     init_status<<<(B + 127) / 128, 128, 0, s>>>(B, d_cl, lmax, w.st);
     make_eps<<<B, 64, 0, s>>>(B, lmax, lp, d_cl, w.cref, w.eps);
+    count_launch(ctx, d_stride == 0 ? 5 : 4);
     // y = Mref d: one map (broadcast) or one per element
     if (d_stride == 0) {
         trmv_lower<<<dim3(nt, 1), 256, 0, s>>>(nt, n, N, w.Mref, d_d, 0, w.r);
@@ -599,25 +601,34 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
         contract_fwd<<<dim3((unsigned)(tiled / 128), (B + 127) / 128), 256, smem, s>>>(B, lp, w.U, w.eps, w.A,
                                                                                         w.Acopy, tiled);
     }
+    stage_mark(ctx, ST_CHOL, s);
     if ((rc = tiled_cholesky<float>(ctx, B, nt, w.A, w.Dinv, w.diag, w.st, tiled, s))) return rc;
     logdet_mixed<<<B, 256, 0, s>>>(n, N, w.diag, w.ldref, w.ld);
+    count_launch(ctx);
+    stage_mark(ctx, ST_TRTRI, s);
     if ((rc = tiled_trtri<float>(ctx, B, nt, w.A, w.Dinv, w.M, tiled, s))) return rc;
+    stage_mark(ctx, ST_LAUUM, s);
     if ((rc = tiled_lauum<float>(ctx, B, nt, w.M, w.A, tiled, s))) return rc;
+    stage_mark(ctx, ST_SOLVE, s);
     // x = V y; r = y - A x; x += V r
-    symv_partials<float><<<dim3(ntile, B), 256, 0, s>>>(nt, w.A, tiled, w.y, N, w.part);
+    symv_partials<false><<<dim3(ntile, B), 256, 0, s>>>(nt, w.A, tiled, w.y, N, w.part);
     symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, w.part, w.x, N, nullptr, 1.0);
-    symv_partials<float><<<dim3(ntile, B), 256, 0, s>>>(nt, w.Acopy, tiled, w.x, N, w.part);
+    symv_partials<true><<<dim3(ntile, B), 256, 0, s>>>(nt, w.Acopy, tiled, w.x, N, w.part);
     symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, w.part, w.r, N, w.y, -1.0);
-    symv_partials<float><<<dim3(ntile, B), 256, 0, s>>>(nt, w.A, tiled, w.r, N, w.part);
+    symv_partials<false><<<dim3(ntile, B), 256, 0, s>>>(nt, w.A, tiled, w.r, N, w.part);
     symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, w.part, w.x, N, w.x, 1.0);
     chi2_mixed<<<B, 256, 0, s>>>(n, N, N, w.y, w.x, w.ld, d_m2lnl, d_chi2, d_logdet);
+    count_launch(ctx, 7);
+    stage_mark(ctx, ST_ADJOINT, s);
     if (d_grad) {
         const size_t sma = sizeof(float) * (64 * 49 + 64 * 65 + 2 * 64 * 64);
         cudaFuncSetAttribute(contract_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma);
         contract_adj<<<dim3(ntile, (B + 63) / 64), 256, sma, s>>>(B, N, lp, w.U, w.A, tiled, w.x, w.gpart);
         adj_finish<<<B, 64, 0, s>>>(B, ntile, lmax, lp, w.gpart, w.cref, d_grad);
+        count_launch(ctx, 2);
     }
     if (d_status) CG_CUDA_TRY(ctx, cudaMemcpyAsync(d_status, w.st, sizeof(int) * B, cudaMemcpyDeviceToDevice, s));
+    stage_mark(ctx, ST_END, s);
     CG_CUDA_TRY(ctx, cudaGetLastError());
     return CG_OK;
 }

@@ -105,6 +105,15 @@ int cg_set_reference(cg_ctx* ctx, const double* cl_ref);
 /* number of reference (re)factorisations so far (mixed path) */
 int cg_reference_count(const cg_ctx* ctx);
 
+/* ---- instrumentation ------------------------------------------------------ */
+/* kernels this context has launched so far */
+long long cg_launch_count(const cg_ctx* ctx);
+/* record CUDA events between the stages of each cg_loglike* call */
+int cg_set_profiling(cg_ctx* ctx, int enable);
+/* per-stage device milliseconds of the last profiled call: ms[7] =
+   {build/contraction, cholesky, trtri, lauum, solve+refine, adjoint, 0} */
+int cg_stage_times(cg_ctx* ctx, double* ms);
+
 /* ---- Likelihood drop-in (source/likelihood.cpp:38-41,69-180) ------------- */
 /* construct from packed C, fiducial (nullable = 0) and noise, with optional
    foreground marginalisation; all host pointers, n(n+1)/2 doubles each */
