@@ -54,6 +54,11 @@ bool dalloc(T** p, size_t count)
 
 }  // namespace
 
+namespace cg {
+// error text for entry points that have no context (read with cg_last_error(NULL))
+void set_global_error(const std::string& msg) { g_create_error = msg; }
+}  // namespace cg
+
 extern "C" void cg_config_init(cg_config* cfg)
 {
     std::memset(cfg, 0, sizeof(*cfg));

@@ -125,6 +125,24 @@ double cg_likelihood_logdet(const cg_lik* lik);
 void cg_likelihood_destroy(cg_lik* lik);
 const char* cg_likelihood_last_error(const cg_lik* lik);
 
+/* No counterpart in the reference.  The same construct + calculate as
+   cg_likelihood_create / cg_likelihood_calculate, for one map, for callers
+   that cannot allocate device memory (code running inside another framework's
+   memory pool, plug-ins whose host owns every device allocation).  Inputs
+   d_c_packed, d_fid_packed (nullable = 0), d_noise_packed (n(n+1)/2 doubles
+   each) and d_t (n) and outputs d_out[2] = {chi2, raw ln det C} and d_status
+   (nullable; CG_OK or CG_ERR_NOT_PD) are all device pointers owned by the
+   caller; the call itself allocates nothing and runs asynchronously on
+   `stream`.  Its workspace is one static device array sized for n <= 768
+   (about 5.5 MB, held on every GPU that loads the library until exit); larger
+   n is rejected with CG_ERR_BAD_ARG (text in cg_last_error(NULL)).  Every call
+   shares that array: calls whose GPU work overlaps race and must be
+   serialised.  The first call on a device looks up the array's address, so
+   make it before capturing a CUDA graph on that device. */
+int cg_likelihood_noalloc(int n, const double* d_c_packed, const double* d_fid_packed,
+                          const double* d_noise_packed, const double* d_t, double* d_out, int* d_status,
+                          void* stream);
+
 /* ---- HEALPix geometry (host; Gorski et al. 2005) ------------------------ */
 long cg_nside2npix(long nside);
 long cg_ring2nest(long nside, long ipring);
