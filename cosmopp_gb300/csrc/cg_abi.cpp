@@ -126,7 +126,8 @@ extern "C" int cg_create(cg_ctx** out, const cg_config* cfg)
     for (double v : ctx->xyz)
         if (!std::isfinite(v)) { g_create_error = "non-finite direction"; return CG_ERR_NONFINITE; }
     ctx->lmax = cfg->lmax;
-    ctx->nt = (ctx->n + cg::TS - 1) / cg::TS;
+    // an even number of 64-tiles, so the tensor-core kernels can work on 128x128 supertiles
+    ctx->nt = 2 * ((ctx->n + 2 * cg::TS - 1) / (2 * cg::TS));
     ctx->N = ctx->nt * cg::TS;
     ctx->max_batch = cfg->max_batch;
     ctx->precision = cfg->precision;

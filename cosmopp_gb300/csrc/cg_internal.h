@@ -82,7 +82,7 @@ struct MixedWork {
     float* A = nullptr;          // [cap][tiled] I + K_b, then L_b, then V_b = (I + K_b)^-1
     float* Acopy = nullptr;      // [cap][tiled] I + K_b kept for the refinement residual
     float* M = nullptr;          // [cap][tiled] L_b^-1
-    float* Dinv = nullptr;       // [cap][nt][TS*TS]
+    float* Dinv = nullptr;       // [cap][nt/2][128*128] inverses of the 128x128 diagonal blocks of L_b (row-major)
     float* diag = nullptr;       // [cap][N]
     float* eps = nullptr;        // [cap][lpad] C_l / Cref_l - 1
     double* y = nullptr;         // [cap][N] L_ref^-1 d
@@ -92,6 +92,7 @@ struct MixedWork {
     float* gpart = nullptr;      // [tiles][cap][lpad] adjoint partials
     double* ld = nullptr;        // [cap] ln det C_b
     int* st = nullptr;           // [cap]
+    int* tcerr = nullptr;        // [1] set when a bounded tensor-core wait gave up
 };
 
 }  // namespace cg
@@ -164,6 +165,12 @@ template <typename T>
 int tiled_trtri(cg_ctx* ctx, int B, int nt, const T* L, const T* Dinv, T* M, size_t strideA, cudaStream_t s);
 template <typename T>
 int tiled_lauum(cg_ctx* ctx, int B, int nt, const T* M, T* V, size_t strideA, cudaStream_t s);
+// tensor-core FP32 (3xTF32) versions (k_tc.cu); d_err is set if a bounded wait gave up
+int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* M, float* V, size_t strideA, int* d_err, cudaStream_t s);
+int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, float* A, float* Linv, float* diag, int* status, size_t strideA,
+                      int* d_err, cudaStream_t s);
+int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* L, const float* Linv, float* M, size_t strideA, int* d_err,
+                   cudaStream_t s);
 // mixed path (k_mixed.cu)
 int mixed_prepare_reference(cg_ctx* ctx, const double* cl_ref_host);
 int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, const double* d_d, int d_stride,

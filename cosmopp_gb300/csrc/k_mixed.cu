@@ -314,6 +314,13 @@ __global__ void __launch_bounds__(256) chi2_mixed(int n, int N, int ystride, con
     }
 }
 
+// a tensor-core kernel whose bounded wait gave up marks every element of the batch
+__global__ void merge_tc_status(int B, int* __restrict__ err, int* __restrict__ status)
+{
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b < B && *err) status[b] = CG_ERR_TIMEOUT;
+}
+
 // broadcast y (one map) to every batch element: yb[b][i] = y[i]
 __global__ void broadcast_vec(int B, int N, const double* __restrict__ y, double* __restrict__ yb)
 {
@@ -419,7 +426,7 @@ void mixed_free(cg_ctx* ctx)
     cudaFree(w.Lref); cudaFree(w.Mref); cudaFree(w.Dinv_ref); cudaFree(w.diag_ref); cudaFree(w.Y); cudaFree(w.Z);
     cudaFree(w.U); cudaFree(w.A); cudaFree(w.M); cudaFree(w.Dinv); cudaFree(w.diag); cudaFree(w.eps); cudaFree(w.y);
     cudaFree(w.x); cudaFree(w.r); cudaFree(w.gpart); cudaFree(w.st); cudaFree(w.Acopy); cudaFree(w.cref);
-    cudaFree(w.ldref); cudaFree(w.part); cudaFree(w.ld);
+    cudaFree(w.ldref); cudaFree(w.part); cudaFree(w.ld); cudaFree(w.tcerr);
     w = MixedWork();
 }
 
@@ -438,6 +445,8 @@ static int ensure_ref_bufs(cg_ctx* ctx)
     if (!rc) rc = dalloc(ctx, &w.U, tiled * lp);
     if (!rc) rc = dalloc(ctx, &w.cref, (size_t)ctx->lmax + 1);
     if (!rc) rc = dalloc(ctx, &w.ldref, 1);
+    if (!rc) rc = dalloc(ctx, &w.tcerr, 1);
+    if (!rc) CG_CUDA_TRY(ctx, cudaMemset(w.tcerr, 0, sizeof(int)));
     if (rc) { mixed_free(ctx); return rc; }
     w.lpad = lp;
     return CG_OK;
@@ -458,7 +467,7 @@ static int ensure_batch_bufs(cg_ctx* ctx, int B)
     int rc = dalloc(ctx, &w.A, tiled * B);
     if (!rc) rc = dalloc(ctx, &w.Acopy, tiled * B);
     if (!rc) rc = dalloc(ctx, &w.M, tiled * B);
-    if (!rc) rc = dalloc(ctx, &w.Dinv, (size_t)B * nt * TILE_ELEMS);
+    if (!rc) rc = dalloc(ctx, &w.Dinv, (size_t)B * (nt / 2) * 128 * 128);
     if (!rc) rc = dalloc(ctx, &w.diag, (size_t)B * N);
     if (!rc) rc = dalloc(ctx, &w.eps, (size_t)B * lp);
     if (!rc) rc = dalloc(ctx, &w.y, (size_t)B * N);
@@ -602,13 +611,13 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
                                                                                         w.Acopy, tiled);
     }
     stage_mark(ctx, ST_CHOL, s);
-    if ((rc = tiled_cholesky<float>(ctx, B, nt, w.A, w.Dinv, w.diag, w.st, tiled, s))) return rc;
+    if ((rc = tiled_cholesky_tc(ctx, B, nt, w.A, w.Dinv, w.diag, w.st, tiled, w.tcerr, s))) return rc;
     logdet_mixed<<<B, 256, 0, s>>>(n, N, w.diag, w.ldref, w.ld);
     count_launch(ctx);
     stage_mark(ctx, ST_TRTRI, s);
-    if ((rc = tiled_trtri<float>(ctx, B, nt, w.A, w.Dinv, w.M, tiled, s))) return rc;
+    if ((rc = tiled_trtri_tc(ctx, B, nt, w.A, w.Dinv, w.M, tiled, w.tcerr, s))) return rc;
     stage_mark(ctx, ST_LAUUM, s);
-    if ((rc = tiled_lauum<float>(ctx, B, nt, w.M, w.A, tiled, s))) return rc;
+    if ((rc = tiled_lauum_tc(ctx, B, nt, w.M, w.A, tiled, w.tcerr, s))) return rc;
     stage_mark(ctx, ST_SOLVE, s);
     // x = V y; r = y - A x; x += V r
     symv_partials<false><<<dim3(ntile, B), 256, 0, s>>>(nt, w.A, tiled, w.y, N, w.part);
@@ -627,6 +636,8 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
         adj_finish<<<B, 64, 0, s>>>(B, ntile, lmax, lp, w.gpart, w.cref, d_grad);
         count_launch(ctx, 2);
     }
+    merge_tc_status<<<(B + 127) / 128, 128, 0, s>>>(B, w.tcerr, w.st);
+    count_launch(ctx);
     if (d_status) CG_CUDA_TRY(ctx, cudaMemcpyAsync(d_status, w.st, sizeof(int) * B, cudaMemcpyDeviceToDevice, s));
     stage_mark(ctx, ST_END, s);
     CG_CUDA_TRY(ctx, cudaGetLastError());
