@@ -48,14 +48,16 @@ __device__ __forceinline__ void put4(float* hi, float* lo, int r, int q, float4 
 constexpr uint32_t COL_R = 0, COL_S0 = 128, COL_S1 = 256, TMEM_COLS = 512;
 constexpr int SEG = 2;  // chunks per segment: 24 MMAs accumulate in TMEM before a drain
 
-// R (+)= S for this warp's 32 lanes: FP32 adds with round-to-nearest on the CUDA cores.  The
+// R (+)= S for this thread's lane: FP32 adds with round-to-nearest on the CUDA cores.  The
 // tensor core's own FP32 accumulation is not round-to-nearest, so long K loops drift; short
-// segments drained this way keep the sum at FP32 accuracy.
+// segments drained this way keep the sum at FP32 accuracy.  Warps 0-3 fold columns 0-63,
+// warps 4-7 columns 64-127 (warp w reaches TMEM lanes 32 (w % 4) .. + 31).
 __device__ __forceinline__ void drain(uint32_t tm, uint32_t scol, bool first)
 {
-    const uint32_t lane_off = (uint32_t)(32 * (threadIdx.x / 32)) << 16;
+    const uint32_t lane_off = (uint32_t)(32 * ((threadIdx.x / 32) % 4)) << 16;
+    const uint32_t c0 = 64 * (threadIdx.x / 128);
 #pragma unroll 1
-    for (uint32_t cc = 0; cc < 128; cc += 32) {
+    for (uint32_t cc = c0; cc < c0 + 64; cc += 32) {
         float sv[32];
         tmem_ld32(tm + lane_off + scol + cc, sv);
         if (!first) {
@@ -68,20 +70,26 @@ __device__ __forceinline__ void drain(uint32_t tm, uint32_t scol, bool first)
     }
 }
 
+constexpr int NTH = 256;  // threads per CTA: row r = t % 128, K half h = t / 128 (q in 4h .. 4h+3)
+
 // K loop: nchunks chunks; fa(c, r, q) / fb(c, r, q) return the float4 of row r, K columns
-// 4q..4q+3 of chunk c.  The result is left in tensor-memory columns COL_R .. COL_R + 127.
-// Returns false if an mbarrier wait gave up (the caller flags an error).
+// 4q..4q+3 of chunk c.  Loads run two chunks ahead of the MMAs.  The result is left in
+// tensor-memory columns COL_R .. COL_R + 127.  Returns false if an mbarrier wait gave up.
 template <class FA, class FB>
 __device__ bool tc_kloop(int nchunks, FA fa, FB fb, TcSmem& sm, uint64_t* bars, uint32_t tm)
 {
-    const int r = threadIdx.x;  // this thread's row of A and of B
-    float4 ra[KC / 4], rb[KC / 4];
+    const int r = threadIdx.x % 128, h = threadIdx.x / 128;
+    float4 pa0[4], pb0[4], pa1[4], pb1[4];
     bool ok = true;
     if (nchunks > 0) {
 #pragma unroll
-        for (int q = 0; q < KC / 4; ++q) { ra[q] = fa(0, r, q); rb[q] = fb(0, r, q); }
+        for (int q = 0; q < 4; ++q) { pa0[q] = fa(0, r, 4 * h + q); pb0[q] = fb(0, r, 4 * h + q); }
     }
-    for (int c = 0; c < nchunks; ++c) {
+    if (nchunks > 1) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) { pa1[q] = fa(1, r, 4 * h + q); pb1[q] = fb(1, r, 4 * h + q); }
+    }
+    auto step = [&](int c, float4 (&qa)[4], float4 (&qb)[4]) {
         const int st = c & 1, seg = c / SEG, pos = c % SEG;
         if (c >= 2) ok &= mbar_wait(&bars[st], ((c - 2) >> 1) & 1);  // MMAs of chunk c-2 done: stage free
         if (pos == 1 && seg >= 1) {
@@ -91,13 +99,13 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, TcSmem& sm, uint64_t* bars, 
             fence_before();
         }
 #pragma unroll
-        for (int q = 0; q < KC / 4; ++q) {
-            put4(sm.buf[st][0], sm.buf[st][1], r, q, ra[q]);
-            put4(sm.buf[st][2], sm.buf[st][3], r, q, rb[q]);
+        for (int q = 0; q < 4; ++q) {
+            put4(sm.buf[st][0], sm.buf[st][1], r, 4 * h + q, qa[q]);
+            put4(sm.buf[st][2], sm.buf[st][3], r, 4 * h + q, qb[q]);
         }
-        if (c + 1 < nchunks) {
+        if (c + 2 < nchunks) {
 #pragma unroll
-            for (int q = 0; q < KC / 4; ++q) { ra[q] = fa(c + 1, r, q); rb[q] = fb(c + 1, r, q); }
+            for (int q = 0; q < 4; ++q) { qa[q] = fa(c + 2, r, 4 * h + q); qb[q] = fb(c + 2, r, 4 * h + q); }
         }
         fence_proxy_async();
         __syncthreads();
@@ -116,6 +124,10 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, TcSmem& sm, uint64_t* bars, 
             }
             mma_commit(&bars[st]);
         }
+    };
+    for (int c = 0; c < nchunks; c += 2) {
+        step(c, pa0, pb0);
+        if (c + 1 < nchunks) step(c + 1, pa1, pb1);
     }
     // wait for the last chunk (its commit tracks every earlier MMA too) and fold the open segment(s)
     if (nchunks > 0) {
@@ -123,10 +135,7 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, TcSmem& sm, uint64_t* bars, 
         fence_after();
         const int last_seg = (nchunks - 1) / SEG;
         const int last_pos = (nchunks - 1) % SEG;
-        if (last_seg >= 1 && last_pos == 0) {
-            // segment last_seg-1 was closed by chunk nchunks-2 but not drained yet (no chunk at pos 1 followed)
-            drain(tm, (last_seg - 1) & 1 ? COL_S1 : COL_S0, last_seg == 1);
-        }
+        if (last_seg >= 1 && last_pos == 0) drain(tm, (last_seg - 1) & 1 ? COL_S1 : COL_S0, last_seg == 1);
         drain(tm, last_seg & 1 ? COL_S1 : COL_S0, last_seg == 0);
         fence_before();
     }
@@ -145,14 +154,14 @@ constexpr float4 kZero4 = {0.f, 0.f, 0.f, 0.f};
 constexpr int LINV = 128 * 128;  // floats per 128x128 diagonal-block inverse
 
 // the accumulator row this thread holds in TMEM (warp w: lanes 32w..32w+31)
-__device__ __forceinline__ uint32_t lane_base() { return (uint32_t)(32 * (threadIdx.x / 32)) << 16; }
+__device__ __forceinline__ uint32_t lane_base() { return (uint32_t)(32 * ((threadIdx.x / 32) % 4)) << 16; }
 
 // write the 128x128 result in R (times sgn) into the four column-major tiles of supertile (I2, J2)
 // (skipping the tile above the diagonal of a diagonal supertile)
 __device__ __forceinline__ void store_block(uint32_t tm, float* base, int I2, int J2, float sgn)
 {
-    const int row = threadIdx.x;
-    for (int cc = 0; cc < 128; cc += 32) {
+    const int row = threadIdx.x % 128, c0 = 64 * (threadIdx.x / 128);
+    for (int cc = c0; cc < c0 + 64; cc += 32) {
         float v[32];
         tmem_ld32(tm + lane_base() + COL_R + cc, v);
         const int ti = 2 * I2 + row / 64, tj = 2 * J2 + cc / 64;
@@ -204,34 +213,70 @@ __device__ __forceinline__ void tc_rearm(TcCtl& ctl)
 }
 
 // Cholesky of the 128x128 block in s (column-major, leading dimension 129, lower part used)
-// and the inverse of its factor into inv (same layout); 128 threads.  Sets *bad on a
-// non-positive pivot.
-__device__ void factor_block128(float* s, float* inv, int* bad)
+// and the inverse of its factor into inv (same layout); 256 threads.  Panels of 8 columns
+// factorised column by column, then one rank-8 update of the trailing block.  The inverse is
+// block-recursive: inv11 = L11^-1, inv22 = L22^-1 (in parallel), inv21 = -inv22 (L21 inv11),
+// with tmp a 64x65 scratch block.  Sets *bad on a non-positive pivot.
+__device__ void factor_block128(float* s, float* inv, float* tmp, int* bad)
 {
     constexpr int L = 129;
     const int t = threadIdx.x;
-    for (int c = 0; c < 128; ++c) {
-        if (t == 0) {
-            float v = s[c * L + c];
-            if (!(v > 0.f)) { *bad = 1; v = 1.f; }
-            s[c * L + c] = sqrtf(v);
+    for (int kb = 0; kb < 128; kb += 8) {
+        for (int c = kb; c < kb + 8; ++c) {
+            if (t == 0) {
+                float v = s[c * L + c];
+                if (!(v > 0.f)) { *bad = 1; v = 1.f; }
+                s[c * L + c] = sqrtf(v);
+            }
+            __syncthreads();
+            const float piv = s[c * L + c];
+            if (t > c && t < 128) s[c * L + t] /= piv;
+            __syncthreads();
+            const int nq = kb + 7 - c;  // remaining panel columns c+1 .. kb+7
+            for (int e = t; e < nq * 128; e += NTH) {
+                const int q = c + 1 + e / 128, rr = e % 128;
+                if (rr >= q) s[q * L + rr] -= s[c * L + rr] * s[c * L + q];
+            }
+            __syncthreads();
         }
-        __syncthreads();
-        const float piv = s[c * L + c];
-        if (t > c) s[c * L + t] /= piv;
-        __syncthreads();
-        if (t > c) {  // column q = t of the trailing block: rows r >= q
-            const float lq = s[c * L + t];
-            for (int r = t; r < 128; ++r) s[t * L + r] -= s[c * L + r] * lq;
+        const int q0 = kb + 8;
+        for (int e = t; e < (128 - q0) * 128; e += NTH) {
+            const int q = q0 + e / 128, rr = e % 128;
+            if (rr < q) continue;
+            float acc = s[q * L + rr];
+#pragma unroll
+            for (int c = 0; c < 8; ++c) acc -= s[(kb + c) * L + rr] * s[(kb + c) * L + q];
+            s[q * L + rr] = acc;
         }
         __syncthreads();
     }
-    // column t of the inverse by forward substitution
-    for (int r = 0; r < 128; ++r) {
-        if (r < t) { inv[t * L + r] = 0.f; continue; }
-        float acc = (r == t) ? 1.f : 0.f;
-        for (int m = t; m < r; ++m) acc -= s[m * L + r] * inv[t * L + m];
-        inv[t * L + r] = acc / s[r * L + r];
+    // diagonal 64-blocks: thread t < 64 -> column t of L11^-1, 128 <= t < 192 -> column t-128 of L22^-1
+    if (t < 64 || (t >= 128 && t < 192)) {
+        const int off = (t < 64) ? 0 : 64;
+        const int col = off + (t % 64);
+        for (int r = off; r < off + 64; ++r) {
+            if (r < col) { inv[col * L + r] = 0.f; continue; }
+            float acc = (r == col) ? 1.f : 0.f;
+            for (int m = col; m < r; ++m) acc -= s[m * L + r] * inv[col * L + m];
+            inv[col * L + r] = acc / s[r * L + r];
+        }
+    }
+    __syncthreads();
+    // tmp = L21 inv11 (rows 64..127, cols 0..63 of L times inv11)
+    for (int e = t; e < 64 * 64; e += NTH) {
+        const int rr = e % 64, cc = e / 64;
+        float acc = 0.f;
+        for (int m = cc; m < 64; ++m) acc += s[m * L + 64 + rr] * inv[cc * L + m];
+        tmp[cc * 65 + rr] = acc;
+    }
+    __syncthreads();
+    // inv21 = -inv22 tmp; inv12 = 0
+    for (int e = t; e < 64 * 64; e += NTH) {
+        const int rr = e % 64, cc = e / 64;
+        float acc = 0.f;
+        for (int m = 0; m <= rr; ++m) acc += inv[(64 + m) * L + 64 + rr] * tmp[cc * 65 + m];
+        inv[cc * L + 64 + rr] = -acc;
+        inv[(64 + cc) * L + rr] = 0.f;
     }
     __syncthreads();
 }
@@ -239,7 +284,7 @@ __device__ void factor_block128(float* s, float* inv, int* bad)
 // Left-looking Cholesky, column block J2, row block I2 = J2 + blockIdx.x; grid (nt2 - J2, B).
 // Off-diagonal blocks: A_IJ <- A_IJ - sum_{k < 2 J2} L_I,k L_J,k^T (S, stored in place).
 // Diagonal block: S_JJ factorised to L_JJ (in place), its diagonal to diag, its inverse to Linv.
-__global__ void __launch_bounds__(128) chol_tc_update(int J2, int nt, float* __restrict__ A, size_t strideA,
+__global__ void __launch_bounds__(NTH) chol_tc_update(int J2, int nt, float* __restrict__ A, size_t strideA,
                                                       float* __restrict__ Linv, float* __restrict__ diag,
                                                       int* __restrict__ status, int* __restrict__ err)
 {
@@ -261,10 +306,10 @@ __global__ void __launch_bounds__(128) chol_tc_update(int J2, int nt, float* __r
     bool ok = true;
     if (nchunks > 0) ok = tc_kloop(nchunks, fa, fb, sm, ctl.bars, tm);
     if (!ok && threadIdx.x == 0) atomicExch(err, 1);
-    const int row = threadIdx.x;
+    const int row = threadIdx.x % 128, c0 = 64 * (threadIdx.x / 128);
     if (I2 > J2) {
         if (nchunks > 0) {
-            for (int cc = 0; cc < 128; cc += 32) {
+            for (int cc = c0; cc < c0 + 64; cc += 32) {
                 float v[32];
                 tmem_ld32(tm + lane_base() + COL_R + cc, v);
                 float* t = Ab + (size_t)tile_index(2 * I2 + row / 64, 2 * J2 + cc / 64) * TILE_ELEMS;
@@ -278,8 +323,9 @@ __global__ void __launch_bounds__(128) chol_tc_update(int J2, int nt, float* __r
     // diagonal block: S = A_JJ - P into shared memory (column-major, ld 129), lower part
     float* s = reinterpret_cast<float*>(smem_raw);
     float* inv = s + 128 * 129;
+    float* tmp = inv + 128 * 129;
     __syncthreads();
-    for (int cc = 0; cc < 128; cc += 32) {
+    for (int cc = c0; cc < c0 + 64; cc += 32) {
         float v[32];
         if (nchunks > 0) tmem_ld32(tm + lane_base() + COL_R + cc, v);
         else {
@@ -296,23 +342,23 @@ __global__ void __launch_bounds__(128) chol_tc_update(int J2, int nt, float* __r
         }
     }
     __syncthreads();
-    factor_block128(s, inv, &ctl.bad);
+    factor_block128(s, inv, tmp, &ctl.bad);
     // L_JJ into the three lower tiles (strict upper of the diagonal tiles zeroed), diag, Linv row-major
-    for (int col = 0; col < 128; ++col) {
+    for (int col = c0; col < c0 + 64; ++col) {
         const int ti = 2 * J2 + row / 64, tj = 2 * J2 + col / 64;
         if (tj > ti) continue;
         float* t = Ab + (size_t)tile_index(ti, tj) * TILE_ELEMS;
         t[(row % 64) + TS * (col % 64)] = (row >= col) ? s[col * 129 + row] : 0.f;
     }
-    diag[(size_t)b * nt * TS + J2 * 128 + row] = s[row * 129 + row];
+    if (threadIdx.x < 128) diag[(size_t)b * nt * TS + J2 * 128 + row] = s[row * 129 + row];
     float* li = Linv + ((size_t)b * nt2 + J2) * LINV;
-    for (int col = 0; col < 128; ++col) li[row * 128 + col] = inv[col * 129 + row];
+    for (int col = c0; col < c0 + 64; ++col) li[row * 128 + col] = inv[col * 129 + row];
     if (threadIdx.x == 0 && ctl.bad && status && status[b] == CG_OK) status[b] = CG_ERR_NOT_PD;
     tc_end(tm);
 }
 
 // L_IJ = S_IJ Linv_J^T for I2 = J2 + 1 + blockIdx.x; grid (nt2 - J2 - 1, B)
-__global__ void __launch_bounds__(128) chol_tc_panel(int J2, int nt, float* __restrict__ A, size_t strideA,
+__global__ void __launch_bounds__(NTH) chol_tc_panel(int J2, int nt, float* __restrict__ A, size_t strideA,
                                                      const float* __restrict__ Linv, int* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
@@ -337,7 +383,7 @@ __global__ void __launch_bounds__(128) chol_tc_panel(int J2, int nt, float* __re
 }
 
 // Row block I2 of M = L^-1; CTA J2 = blockIdx.x <= I2; grid (I2 + 1, B)
-__global__ void __launch_bounds__(128) trtri_tc_row(int I2, int nt, const float* __restrict__ Lm,
+__global__ void __launch_bounds__(NTH) trtri_tc_row(int I2, int nt, const float* __restrict__ Lm,
                                                     const float* __restrict__ Linv, float* __restrict__ M,
                                                     size_t strideA, int* __restrict__ err)
 {
@@ -348,9 +394,9 @@ __global__ void __launch_bounds__(128) trtri_tc_row(int I2, int nt, const float*
     const float* Lb = Lm + (size_t)b * strideA;
     float* Mb = M + (size_t)b * strideA;
     const float* li = Linv + ((size_t)b * nt2 + I2) * LINV;
-    const int row = threadIdx.x;
+    const int row = threadIdx.x % 128, c0 = 64 * (threadIdx.x / 128);
     if (J2 == I2) {  // M_II = Linv_I, into the three lower column-major tiles
-        for (int col = 0; col < 128; ++col) {
+        for (int col = c0; col < c0 + 64; ++col) {
             const int ti = 2 * I2 + row / 64, tj = 2 * I2 + col / 64;
             if (tj > ti) continue;
             Mb[(size_t)tile_index(ti, tj) * TILE_ELEMS + (row % 64) + TS * (col % 64)] = li[row * 128 + col];
@@ -396,23 +442,17 @@ __global__ void __launch_bounds__(128) trtri_tc_row(int I2, int nt, const float*
 
 // V_IJ (128x128 supertile, lower) = sum over k of M_k,I^T M_k,J with M column-major tiles.
 // grid (supertiles of the lower triangle, B), 128 threads.
-__global__ void __launch_bounds__(128) lauum_tc(int nt, const float* __restrict__ M, float* __restrict__ V,
+__global__ void __launch_bounds__(NTH) lauum_tc(int nt, const float* __restrict__ M, float* __restrict__ V,
                                                 size_t strideA, int* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     TcSmem& sm = *reinterpret_cast<TcSmem*>(smem_raw);
-    __shared__ uint64_t bars[2];
-    __shared__ uint32_t tbase;
+    __shared__ TcCtl ctl;
     int I2, J2;
     tile_coords(blockIdx.x, I2, J2);
     const int b = blockIdx.y;
     const float* Mb = M + (size_t)b * strideA;
-    if (threadIdx.x < 32) tmem_alloc(&tbase, TMEM_COLS);
-    if (threadIdx.x == 0) { mbar_init(&bars[0], 1); mbar_init(&bars[1], 1); }
-    fence_before();
-    __syncthreads();
-    fence_after();
-    const uint32_t tm = tbase;
+    const uint32_t tm = tc_begin(ctl);
     const int k0 = 2 * I2;                     // first tile row with a non-zero M_k,row
     const int nchunks = (nt - k0) * (TS / KC);
     // A(r, m) = M_{k, 2I2 + r/64}(m, r%64): tile (k, col) column-major, element (m, r') at m + 64 r'
@@ -428,29 +468,19 @@ __global__ void __launch_bounds__(128) lauum_tc(int nt, const float* __restrict_
         const float* t = Mb + (size_t)tile_index(k, col) * TILE_ELEMS;
         return ld4(t + (r % 64) * TS + (c % 2) * KC + 4 * q);
     };
-    const bool ok = tc_kloop(nchunks, fa, fb, sm, bars, tm);
+    const bool ok = tc_kloop(nchunks, fa, fb, sm, ctl.bars, tm);
     if (!ok && threadIdx.x == 0) atomicExch(err, 1);
-    // epilogue: warp w holds rows 32w..32w+31; write column-major tiles (coalesced per column)
-    const int w = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const int row = 32 * w + lane;
-    float* Vb = V + (size_t)b * strideA;
-    for (int cc = 0; cc < 128; cc += 32) {
-        float v[32];
-        tmem_ld32(tm + ((uint32_t)(32 * w) << 16) + COL_R + cc, v);
-        const int ti = 2 * I2 + row / 64, tj = 2 * J2 + cc / 64;
-        if (tj > ti) continue;  // above the diagonal of a diagonal supertile
-        float* t = Vb + (size_t)tile_index(ti, tj) * TILE_ELEMS;
-#pragma unroll
-        for (int i = 0; i < 32; ++i) t[(row % 64) + TS * ((cc % 64) + i)] = v[i];
-    }
-    fence_before();
-    __syncthreads();
-    if (threadIdx.x < 32) tmem_dealloc(tm, TMEM_COLS);
+    store_block(tm, V + (size_t)b * strideA, I2, J2, 1.f);
+    tc_end(tm);
 }
 
 }  // namespace
 
-static size_t tc_smem() { return sizeof(TcSmem) > 2 * 128 * 129 * 4 ? sizeof(TcSmem) : 2 * 128 * 129 * 4; }
+static size_t tc_smem()
+{
+    const size_t fac = (2 * 128 * 129 + 64 * 65) * sizeof(float);  // block, its inverse, scratch
+    return sizeof(TcSmem) > fac ? sizeof(TcSmem) : fac;
+}
 
 int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, float* A, float* Linv, float* diag, int* status, size_t strideA,
                       int* d_err, cudaStream_t s)
@@ -465,10 +495,10 @@ int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, float* A, float* Linv, float* 
     }
     const int nt2 = nt / 2;
     for (int J2 = 0; J2 < nt2; ++J2) {
-        chol_tc_update<<<dim3(nt2 - J2, B), 128, smem, s>>>(J2, nt, A, strideA, Linv, diag, status, d_err);
+        chol_tc_update<<<dim3(nt2 - J2, B), NTH, smem, s>>>(J2, nt, A, strideA, Linv, diag, status, d_err);
         count_launch(ctx);
         if (J2 + 1 < nt2) {
-            chol_tc_panel<<<dim3(nt2 - J2 - 1, B), 128, smem, s>>>(J2, nt, A, strideA, Linv, d_err);
+            chol_tc_panel<<<dim3(nt2 - J2 - 1, B), NTH, smem, s>>>(J2, nt, A, strideA, Linv, d_err);
             count_launch(ctx);
         }
     }
@@ -488,7 +518,7 @@ int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* L, const float* Linv
     }
     const int nt2 = nt / 2;
     for (int I2 = 0; I2 < nt2; ++I2) {
-        trtri_tc_row<<<dim3(I2 + 1, B), 128, smem, s>>>(I2, nt, L, Linv, M, strideA, d_err);
+        trtri_tc_row<<<dim3(I2 + 1, B), NTH, smem, s>>>(I2, nt, L, Linv, M, strideA, d_err);
         count_launch(ctx);
     }
     CG_CUDA_TRY(ctx, cudaGetLastError());
@@ -498,14 +528,14 @@ int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* L, const float* Linv
 int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* M, float* V, size_t strideA, int* d_err, cudaStream_t s)
 {
     if (nt % 2) { ctx->err = "tensor-core lauum needs an even tile count"; return CG_ERR_BAD_ARG; }
-    const int smem = (int)sizeof(TcSmem) + 1024;
+    const int smem = (int)tc_smem() + 1024;
     static bool attr = false;
     if (!attr) {
         CG_CUDA_TRY(ctx, cudaFuncSetAttribute(lauum_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
         attr = true;
     }
     const int nt2 = nt / 2;
-    lauum_tc<<<dim3(nt2 * (nt2 + 1) / 2, B), 128, smem, s>>>(nt, M, V, strideA, d_err);
+    lauum_tc<<<dim3(nt2 * (nt2 + 1) / 2, B), NTH, smem, s>>>(nt, M, V, strideA, d_err);
     count_launch(ctx);
     CG_CUDA_TRY(ctx, cudaGetLastError());
     return CG_OK;
