@@ -45,12 +45,20 @@ __global__ void __launch_bounds__(NT_THREADS) chol_diag(int k, int nt, T* A, siz
     __shared__ int bad;
     const int b = blockIdx.x;
     T* tile = A + (size_t)b * strideA + (size_t)tile_index(k, k) * TILE_ELEMS;
-    for (int e = threadIdx.x; e < TILE_ELEMS; e += blockDim.x) s[(e / TS) * L + (e % TS)] = tile[e];
+    // The trailing updates are summed in u (sinv's storage, unused until the inverse) and
+    // subtracted from the column once, when it is reached.  Subtracting each rank-1 term
+    // from A directly loses every term below half an ulp of A's diagonal (about 1 for a
+    // whitened matrix), which biases L's diagonal, hence the log-determinant, upwards.
+    T* u = sinv;
+    for (int e = threadIdx.x; e < TILE_ELEMS; e += blockDim.x) {
+        s[(e / TS) * L + (e % TS)] = tile[e];
+        u[(e / TS) * L + (e % TS)] = T(0);
+    }
     if (threadIdx.x == 0) bad = 0;
     __syncthreads();
     for (int c = 0; c < TS; ++c) {
         if (threadIdx.x == 0) {
-            T v = s[c * L + c];
+            T v = s[c * L + c] - u[c * L + c];
             if (!(v > T(0))) {  // not positive definite (or NaN): flag, keep going on a benign value
                 bad = 1;
                 v = T(1);
@@ -59,7 +67,7 @@ __global__ void __launch_bounds__(NT_THREADS) chol_diag(int k, int nt, T* A, siz
         }
         __syncthreads();
         const T piv = s[c * L + c];
-        for (int r = c + 1 + threadIdx.x; r < TS; r += blockDim.x) s[c * L + r] /= piv;
+        for (int r = c + 1 + threadIdx.x; r < TS; r += blockDim.x) s[c * L + r] = (s[c * L + r] - u[c * L + r]) / piv;
         __syncthreads();
         const int m = TS - c - 1;  // trailing triangle of size m
         const int cnt = m * (m + 1) / 2;
@@ -67,7 +75,7 @@ __global__ void __launch_bounds__(NT_THREADS) chol_diag(int k, int nt, T* A, siz
             int rr, ss;
             tile_coords(e, rr, ss);  // rr >= ss within the trailing block
             const int r = c + 1 + rr, q = c + 1 + ss;
-            s[q * L + r] -= s[c * L + r] * s[c * L + q];
+            u[q * L + r] += s[c * L + r] * s[c * L + q];
         }
         __syncthreads();
     }

@@ -1,7 +1,12 @@
 // Tensor-core (tcgen05, kind::tf32) tile products for the FP32 whitened
 // matrices of the mixed path, at FP32 accuracy by the 3xTF32 split
-// a*b ~ a_hi*b_hi + a_hi*b_lo + a_lo*b_hi (a_hi = the 19 bits the tensor core
-// reads, a_lo = a - a_hi), accumulated in FP32 in tensor memory.
+// a*b ~ a_hi*b_hi + a_hi*b_lo + a_lo*b_hi with a_hi = a rounded to nearest TF32
+// and a_lo = a - a_hi rounded to nearest TF32 (unbiased; truncating instead
+// biases sums of squares).  The tensor core's FP32 accumulation is not
+// round-to-nearest and drifts by ~0.4 ulp per instruction, always the same
+// way, so each chunk accumulates the hi*hi products (4 MMAs) and the
+// correction products (8 MMAs) in separate tensor-memory accumulators that are
+// folded into a per-thread FP32 register sum (round-to-nearest) one chunk later.
 //
 // One CTA (128 threads) owns a 128x128 output supertile (2x2 of the 64x64
 // storage tiles) and runs a K loop over 32-wide chunks: every thread loads
@@ -39,46 +44,46 @@ struct TcSmem {
 __device__ __forceinline__ void put4(float* hi, float* lo, int r, int q, float4 v)
 {
     const uint32_t o = kmajor_offset(r, 4 * q, KC) / 4;
-    float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
-    *reinterpret_cast<float4*>(hi + o) = v;
-    *reinterpret_cast<float4*>(lo + o) = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+    const float4 h = make_float4(tf32_rn(v.x), tf32_rn(v.y), tf32_rn(v.z), tf32_rn(v.w));
+    *reinterpret_cast<float4*>(hi + o) = h;
+    *reinterpret_cast<float4*>(lo + o) =
+        make_float4(tf32_rn(v.x - h.x), tf32_rn(v.y - h.y), tf32_rn(v.z - h.z), tf32_rn(v.w - h.w));
 }
 
-// Tensor-memory columns: R (running sum) at 0, segment accumulators S0 / S1 at 128 / 256.
-constexpr uint32_t COL_R = 0, COL_S0 = 128, COL_S1 = 256, TMEM_COLS = 512;
-constexpr int SEG = 2;  // chunks per segment: 24 MMAs accumulate in TMEM before a drain
+// Tensor-memory columns: two accumulator sets (chunk parity), each a hi*hi accumulator and a
+// correction accumulator of 128 columns.
+constexpr uint32_t TMEM_COLS = 512;
+__device__ __forceinline__ uint32_t col_main(int set) { return 256u * set; }
+__device__ __forceinline__ uint32_t col_corr(int set) { return 256u * set + 128u; }
 
-// R (+)= S for this thread's lane: FP32 adds with round-to-nearest on the CUDA cores.  The
-// tensor core's own FP32 accumulation is not round-to-nearest, so long K loops drift; short
-// segments drained this way keep the sum at FP32 accuracy.  Warps 0-3 fold columns 0-63,
-// warps 4-7 columns 64-127 (warp w reaches TMEM lanes 32 (w % 4) .. + 31).
-__device__ __forceinline__ void drain(uint32_t tm, uint32_t scol, bool first)
+// R[j] += (main + corr) for this thread's row (lane) and its 64 columns (64 h + j): warps 0-3
+// fold columns 0-63, warps 4-7 columns 64-127 (warp w reaches TMEM lanes 32 (w % 4) .. + 31).
+__device__ __forceinline__ void drain(uint32_t tm, int set, float (&R)[64])
 {
     const uint32_t lane_off = (uint32_t)(32 * ((threadIdx.x / 32) % 4)) << 16;
     const uint32_t c0 = 64 * (threadIdx.x / 128);
-#pragma unroll 1
-    for (uint32_t cc = c0; cc < c0 + 64; cc += 32) {
-        float sv[32];
-        tmem_ld32(tm + lane_off + scol + cc, sv);
-        if (!first) {
-            float rv[32];
-            tmem_ld32(tm + lane_off + COL_R + cc, rv);
 #pragma unroll
-            for (int i = 0; i < 32; ++i) sv[i] += rv[i];
-        }
-        tmem_st32(tm + lane_off + COL_R + cc, sv);
+    for (int part = 0; part < 4; ++part) {
+        float m[16], c[16];
+        tmem_ld16(tm + lane_off + col_main(set) + c0 + 16 * part, m);
+        tmem_ld16(tm + lane_off + col_corr(set) + c0 + 16 * part, c);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) R[16 * part + i] += m[i] + c[i];
     }
 }
 
 constexpr int NTH = 256;  // threads per CTA: row r = t % 128, K half h = t / 128 (q in 4h .. 4h+3)
 
 // K loop: nchunks chunks; fa(c, r, q) / fb(c, r, q) return the float4 of row r, K columns
-// 4q..4q+3 of chunk c.  Loads run two chunks ahead of the MMAs.  The result is left in
-// tensor-memory columns COL_R .. COL_R + 127.  Returns false if an mbarrier wait gave up.
+// 4q..4q+3 of chunk c.  Loads run two chunks ahead of the MMAs.  On return R[j] holds the
+// product for row t % 128, column 64 (t / 128) + j (0 if nchunks == 0).  Returns false if an
+// mbarrier wait gave up.
 template <class FA, class FB>
-__device__ bool tc_kloop(int nchunks, FA fa, FB fb, TcSmem& sm, uint64_t* bars, uint32_t tm)
+__device__ bool tc_kloop(int nchunks, FA fa, FB fb, TcSmem& sm, uint64_t* bars, uint32_t tm, float (&R)[64])
 {
     const int r = threadIdx.x % 128, h = threadIdx.x / 128;
+#pragma unroll
+    for (int j = 0; j < 64; ++j) R[j] = 0.f;
     float4 pa0[4], pb0[4], pa1[4], pb1[4];
     bool ok = true;
     if (nchunks > 0) {
@@ -90,12 +95,12 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, TcSmem& sm, uint64_t* bars, 
         for (int q = 0; q < 4; ++q) { pa1[q] = fa(1, r, 4 * h + q); pb1[q] = fb(1, r, 4 * h + q); }
     }
     auto step = [&](int c, float4 (&qa)[4], float4 (&qb)[4]) {
-        const int st = c & 1, seg = c / SEG, pos = c % SEG;
-        if (c >= 2) ok &= mbar_wait(&bars[st], ((c - 2) >> 1) & 1);  // MMAs of chunk c-2 done: stage free
-        if (pos == 1 && seg >= 1) {
-            // chunk c-2 closed segment seg-1 (SEG == 2): fold it into R while segment seg runs
+        const int st = c & 1;
+        if (c >= 2) {
+            // MMAs of chunk c-2 done: its stage is free and its accumulators are folded into R
+            ok &= mbar_wait(&bars[st], ((c - 2) >> 1) & 1);
             fence_after();
-            drain(tm, (seg - 1) & 1 ? COL_S1 : COL_S0, seg == 1);
+            drain(tm, st, R);
             fence_before();
         }
 #pragma unroll
@@ -111,16 +116,15 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, TcSmem& sm, uint64_t* bars, 
         __syncthreads();
         if (threadIdx.x == 0) {
             fence_after();
-            const uint32_t acc_col = (seg & 1) ? COL_S1 : COL_S0;
             const uint32_t ah = smem_u32(sm.buf[st][0]), al = smem_u32(sm.buf[st][1]);
             const uint32_t bh = smem_u32(sm.buf[st][2]), bl = smem_u32(sm.buf[st][3]);
 #pragma unroll
             for (int kk = 0; kk < KC / 8; ++kk) {
                 const uint32_t off = kk * 2 * LBO;
-                const uint32_t first = (pos == 0 && kk == 0) ? 0u : 1u;
-                mma_tf32(tm + acc_col, smem_desc(al + off, LBO, SBO), smem_desc(bh + off, LBO, SBO), IDESC, first);
-                mma_tf32(tm + acc_col, smem_desc(ah + off, LBO, SBO), smem_desc(bl + off, LBO, SBO), IDESC, 1u);
-                mma_tf32(tm + acc_col, smem_desc(ah + off, LBO, SBO), smem_desc(bh + off, LBO, SBO), IDESC, 1u);
+                const uint32_t acc = kk ? 1u : 0u;
+                mma_tf32(tm + col_corr(st), smem_desc(al + off, LBO, SBO), smem_desc(bh + off, LBO, SBO), IDESC, acc);
+                mma_tf32(tm + col_corr(st), smem_desc(ah + off, LBO, SBO), smem_desc(bl + off, LBO, SBO), IDESC, 1u);
+                mma_tf32(tm + col_main(st), smem_desc(ah + off, LBO, SBO), smem_desc(bh + off, LBO, SBO), IDESC, acc);
             }
             mma_commit(&bars[st]);
         }
@@ -129,14 +133,12 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, TcSmem& sm, uint64_t* bars, 
         step(c, pa0, pb0);
         if (c + 1 < nchunks) step(c + 1, pa1, pb1);
     }
-    // wait for the last chunk (its commit tracks every earlier MMA too) and fold the open segment(s)
+    // the last one or two chunks: wait for the last commit (it tracks every earlier MMA) and fold
     if (nchunks > 0) {
         ok &= mbar_wait(&bars[(nchunks - 1) & 1], ((nchunks - 1) >> 1) & 1);
         fence_after();
-        const int last_seg = (nchunks - 1) / SEG;
-        const int last_pos = (nchunks - 1) % SEG;
-        if (last_seg >= 1 && last_pos == 0) drain(tm, (last_seg - 1) & 1 ? COL_S1 : COL_S0, last_seg == 1);
-        drain(tm, last_seg & 1 ? COL_S1 : COL_S0, last_seg == 0);
+        if (nchunks >= 2) drain(tm, (nchunks - 2) & 1, R);
+        drain(tm, (nchunks - 1) & 1, R);
         fence_before();
     }
     return ok;
@@ -156,20 +158,16 @@ constexpr int LINV = 128 * 128;  // floats per 128x128 diagonal-block inverse
 // the accumulator row this thread holds in TMEM (warp w: lanes 32w..32w+31)
 __device__ __forceinline__ uint32_t lane_base() { return (uint32_t)(32 * ((threadIdx.x / 32) % 4)) << 16; }
 
-// write the 128x128 result in R (times sgn) into the four column-major tiles of supertile (I2, J2)
-// (skipping the tile above the diagonal of a diagonal supertile)
-__device__ __forceinline__ void store_block(uint32_t tm, float* base, int I2, int J2, float sgn)
+// write the 128x128 result (this thread: row t % 128, columns 64 (t / 128) + j in R) times sgn
+// into the column-major tiles of supertile (I2, J2), skipping the tile above the diagonal
+__device__ __forceinline__ void store_block(const float (&R)[64], float* base, int I2, int J2, float sgn)
 {
-    const int row = threadIdx.x % 128, c0 = 64 * (threadIdx.x / 128);
-    for (int cc = c0; cc < c0 + 64; cc += 32) {
-        float v[32];
-        tmem_ld32(tm + lane_base() + COL_R + cc, v);
-        const int ti = 2 * I2 + row / 64, tj = 2 * J2 + cc / 64;
-        if (tj > ti) continue;
-        float* t = base + (size_t)tile_index(ti, tj) * TILE_ELEMS;
+    const int row = threadIdx.x % 128, h = threadIdx.x / 128;
+    const int ti = 2 * I2 + row / 64, tj = 2 * J2 + h;
+    if (tj > ti) return;
+    float* t = base + (size_t)tile_index(ti, tj) * TILE_ELEMS;
 #pragma unroll
-        for (int i = 0; i < 32; ++i) t[(row % 64) + TS * ((cc % 64) + i)] = sgn * v[i];
-    }
+    for (int j = 0; j < 64; ++j) t[(row % 64) + TS * j] = sgn * R[j];
 }
 
 struct TcCtl {
@@ -221,21 +219,27 @@ __device__ void factor_block128(float* s, float* inv, float* tmp, int* bad)
 {
     constexpr int L = 129;
     const int t = threadIdx.x;
+    // Trailing updates are summed in u (inv's storage, free until the inverse) and subtracted
+    // once per column: subtracting each term from s directly drops the terms below half an
+    // ulp of the diagonal (about 1 after whitening) and biases the log-determinant upwards.
+    float* u = inv;
+    for (int e = t; e < 128 * 128; e += NTH) u[(e / 128) * L + e % 128] = 0.f;
+    __syncthreads();
     for (int kb = 0; kb < 128; kb += 8) {
         for (int c = kb; c < kb + 8; ++c) {
             if (t == 0) {
-                float v = s[c * L + c];
+                float v = s[c * L + c] - u[c * L + c];
                 if (!(v > 0.f)) { *bad = 1; v = 1.f; }
                 s[c * L + c] = sqrtf(v);
             }
             __syncthreads();
             const float piv = s[c * L + c];
-            if (t > c && t < 128) s[c * L + t] /= piv;
+            if (t > c && t < 128) s[c * L + t] = (s[c * L + t] - u[c * L + t]) / piv;
             __syncthreads();
             const int nq = kb + 7 - c;  // remaining panel columns c+1 .. kb+7
             for (int e = t; e < nq * 128; e += NTH) {
                 const int q = c + 1 + e / 128, rr = e % 128;
-                if (rr >= q) s[q * L + rr] -= s[c * L + rr] * s[c * L + q];
+                if (rr >= q) u[q * L + rr] += s[c * L + rr] * s[c * L + q];
             }
             __syncthreads();
         }
@@ -243,10 +247,10 @@ __device__ void factor_block128(float* s, float* inv, float* tmp, int* bad)
         for (int e = t; e < (128 - q0) * 128; e += NTH) {
             const int q = q0 + e / 128, rr = e % 128;
             if (rr < q) continue;
-            float acc = s[q * L + rr];
+            float acc = u[q * L + rr];
 #pragma unroll
-            for (int c = 0; c < 8; ++c) acc -= s[(kb + c) * L + rr] * s[(kb + c) * L + q];
-            s[q * L + rr] = acc;
+            for (int c = 0; c < 8; ++c) acc += s[(kb + c) * L + rr] * s[(kb + c) * L + q];
+            u[q * L + rr] = acc;
         }
         __syncthreads();
     }
@@ -303,19 +307,15 @@ __global__ void __launch_bounds__(NTH) chol_tc_update(int J2, int nt, float* __r
         const float* t = Ab + (size_t)tile_index(2 * J2 + r / 64, c / 2) * TILE_ELEMS;
         return ld4_col(t, r % 64, (c % 2) * KC + 4 * q);
     };
-    bool ok = true;
-    if (nchunks > 0) ok = tc_kloop(nchunks, fa, fb, sm, ctl.bars, tm);
+    float R[64];
+    const bool ok = tc_kloop(nchunks, fa, fb, sm, ctl.bars, tm, R);
     if (!ok && threadIdx.x == 0) atomicExch(err, 1);
     const int row = threadIdx.x % 128, c0 = 64 * (threadIdx.x / 128);
     if (I2 > J2) {
         if (nchunks > 0) {
-            for (int cc = c0; cc < c0 + 64; cc += 32) {
-                float v[32];
-                tmem_ld32(tm + lane_base() + COL_R + cc, v);
-                float* t = Ab + (size_t)tile_index(2 * I2 + row / 64, 2 * J2 + cc / 64) * TILE_ELEMS;
+            float* t = Ab + (size_t)tile_index(2 * I2 + row / 64, 2 * J2 + c0 / 64) * TILE_ELEMS;
 #pragma unroll
-                for (int i = 0; i < 32; ++i) t[(row % 64) + TS * ((cc % 64) + i)] -= v[i];
-            }
+            for (int j = 0; j < 64; ++j) t[(row % 64) + TS * j] -= R[j];
         }
         tc_end(tm);
         return;
@@ -325,20 +325,12 @@ __global__ void __launch_bounds__(NTH) chol_tc_update(int J2, int nt, float* __r
     float* inv = s + 128 * 129;
     float* tmp = inv + 128 * 129;
     __syncthreads();
-    for (int cc = c0; cc < c0 + 64; cc += 32) {
-        float v[32];
-        if (nchunks > 0) tmem_ld32(tm + lane_base() + COL_R + cc, v);
-        else {
+    {
+        const int ti = 2 * J2 + row / 64, tj = 2 * J2 + c0 / 64;
+        if (tj <= ti) {
+            const float* t = Ab + (size_t)tile_index(ti, tj) * TILE_ELEMS;
 #pragma unroll
-            for (int i = 0; i < 32; ++i) v[i] = 0.f;
-        }
-        const int ti = 2 * J2 + row / 64, tj = 2 * J2 + cc / 64;
-        if (tj > ti) continue;
-        const float* t = Ab + (size_t)tile_index(ti, tj) * TILE_ELEMS;
-#pragma unroll
-        for (int i = 0; i < 32; ++i) {
-            const int col = cc + i;
-            s[col * 129 + row] = t[(row % 64) + TS * (col % 64)] - v[i];
+            for (int j = 0; j < 64; ++j) s[(c0 + j) * 129 + row] = t[(row % 64) + TS * j] - R[j];
         }
     }
     __syncthreads();
@@ -375,10 +367,11 @@ __global__ void __launch_bounds__(NTH) chol_tc_panel(int J2, int nt, float* __re
         return ld4_col(t, r % 64, m % 64);
     };
     auto fb = [&](int c, int r, int q) -> float4 { return ld4(li + r * 128 + c * KC + 4 * q); };
-    const bool ok = tc_kloop(128 / KC, fa, fb, sm, ctl.bars, tm);
+    float R[64];
+    const bool ok = tc_kloop(128 / KC, fa, fb, sm, ctl.bars, tm, R);
     if (!ok && threadIdx.x == 0) atomicExch(err, 1);
     __syncthreads();  // every S read is done before the tiles are overwritten
-    store_block(tm, Ab, I2, J2, 1.f);
+    store_block(R, Ab, I2, J2, 1.f);
     tc_end(tm);
 }
 
@@ -419,9 +412,10 @@ __global__ void __launch_bounds__(NTH) trtri_tc_row(int I2, int nt, const float*
         const float* t = Mb + (size_t)tile_index(k, col) * TILE_ELEMS;
         return ld4(t + (r % 64) * TS + (c % 2) * KC + 4 * q);
     };
-    bool ok = tc_kloop(nchunks, fa, fb, sm, ctl.bars, tm);
+    float R[64];
+    bool ok = tc_kloop(nchunks, fa, fb, sm, ctl.bars, tm, R);
     // S into the M tiles of block (I2, J2) (not read by any other block of this launch)
-    store_block(tm, Mb, I2, J2, 1.f);
+    store_block(R, Mb, I2, J2, 1.f);
     __syncthreads();
     tc_rearm(ctl);
     // M_IJ = -Linv_I S: A(r, m) = Linv(r, m) row-major; B(c, m) = S(m, c) column-major tiles
@@ -432,10 +426,10 @@ __global__ void __launch_bounds__(NTH) trtri_tc_row(int I2, int nt, const float*
         const float* t = Mb + (size_t)tile_index(2 * I2 + m / 64, 2 * J2 + r / 64) * TILE_ELEMS;
         return __ldcg(reinterpret_cast<const float4*>(t + (r % 64) * TS + (m % 64)));
     };
-    ok &= tc_kloop(128 / KC, fa2, fb2, sm, ctl.bars, tm);
+    ok &= tc_kloop(128 / KC, fa2, fb2, sm, ctl.bars, tm, R);
     if (!ok && threadIdx.x == 0) atomicExch(err, 1);
     __syncthreads();
-    store_block(tm, Mb, I2, J2, -1.f);
+    store_block(R, Mb, I2, J2, -1.f);
     tc_end(tm);
 }
 
@@ -468,9 +462,10 @@ __global__ void __launch_bounds__(NTH) lauum_tc(int nt, const float* __restrict_
         const float* t = Mb + (size_t)tile_index(k, col) * TILE_ELEMS;
         return ld4(t + (r % 64) * TS + (c % 2) * KC + 4 * q);
     };
-    const bool ok = tc_kloop(nchunks, fa, fb, sm, ctl.bars, tm);
+    float R[64];
+    const bool ok = tc_kloop(nchunks, fa, fb, sm, ctl.bars, tm, R);
     if (!ok && threadIdx.x == 0) atomicExch(err, 1);
-    store_block(tm, V + (size_t)b * strideA, I2, J2, 1.f);
+    store_block(R, V + (size_t)b * strideA, I2, J2, 1.f);
     tc_end(tm);
 }
 
