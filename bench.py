@@ -42,6 +42,9 @@ def parse():
     ap.add_argument("--batch", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--fp64-compare-batch", type=int, default=16)
+    ap.add_argument("--workload", default=WORKLOAD, help="named workload in cosmopp_gb300.workload.WORKLOADS")
+    ap.add_argument("--hmc-iters", type=int, default=12, help="batched-HMC iterations reported beside the line "
+                                                              "(64 chains x 20 leapfrog steps of 0.05); 0 = skip")
     return ap.parse_args()
 
 
@@ -156,7 +159,7 @@ def run_reference(args):
     import cosmopp_gb300 as cg
     from cosmopp_gb300 import workload as W
     from oracle import oracle as O
-    wl = W.make(WORKLOAD, batch=args.batch)
+    wl = W.make(args.workload, batch=args.batch)
     # data map from the oracle's own FP64 covariance (no GPU on this arm)
     O.build()
     nest = cg.ring2nest(wl.nside, wl.ring_kept)
@@ -175,7 +178,7 @@ def run_reference(args):
     out = {"metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": args.gpus, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1000.0 * el / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-           "config": {"workload": WORKLOAD, "nside": wl.nside, "lmax": wl.lmax, "n_pixels": wl.n,
+           "config": {"workload": args.workload, "nside": wl.nside, "lmax": wl.lmax, "n_pixels": wl.n,
                       "sample": "one C_l vector per step"},
            "cpu_baseline": {"value": v, "unit": "evals/s", "cores": cores, "kind": "port",
                             "sample": "%d steps x 1 evaluation (clToCMatrix with per-l Legendre restarts, "
@@ -193,7 +196,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     import cosmopp_gb300 as cg
     from cosmopp_gb300 import workload as W
-    wl = W.make(WORKLOAD, batch=args.batch, batch_seed=7 + rank)
+    wl = W.make(args.workload, batch=args.batch, batch_seed=7 + rank)
     B = len(wl.cl_batch)
     d = make_inputs(wl, cg)
     path = args.path
@@ -305,12 +308,16 @@ def run_ours(args):
                 "achieved": build_bytes / (stages["build"] * 1e-3) / 1e9, "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "traffic": None, "algorithmic_bytes": build_bytes}
         roof["frac"] = roof["achieved"] / roof["peak"]
-        fp32_peak = 70.06  # TFLOP/s, FFMA probe on this machine's GB300 (no FP32 figure in the peaks file)
+        # tcgen05 kind::tf32 runs at half the bf16 rate; the kernel sits inside a long step,
+        # so the sustained bf16 figure is the denominator.  3xTF32 issues three MMAs per
+        # product (hi*hi, hi*lo, lo*hi): tensor-pipe work = 3 x the N^3/3 useful flops.
+        tf32_peak = peaks["bf16_tflops_sustained"] / 2.0
         chol_flops = B * (N ** 3) / 3.0
-        roof_chol = {"kernel": "tiled FP32 Cholesky (chol_diag/panel/update)", "bound": "fp32_cuda_core",
-                     "achieved": chol_flops / (stages["cholesky"] * 1e-3) / 1e12, "peak": fp32_peak,
-                     "unit": "TFLOP/s"}
-        roof_chol["frac"] = roof_chol["achieved"] / fp32_peak
+        useful = chol_flops / (stages["cholesky"] * 1e-3) / 1e12
+        roof_chol = {"kernel": "left-looking 3xTF32 Cholesky (chol_tc_update/chol_tc_panel, tcgen05 kind::tf32)",
+                     "bound": "tensor", "achieved": 3.0 * useful, "useful_tflops": useful,
+                     "peak": tf32_peak, "peak_source": peak_kind + " bf16 sustained / 2", "unit": "TFLOP/s"}
+        roof_chol["frac"] = roof_chol["achieved"] / tf32_peak
         del fac_flops, top
     else:
         roof = {"kernel": "FP64 tiled Cholesky", "bound": "fp64", "achieved": B * (N ** 3) / 3.0 /
@@ -321,7 +328,7 @@ def run_ours(args):
     out = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
            "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32+f64" if path == "mixed" else "f64", "data": "synthetic",
-           "config": {"workload": WORKLOAD, "path": path, "nside": wl.nside, "lmax": wl.lmax, "n_pixels": wl.n,
+           "config": {"workload": args.workload, "path": path, "nside": wl.nside, "lmax": wl.lmax, "n_pixels": wl.n,
                       "batch_per_gpu": B, "fwhm_arcmin": wl.meta["fwhm_arcmin"], "noise_sigma": wl.sigma,
                       "mask_keep": wl.meta["keep"], "reference_point": "fiducial C_l, factorised at set-up",
                       "l2": "per-step working set %.1f GB > 129 MB L2" % (B * 3 * (N * N / 2) * 4 / 1e9),
@@ -361,6 +368,24 @@ def run_ours(args):
                                  "mixed_over_fp64": value / world / (Bf / (ms64 / 1000.0)),
                                  "max_abs_delta_m2lnl": err, "max_rel_delta_grad": gerr}
         c64.close()
+    if rank == 0 and path == "mixed" and args.hmc_iters > 0:
+        # gradient + HMC: 64 chains on ln C_l (l = 2..lmax), 20 leapfrog steps of 0.05, unit masses,
+        # starts at the fiducial +-10% (seeded); every leapfrog step is one batched evaluation
+        from cosmopp_gb300 import diagnostics
+        nch = min(64, B)
+        rng = np.random.default_rng(11)
+        x0 = np.log(wl.cl_fid[2:])[None, :] + np.log1p(rng.uniform(-0.1, 0.1, (nch, wl.lmax - 1)))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        chain, acc = ctx.hmc(d, x0, wl.cl_fid, niter=args.hmc_iters, nleap=20, tau=0.05, seed=3)
+        hmc_s = time.perf_counter() - t0
+        ess = diagnostics.ess(chain[1:, :, 1:])
+        nev = nch * (1 + 20 * args.hmc_iters)
+        out["hmc"] = {"chains": nch, "leapfrog_steps": 20, "step_size": 0.05, "iterations": args.hmc_iters,
+                      "evals_per_s": nev / hmc_s, "accept_rate": float(acc.mean()),
+                      "ess_min": float(ess.min()), "ess_median": float(np.median(ess)),
+                      "ess_per_s_min": float(ess.min() / hmc_s), "wall_s": hmc_s,
+                      "reference_point": "fiducial, re-centred automatically beyond |ln C/C_ref| = 1"}
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(wl, d)
     ctx.close()

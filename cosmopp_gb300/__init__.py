@@ -84,6 +84,8 @@ def library():
                                     ctypes.c_void_p, ctypes.c_void_p]
     L.cg_set_reference.argtypes = [ctypes.c_void_p, _dp]
     L.cg_reference_count.argtypes = [ctypes.c_void_p]
+    L.cg_hmc_run.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, _dp, _dp, ctypes.c_int, ctypes.c_int,
+                             ctypes.c_double, _dp, ctypes.c_int, ctypes.c_ulonglong, _dp, _dp]
     L.cg_launch_count.restype = ctypes.c_longlong
     L.cg_launch_count.argtypes = [ctypes.c_void_p]
     L.cg_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int]
@@ -280,6 +282,19 @@ class Context:
 
     def reference_count(self):
         return self._L.cg_reference_count(self._h)
+
+    def hmc(self, d, x0, cl_template, niter, nleap, tau, mass=None, jitter=False, seed=0):
+        """Batched HMC over ln C_l (l = 2..lmax), one chain per row of x0 (cg_hmc_run).
+        Returns (chain [niter+1, nchains, lmax]: -2lnL then x, accept_rate [nchains])."""
+        x0 = _f64(x0)
+        nchains, npar = x0.shape
+        chain = np.zeros((niter + 1, nchains, npar + 1))
+        acc = np.zeros(nchains)
+        m = None if mass is None else _f64(mass)
+        self._check(self._L.cg_hmc_run(self._h, _p(_f64(d)), nchains, _p(x0), _p(_f64(cl_template)), int(niter),
+                                       int(nleap), float(tau), _p(m), int(bool(jitter)), int(seed), _p(chain),
+                                       _p(acc)))
+        return chain, acc
 
     def launch_count(self):
         """Kernels this context has launched so far."""

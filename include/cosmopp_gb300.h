@@ -105,6 +105,20 @@ int cg_set_reference(cg_ctx* ctx, const double* cl_ref);
 /* number of reference (re)factorisations so far (mixed path) */
 int cg_reference_count(const cg_ctx* ctx);
 
+/* ---- batched HMC (Math::HMC::run, source/hmc.cpp:31-126, over many chains) ---- */
+/* nchains chains on one map, parameters x = ln C_l for l = 2..lmax (lmax - 1 per chain),
+   cl_template gives C_0, C_1 (ignored) and the layout; x0 [nchains][lmax-1].  Each
+   iteration draws p ~ N(0, mass), runs nleap leapfrog steps of size tau with the
+   derivative of -2lnL (halved, as the reference does), and accepts with
+   exp(-dH/2), dH of -2lnL + p^2/m.  jitter != 0 draws tau in (0, tau] and
+   ceil(nleap U) steps each iteration like the reference.  Every leapfrog step is
+   one batched cg_loglike call over all chains.  chain receives
+   [niter+1][nchains][lmax]: -2lnL then x for every chain after every iteration
+   (row 0 = the start); accept_rate [nchains] (nullable). */
+int cg_hmc_run(cg_ctx* ctx, const double* map, int nchains, const double* x0, const double* cl_template,
+               int niter, int nleap, double tau, const double* mass, int jitter, unsigned long long seed,
+               double* chain, double* accept_rate);
+
 /* ---- instrumentation ------------------------------------------------------ */
 /* kernels this context has launched so far */
 long long cg_launch_count(const cg_ctx* ctx);
