@@ -4,24 +4,31 @@
 // and a_lo = a - a_hi rounded to nearest TF32 (unbiased; truncating instead
 // biases sums of squares).  The tensor core's FP32 accumulation is not
 // round-to-nearest and drifts by ~0.4 ulp per instruction, always the same
-// way, so each chunk accumulates the hi*hi products (4 MMAs) and the
-// correction products (8 MMAs) in separate tensor-memory accumulators that are
-// folded into a per-thread FP32 register sum (round-to-nearest) one chunk later.
+// way, so each chunk's hi*hi products (4 MMAs) go to a fresh tensor-memory
+// accumulator that is folded into a per-thread FP32 register sum
+// (round-to-nearest) one chunk later.  The correction products (8 MMAs per
+// chunk) are ~2^-11 of the sum, so their drift is negligible and they
+// accumulate in one tensor-memory accumulator over the whole K loop.
 //
-// One CTA (128 threads) owns a 128x128 output supertile (2x2 of the 64x64
-// storage tiles) and runs a K loop over 32-wide chunks: every thread loads
-// one row of the A and B chunks into registers, the chunk is split hi/lo into
-// a double-buffered shared-memory stage in the K-major canonical layout, and
-// one thread issues 12 MMAs (M128 N128 K8) per chunk and commits them to the
-// stage's mbarrier; the next chunk's global loads overlap those MMAs.
+// One CTA (256 threads) owns a 128x128 output supertile (2x2 of the 64x64
+// storage tiles) and runs a K loop over 32-wide chunks.  Thread t loads row
+// t % 128, K half t / 128 of the A and B chunks into registers two chunks
+// ahead; A is split hi/lo straight into tensor memory (tcgen05.st, lane = row),
+// B into a double-buffered shared-memory stage in the K-major canonical layout.
+// One thread issues the 12 MMAs (M128 N128 K8, A from tensor memory) of a chunk
+// and commits them to the stage's mbarrier.  Keeping A out of shared memory
+// removes its stores and the MMAs' re-reads of it there (shared-memory bandwidth
+// bounds this loop).
 //
 //   chol_tc_update: left-looking Cholesky, column block J: S_IJ = A_IJ - sum_{k<J} L_Ik L_Jk^T;
 //                   the diagonal CTA factors S_JJ = L_JJ L_JJ^T and inverts L_JJ in shared memory
 //   chol_tc_panel:  L_IJ = S_IJ L_JJ^-T                        (I > J)
 //   trtri_tc_row:   M_IJ = -L_II^-1 sum_{k=J}^{I-1} L_Ik M_kJ, M_II = L_II^-1   (M = L^-1)
 //   lauum_tc:       V_IJ = sum_{k >= row} M_kI^T M_kJ = (L L^T)^-1
-// (I, J in 128-row blocks; every matrix in 64x64 column-major storage tiles; the
-// 128x128 inverses of the diagonal blocks of L are kept row-major in Linv.)
+// (I, J in 128-row blocks; A, L and V in 64x64 column-major storage tiles, M in
+// transposed (row-major) tiles and the 128x128 inverses of L's diagonal blocks
+// column-major in Linv.  With these layouts every operand the K loops read has
+// element (r, k) at r + ld k: consecutive threads (rows) read consecutive words.)
 #include "cg_internal.h"
 #include "cg_tc.cuh"
 
@@ -37,7 +44,7 @@ constexpr uint32_t LBO = 128, SBO = KC / 4 * 128;
 constexpr uint32_t IDESC = idesc_tf32(128, 128);
 
 struct TcSmem {
-    float buf[2][4][STAGE_FLOATS];         // [stage][a_hi, a_lo, b_hi, b_lo]
+    float buf[2][2][STAGE_FLOATS];         // [stage][b_hi, b_lo]
 };
 
 // stores one float4 (row r, K columns 4q..4q+3 of the chunk) as hi and lo parts
@@ -50,25 +57,27 @@ __device__ __forceinline__ void put4(float* hi, float* lo, int r, int q, float4 
         make_float4(tf32_rn(v.x - h.x), tf32_rn(v.y - h.y), tf32_rn(v.z - h.z), tf32_rn(v.w - h.w));
 }
 
-// Tensor-memory columns: two accumulator sets (chunk parity), each a hi*hi accumulator and a
-// correction accumulator of 128 columns.
+// Tensor-memory columns (512): hi*hi accumulators for the two chunk parities, the correction
+// accumulator, and the A operand (hi, lo) of the two stages.
 constexpr uint32_t TMEM_COLS = 512;
-__device__ __forceinline__ uint32_t col_main(int set) { return 256u * set; }
-__device__ __forceinline__ uint32_t col_corr(int set) { return 256u * set + 128u; }
+constexpr uint32_t COL_CORR = 256;
+__device__ __forceinline__ uint32_t col_main(int set) { return 128u * set; }
+__device__ __forceinline__ uint32_t col_a_hi(int st) { return 384u + 64u * st; }
+__device__ __forceinline__ uint32_t col_a_lo(int st) { return 384u + 64u * st + 32u; }
 
-// R[j] += (main + corr) for this thread's row (lane) and its 64 columns (64 h + j): warps 0-3
-// fold columns 0-63, warps 4-7 columns 64-127 (warp w reaches TMEM lanes 32 (w % 4) .. + 31).
-__device__ __forceinline__ void drain(uint32_t tm, int set, float (&R)[64])
+// the accumulator row this thread holds in TMEM (warp w: lanes 32 (w % 4) .. + 31)
+__device__ __forceinline__ uint32_t lane_base() { return (uint32_t)(32 * ((threadIdx.x / 32) % 4)) << 16; }
+
+// R[j] += accumulator at column col of this thread's row, columns 64 (t / 128) + j
+__device__ __forceinline__ void drain(uint32_t tm, uint32_t col, float (&R)[64])
 {
-    const uint32_t lane_off = (uint32_t)(32 * ((threadIdx.x / 32) % 4)) << 16;
     const uint32_t c0 = 64 * (threadIdx.x / 128);
 #pragma unroll
     for (int part = 0; part < 4; ++part) {
-        float m[16], c[16];
-        tmem_ld16(tm + lane_off + col_main(set) + c0 + 16 * part, m);
-        tmem_ld16(tm + lane_off + col_corr(set) + c0 + 16 * part, c);
+        float m[16];
+        tmem_ld16(tm + lane_base() + col + c0 + 16 * part, m);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) R[16 * part + i] += m[i] + c[i];
+        for (int i = 0; i < 16; ++i) R[16 * part + i] += m[i];
     }
 }
 
@@ -97,34 +106,45 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, TcSmem& sm, uint64_t* bars, 
     auto step = [&](int c, float4 (&qa)[4], float4 (&qb)[4]) {
         const int st = c & 1;
         if (c >= 2) {
-            // MMAs of chunk c-2 done: its stage is free and its accumulators are folded into R
+            // MMAs of chunk c-2 done: its A columns and B stage are free, its hi*hi sum goes to R
             ok &= mbar_wait(&bars[st], ((c - 2) >> 1) & 1);
             fence_after();
-            drain(tm, st, R);
-            fence_before();
+            drain(tm, col_main(st), R);
+        }
+        {
+            float ahi[16], alo[16];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float v[4] = {qa[q].x, qa[q].y, qa[q].z, qa[q].w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    ahi[4 * q + i] = tf32_rn(v[i]);
+                    alo[4 * q + i] = tf32_rn(v[i] - ahi[4 * q + i]);
+                }
+            }
+            tmem_st16(tm + lane_base() + col_a_hi(st) + 16 * h, ahi);
+            tmem_st16(tm + lane_base() + col_a_lo(st) + 16 * h, alo);
         }
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            put4(sm.buf[st][0], sm.buf[st][1], r, 4 * h + q, qa[q]);
-            put4(sm.buf[st][2], sm.buf[st][3], r, 4 * h + q, qb[q]);
-        }
+        for (int q = 0; q < 4; ++q) put4(sm.buf[st][0], sm.buf[st][1], r, 4 * h + q, qb[q]);
         if (c + 2 < nchunks) {
 #pragma unroll
             for (int q = 0; q < 4; ++q) { qa[q] = fa(c + 2, r, 4 * h + q); qb[q] = fb(c + 2, r, 4 * h + q); }
         }
+        tmem_wait_st();
         fence_proxy_async();
+        fence_before();
         __syncthreads();
         if (threadIdx.x == 0) {
             fence_after();
-            const uint32_t ah = smem_u32(sm.buf[st][0]), al = smem_u32(sm.buf[st][1]);
-            const uint32_t bh = smem_u32(sm.buf[st][2]), bl = smem_u32(sm.buf[st][3]);
+            const uint32_t bh = smem_u32(sm.buf[st][0]), bl = smem_u32(sm.buf[st][1]);
+            const uint32_t ah = tm + col_a_hi(st), al = tm + col_a_lo(st);
 #pragma unroll
             for (int kk = 0; kk < KC / 8; ++kk) {
                 const uint32_t off = kk * 2 * LBO;
-                const uint32_t acc = kk ? 1u : 0u;
-                mma_tf32(tm + col_corr(st), smem_desc(al + off, LBO, SBO), smem_desc(bh + off, LBO, SBO), IDESC, acc);
-                mma_tf32(tm + col_corr(st), smem_desc(ah + off, LBO, SBO), smem_desc(bl + off, LBO, SBO), IDESC, 1u);
-                mma_tf32(tm + col_main(st), smem_desc(ah + off, LBO, SBO), smem_desc(bh + off, LBO, SBO), IDESC, acc);
+                mma_tf32_ta(tm + COL_CORR, al + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, (c | kk) ? 1u : 0u);
+                mma_tf32_ta(tm + COL_CORR, ah + 8 * kk, smem_desc(bl + off, LBO, SBO), IDESC, 1u);
+                mma_tf32_ta(tm + col_main(st), ah + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, kk ? 1u : 0u);
             }
             mma_commit(&bars[st]);
         }
@@ -133,30 +153,42 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, TcSmem& sm, uint64_t* bars, 
         step(c, pa0, pb0);
         if (c + 1 < nchunks) step(c + 1, pa1, pb1);
     }
-    // the last one or two chunks: wait for the last commit (it tracks every earlier MMA) and fold
+    // the last one or two chunks and the corrections: wait for the last commit (it tracks every
+    // earlier MMA) and fold
     if (nchunks > 0) {
         ok &= mbar_wait(&bars[(nchunks - 1) & 1], ((nchunks - 1) >> 1) & 1);
         fence_after();
-        if (nchunks >= 2) drain(tm, (nchunks - 2) & 1, R);
-        drain(tm, (nchunks - 1) & 1, R);
+        if (nchunks >= 2) drain(tm, col_main((nchunks - 2) & 1), R);
+        drain(tm, col_main((nchunks - 1) & 1), R);
+        drain(tm, COL_CORR, R);
         fence_before();
     }
     return ok;
 }
 
-__device__ __forceinline__ float4 ld4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
-
-// element (r, m..m+3) of a column-major 64x64 tile: four loads, each coalesced across the warp's rows
+// element (r, m..m+3) of a column-major 64x64 tile (or of the transpose of a row-major one): four
+// loads, each coalesced across the warp's rows
 __device__ __forceinline__ float4 ld4_col(const float* t, int r, int m)
 {
     return make_float4(t[r + TS * m], t[r + TS * (m + 1)], t[r + TS * (m + 2)], t[r + TS * (m + 3)]);
 }
 
+// the same for data written earlier in the same kernel: coherent L2 loads, not the read-only path
+__device__ __forceinline__ float4 ld4_col_cg(const float* t, int r, int m)
+{
+    return make_float4(__ldcg(t + r + TS * m), __ldcg(t + r + TS * (m + 1)), __ldcg(t + r + TS * (m + 2)),
+                       __ldcg(t + r + TS * (m + 3)));
+}
+
+// element (r, m..m+3) of a column-major 128x128 block (Linv)
+__device__ __forceinline__ float4 ld4_linv(const float* li, int r, int m)
+{
+    return make_float4(li[r + 128 * m], li[r + 128 * (m + 1)], li[r + 128 * (m + 2)], li[r + 128 * (m + 3)]);
+}
+
 constexpr float4 kZero4 = {0.f, 0.f, 0.f, 0.f};
 constexpr int LINV = 128 * 128;  // floats per 128x128 diagonal-block inverse
 
-// the accumulator row this thread holds in TMEM (warp w: lanes 32w..32w+31)
-__device__ __forceinline__ uint32_t lane_base() { return (uint32_t)(32 * ((threadIdx.x / 32) % 4)) << 16; }
 
 // write the 128x128 result (this thread: row t % 128, columns 64 (t / 128) + j in R) times sgn
 // into the column-major tiles of supertile (I2, J2), skipping the tile above the diagonal
@@ -168,6 +200,18 @@ __device__ __forceinline__ void store_block(const float (&R)[64], float* base, i
     float* t = base + (size_t)tile_index(ti, tj) * TILE_ELEMS;
 #pragma unroll
     for (int j = 0; j < 64; ++j) t[(row % 64) + TS * j] = sgn * R[j];
+}
+
+// the same into row-major (transposed) tiles: this thread's row is 64 contiguous floats
+__device__ __forceinline__ void store_block_t(const float (&R)[64], float* base, int I2, int J2, float sgn)
+{
+    const int row = threadIdx.x % 128, h = threadIdx.x / 128;
+    const int ti = 2 * I2 + row / 64, tj = 2 * J2 + h;
+    if (tj > ti) return;
+    float4* t = reinterpret_cast<float4*>(base + (size_t)tile_index(ti, tj) * TILE_ELEMS + (row % 64) * TS);
+#pragma unroll
+    for (int j = 0; j < 16; ++j)
+        t[j] = make_float4(sgn * R[4 * j], sgn * R[4 * j + 1], sgn * R[4 * j + 2], sgn * R[4 * j + 3]);
 }
 
 struct TcCtl {
@@ -335,7 +379,7 @@ __global__ void __launch_bounds__(NTH) chol_tc_update(int J2, int nt, float* __r
     }
     __syncthreads();
     factor_block128(s, inv, tmp, &ctl.bad);
-    // L_JJ into the three lower tiles (strict upper of the diagonal tiles zeroed), diag, Linv row-major
+    // L_JJ into the three lower tiles (strict upper of the diagonal tiles zeroed), diag, Linv column-major
     for (int col = c0; col < c0 + 64; ++col) {
         const int ti = 2 * J2 + row / 64, tj = 2 * J2 + col / 64;
         if (tj > ti) continue;
@@ -344,7 +388,7 @@ __global__ void __launch_bounds__(NTH) chol_tc_update(int J2, int nt, float* __r
     }
     if (threadIdx.x < 128) diag[(size_t)b * nt * TS + J2 * 128 + row] = s[row * 129 + row];
     float* li = Linv + ((size_t)b * nt2 + J2) * LINV;
-    for (int col = c0; col < c0 + 64; ++col) li[row * 128 + col] = inv[col * 129 + row];
+    for (int col = c0; col < c0 + 64; ++col) li[col * 128 + row] = inv[col * 129 + row];
     if (threadIdx.x == 0 && ctl.bad && status && status[b] == CG_OK) status[b] = CG_ERR_NOT_PD;
     tc_end(tm);
 }
@@ -360,13 +404,13 @@ __global__ void __launch_bounds__(NTH) chol_tc_panel(int J2, int nt, float* __re
     float* Ab = A + (size_t)b * strideA;
     const float* li = Linv + ((size_t)b * nt2 + J2) * LINV;
     const uint32_t tm = tc_begin(ctl);
-    // A(r, m) = S(r, m): block column m/64 of row block I2; B(c, m) = Linv(c, m) row-major
+    // A(r, m) = S(r, m): block column m/64 of row block I2; B(c, m) = Linv(c, m) column-major
     auto fa = [&](int c, int r, int q) -> float4 {
         const int m = c * KC + 4 * q;
         const float* t = Ab + (size_t)tile_index(2 * I2 + r / 64, 2 * J2 + m / 64) * TILE_ELEMS;
         return ld4_col(t, r % 64, m % 64);
     };
-    auto fb = [&](int c, int r, int q) -> float4 { return ld4(li + r * 128 + c * KC + 4 * q); };
+    auto fb = [&](int c, int r, int q) -> float4 { return ld4_linv(li, r, c * KC + 4 * q); };
     float R[64];
     const bool ok = tc_kloop(128 / KC, fa, fb, sm, ctl.bars, tm, R);
     if (!ok && threadIdx.x == 0) atomicExch(err, 1);
@@ -388,17 +432,17 @@ __global__ void __launch_bounds__(NTH) trtri_tc_row(int I2, int nt, const float*
     float* Mb = M + (size_t)b * strideA;
     const float* li = Linv + ((size_t)b * nt2 + I2) * LINV;
     const int row = threadIdx.x % 128, c0 = 64 * (threadIdx.x / 128);
-    if (J2 == I2) {  // M_II = Linv_I, into the three lower column-major tiles
+    if (J2 == I2) {  // M_II = Linv_I, into the three lower row-major tiles
         for (int col = c0; col < c0 + 64; ++col) {
             const int ti = 2 * I2 + row / 64, tj = 2 * I2 + col / 64;
             if (tj > ti) continue;
-            Mb[(size_t)tile_index(ti, tj) * TILE_ELEMS + (row % 64) + TS * (col % 64)] = li[row * 128 + col];
+            Mb[(size_t)tile_index(ti, tj) * TILE_ELEMS + (row % 64) * TS + (col % 64)] = li[col * 128 + row];
         }
         return;
     }
     const uint32_t tm = tc_begin(ctl);
     // S = sum_{k=2 J2}^{2 I2 - 1} L_{I,k} M_{k,J}: A(r, m) = L tile (2 I2 + r/64, k)(r%64, m) column-major,
-    // B(c, m) = M tile (k, 2 J2 + c/64)(m, c%64) column-major -> contiguous in m for fixed c
+    // B(c, m) = M tile (k, 2 J2 + c/64)(m, c%64) row-major, at c%64 + 64 m
     const int k0 = 2 * J2;
     const int nchunks = (2 * I2 - k0) * (TS / KC);
     auto fa = [&](int c, int r, int q) -> float4 {
@@ -410,32 +454,32 @@ __global__ void __launch_bounds__(NTH) trtri_tc_row(int I2, int nt, const float*
         const int k = k0 + c / 2, col = 2 * J2 + r / 64;
         if (k < col) return kZero4;
         const float* t = Mb + (size_t)tile_index(k, col) * TILE_ELEMS;
-        return ld4(t + (r % 64) * TS + (c % 2) * KC + 4 * q);
+        return ld4_col(t, r % 64, (c % 2) * KC + 4 * q);
     };
     float R[64];
     bool ok = tc_kloop(nchunks, fa, fb, sm, ctl.bars, tm, R);
     // S into the M tiles of block (I2, J2) (not read by any other block of this launch)
-    store_block(R, Mb, I2, J2, 1.f);
+    store_block_t(R, Mb, I2, J2, 1.f);
     __syncthreads();
     tc_rearm(ctl);
-    // M_IJ = -Linv_I S: A(r, m) = Linv(r, m) row-major; B(c, m) = S(m, c) column-major tiles
-    auto fa2 = [&](int c, int r, int q) -> float4 { return ld4(li + r * 128 + c * KC + 4 * q); };
+    // M_IJ = -Linv_I S: A(r, m) = Linv(r, m) column-major; B(c, m) = S(m, c), row-major tiles
+    auto fa2 = [&](int c, int r, int q) -> float4 { return ld4_linv(li, r, c * KC + 4 * q); };
     auto fb2 = [&](int c, int r, int q) -> float4 {
-        // S was written by this kernel: coherent L2 loads, not the read-only path
         const int m = c * KC + 4 * q;
         const float* t = Mb + (size_t)tile_index(2 * I2 + m / 64, 2 * J2 + r / 64) * TILE_ELEMS;
-        return __ldcg(reinterpret_cast<const float4*>(t + (r % 64) * TS + (m % 64)));
+        return ld4_col_cg(t, r % 64, m % 64);
     };
     ok &= tc_kloop(128 / KC, fa2, fb2, sm, ctl.bars, tm, R);
     if (!ok && threadIdx.x == 0) atomicExch(err, 1);
     __syncthreads();
-    store_block(R, Mb, I2, J2, -1.f);
+    store_block_t(R, Mb, I2, J2, -1.f);
     tc_end(tm);
 }
 
 
-// V_IJ (128x128 supertile, lower) = sum over k of M_k,I^T M_k,J with M column-major tiles.
-// grid (supertiles of the lower triangle, B), 128 threads.
+// V_IJ (128x128 supertile, lower) = sum over k of M_k,I^T M_k,J with M in row-major tiles; V in
+// column-major tiles.
+// grid (supertiles of the lower triangle, B), 256 threads.
 __global__ void __launch_bounds__(NTH) lauum_tc(int nt, const float* __restrict__ M, float* __restrict__ V,
                                                 size_t strideA, int* __restrict__ err)
 {
@@ -449,18 +493,18 @@ __global__ void __launch_bounds__(NTH) lauum_tc(int nt, const float* __restrict_
     const uint32_t tm = tc_begin(ctl);
     const int k0 = 2 * I2;                     // first tile row with a non-zero M_k,row
     const int nchunks = (nt - k0) * (TS / KC);
-    // A(r, m) = M_{k, 2I2 + r/64}(m, r%64): tile (k, col) column-major, element (m, r') at m + 64 r'
+    // A(r, m) = M_{k, 2I2 + r/64}(m, r%64): tile (k, col) row-major, element (m, r') at r' + 64 m
     auto fa = [&](int c, int r, int q) -> float4 {
         const int k = k0 + c / 2, col = 2 * I2 + r / 64;
         if (k < col) return make_float4(0.f, 0.f, 0.f, 0.f);
         const float* t = Mb + (size_t)tile_index(k, col) * TILE_ELEMS;
-        return ld4(t + (r % 64) * TS + (c % 2) * KC + 4 * q);
+        return ld4_col(t, r % 64, (c % 2) * KC + 4 * q);
     };
     auto fb = [&](int c, int r, int q) -> float4 {
         const int k = k0 + c / 2, col = 2 * J2 + r / 64;
         if (k < col) return make_float4(0.f, 0.f, 0.f, 0.f);
         const float* t = Mb + (size_t)tile_index(k, col) * TILE_ELEMS;
-        return ld4(t + (r % 64) * TS + (c % 2) * KC + 4 * q);
+        return ld4_col(t, r % 64, (c % 2) * KC + 4 * q);
     };
     float R[64];
     const bool ok = tc_kloop(nchunks, fa, fb, sm, ctl.bars, tm, R);
