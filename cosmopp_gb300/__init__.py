@@ -78,6 +78,7 @@ def library():
     L.cg_unit_vectors.argtypes = [ctypes.c_void_p, _dp]
     L.cg_build_cmatrix.argtypes = [ctypes.c_void_p, _dp, _dp]
     L.cg_build_cmatrix_batched.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp]
+    L.cg_fiducial_matrix.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, ctypes.c_int, _dp, _dp]
     L.cg_loglike.argtypes = [ctypes.c_void_p, ctypes.c_int, _dp, _dp, ctypes.c_int, _dp, _dp, _dp, _dp, _ip]
     L.cg_loglike_device.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -248,6 +249,20 @@ class Context:
         out = np.zeros((B, self.n * (self.n + 1) // 2))
         self._check(self._L.cg_build_cmatrix_batched(self._h, B, _p(cl2), _p(out)))
         return out[0] if single else out
+
+    def fiducial_matrix(self, cl, lmax_max, lmax=None, beam=None):
+        """CMatrixGenerator::getFiducialMatrix for this context's pixels: packed sum over
+        l = lmax+1 .. lmax_max (the reference uses lmax_max = 4 nside) plus the monopole/dipole
+        term.  lmax defaults to the context's; cl [>= lmax_max + 1]; beam [lmax_max + 1] or None
+        for the context's Gaussian beam (cg_fiducial_matrix)."""
+        cl = _f64(cl)
+        if cl.shape[0] < lmax_max + 1:
+            raise ValueError("cl must have lmax_max + 1 entries")
+        out = np.zeros(self.n * (self.n + 1) // 2)
+        b = None if beam is None else _f64(beam)
+        self._check(self._L.cg_fiducial_matrix(self._h, _p(cl), int(self.lmax if lmax is None else lmax),
+                                               int(lmax_max), _p(b), _p(out)))
+        return out
 
     def loglike(self, cl, d, grad=False):
         """-2lnL for a batch of C_l vectors on one map d [n] or B maps [B, n].

@@ -152,6 +152,7 @@ extern "C" int cg_create(cg_ctx** out, const cg_config* cfg)
         }
     }
     if (cfg->fwhm_deg < 0 && !cfg->beam) { g_create_error = "invalid fwhm"; return CG_ERR_BAD_ARG; }
+    ctx->fwhm_deg = cfg->beam ? -1.0 : cfg->fwhm_deg;
     // noise: generateNoiseMatrix puts noise * noise on the diagonal (source/c_matrix_generator.cpp:774-787)
     ctx->noise.resize(ctx->n);
     for (int i = 0; i < ctx->n; ++i) {
@@ -223,6 +224,62 @@ extern "C" int cg_build_cmatrix_batched(cg_ctx* ctx, int B, const double* cl, do
 extern "C" int cg_build_cmatrix(cg_ctx* ctx, const double* cl, double* out_packed)
 {
     return cg_build_cmatrix_batched(ctx, 1, cl, out_packed);
+}
+
+extern "C" int cg_fiducial_matrix(cg_ctx* ctx, const double* cl, int lmax, int lmax_max, const double* beam,
+                                  double* out_packed)
+{
+    if (!ctx || !cl || !out_packed || lmax < 1 || lmax_max <= lmax || lmax_max > CG_FIDUCIAL_LMAX_MAX) {
+        if (ctx) ctx->err = "bad arguments to cg_fiducial_matrix (need 1 <= lmax < lmax_max <= 4096)";
+        return CG_ERR_BAD_ARG;
+    }
+    if (!beam && ctx->fwhm_deg < 0) {
+        ctx->err = "cg_fiducial_matrix: the context has a caller-given beam table; pass beam[0..lmax_max]";
+        return CG_ERR_BAD_ARG;
+    }
+    const int L1 = lmax_max + 1;
+    for (int l = 0; l < L1; ++l)
+        if (!std::isfinite(cl[l]) || (beam && !std::isfinite(beam[l]))) {
+            ctx->err = "non-finite C_l or beam";
+            return CG_ERR_NONFINITE;
+        }
+    // tables as source/c_matrix_generator.cpp:706-772 forms its terms: Bonnet coefficients
+    // (include/legendre.hpp:34), cl[l] * ((2l+1)/(4 pi)), the beam (unit pixel window), 100 cl[2]
+    std::vector<double> tab((size_t)4 * L1, 0.0);
+    double* a = tab.data();
+    double* b = a + L1;
+    double* fc = b + L1;
+    double* bm = fc + L1;
+    for (int l = 0; l < L1; ++l) {
+        if (l >= 1) {
+            a[l] = 2 - 1.0 / l;
+            b[l] = 1 - 1.0 / l;
+        }
+        fc[l] = cl[l] * ((2 * l + 1) / (4 * cg::kPiHost));
+        double f = 1.0;
+        f *= beam ? beam[l] : cg_beam(l, ctx->fwhm_deg);
+        bm[l] = f;
+    }
+    const double m0 = 100 * cl[2];
+    CG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const size_t np = (size_t)ctx->n * (ctx->n + 1) / 2;
+    double *d_tab = nullptr, *d_out = nullptr;
+    CG_CUDA_TRY(ctx, cudaMalloc((void**)&d_tab, sizeof(double) * tab.size()));
+    if (cudaMalloc((void**)&d_out, sizeof(double) * np) != cudaSuccess) {
+        cudaFree(d_tab);
+        ctx->err = "cg_fiducial_matrix: out of device memory";
+        return CG_ERR_CUDA;
+    }
+    cudaMemcpyAsync(d_tab, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, ctx->stream);
+    int rc = cg::fp64_build_fiducial(ctx, lmax + 1, lmax_max, d_tab, m0, d_out, ctx->stream);
+    if (rc == CG_OK) {
+        cudaMemcpyAsync(out_packed, d_out, sizeof(double) * np, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = CG_ERR_CUDA; }
+    }
+    cudaFree(d_tab);
+    cudaFree(d_out);
+    return rc;
 }
 
 // ---- likelihood ------------------------------------------------------------

@@ -18,6 +18,7 @@ namespace cg {
 // the identity, which changes neither ln det nor any solve.
 constexpr int TS = 64;
 constexpr int TILE_ELEMS = TS * TS;
+constexpr double kPiHost = 3.141592653589793;  // Math::pi, include/math_constants.hpp:8
 
 __host__ __device__ inline int tile_index(int I, int J) { return I * (I + 1) / 2 + J; }
 __host__ __device__ inline int ntiles_lower(int nt) { return nt * (nt + 1) / 2; }
@@ -79,10 +80,11 @@ struct MixedWork {
     double* Z = nullptr;         // [nharm_pad][N] L_ref^-1 Y
     float* U = nullptr;          // [tiles][TS*TS][lpad] whitened Legendre table
     // per batch element
-    float* A = nullptr;          // [cap][tiled] I + K_b, then L_b, then V_b = (I + K_b)^-1
-    float* Acopy = nullptr;      // [cap][tiled] I + K_b kept for the refinement residual
-    float* M = nullptr;          // [cap][tiled] L_b^-1
-    float* Dinv = nullptr;       // [cap][nt/2][128*128] inverses of the 128x128 diagonal blocks of L_b (row-major)
+    float* A = nullptr;          // [cap][tiled] I + K_b (kept for the refinement residual)
+    float* V = nullptr;          // [cap][tiled] V_b = (I + K_b)^-1
+    float* Ls = nullptr;         // [cap][tc_split_elems] L_b, split canonical storage
+    float* Ms = nullptr;         // [cap][tc_split_elems] (L_b^-1)^T blocks, split canonical storage
+    float* Linv = nullptr;       // [cap][tc_linv_elems] inverses of the 128x128 diagonal blocks of L_b
     float* diag = nullptr;       // [cap][N]
     float* eps = nullptr;        // [cap][lpad] C_l / Cref_l - 1
     double* y = nullptr;         // [cap][N] L_ref^-1 d
@@ -101,6 +103,7 @@ struct cg_ctx {
     int device = 0;
     int n = 0, nt = 0, N = 0;    // kept pixels, tiles per side, padded size
     int lmax = 0;
+    double fwhm_deg = -1;        // Gaussian beam FWHM (degrees); -1 when the caller gave the beam table
     int max_batch = 1;
     int precision = CG_PREC_FP64;
     int recenter = CG_RECENTER_AUTO;
@@ -156,6 +159,8 @@ int fp64_ensure(cg_ctx* ctx, int B);
 int fp64_build_tiled(cg_ctx* ctx, int B, const double* d_cl, bool add_noise, cudaStream_t s);
 int fp64_build_tiled_into(cg_ctx* ctx, int B, const double* d_cl, bool add_noise, double* A, cudaStream_t s);
 int fp64_build_packed(cg_ctx* ctx, int B, const double* d_cl, double* d_out, cudaStream_t s);
+int fp64_build_fiducial(cg_ctx* ctx, int lo, int hi, const double* d_tables, double m0, double* d_out,
+                        cudaStream_t s);
 int fp64_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* d_d, int d_stride, double* d_m2lnl,
                  double* d_chi2, double* d_logdet, double* d_grad, int* d_status, cudaStream_t s);
 // generic tiled FP64 / FP32 factorisation entry points (k_chol.cu)
@@ -166,11 +171,14 @@ int tiled_trtri(cg_ctx* ctx, int B, int nt, const T* L, const T* Dinv, T* M, siz
 template <typename T>
 int tiled_lauum(cg_ctx* ctx, int B, int nt, const T* M, T* V, size_t strideA, cudaStream_t s);
 // tensor-core FP32 (3xTF32) versions (k_tc.cu); d_err is set if a bounded wait gave up
-int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* M, float* V, size_t strideA, int* d_err, cudaStream_t s);
-int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, float* A, float* Linv, float* diag, int* status, size_t strideA,
-                      int* d_err, cudaStream_t s);
-int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* L, const float* Linv, float* M, size_t strideA, int* d_err,
+// tensor-core FP32 kernels (k_tc.cu): L, M^T and Linv in the split canonical storage
+size_t tc_split_elems(int nt);   // floats per matrix of the L / M^T storage
+size_t tc_linv_elems(int nt);    // floats per matrix of the Linv blocks
+int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, float* Linv, float* Ms, float* diag,
+                      int* status, int* d_err, cudaStream_t s);
+int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* Ls, const float* Linv, float* Ms, int* d_err,
                    cudaStream_t s);
+int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, float* V, int* d_err, cudaStream_t s);
 // mixed path (k_mixed.cu)
 int mixed_prepare_reference(cg_ctx* ctx, const double* cl_ref_host);
 int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, const double* d_d, int d_stride,

@@ -89,8 +89,10 @@ __device__ __forceinline__ void mbar_init(uint64_t* mbar, uint32_t count)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mbar)), "r"(count));
 }
 
-// bounded wait for the phase with the given parity; returns false if it gave up
-__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint32_t max_iter = 1u << 24)
+// bounded wait for the phase with the given parity; returns false if it gave up, after max_iter
+// attempts or as soon as *abort (a global error flag, nullable) is set by any CTA
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint32_t max_iter = 1u << 24,
+                                          const volatile int* abort = nullptr)
 {
     const uint32_t a = smem_u32(mbar);
     for (uint32_t it = 0; it < max_iter; ++it) {
@@ -101,6 +103,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint3
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
+        if (abort && (it & 255) == 255 && *abort) return false;
     }
     return false;
 }
@@ -137,6 +140,31 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16])
     for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 32 lanes x 32 consecutive 32-bit columns, load and wait in one statement (the registers are
+// only used after the wait)
+__device__ __forceinline__ void tmem_ld32w(uint32_t taddr, float (&v)[32])
+{
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// one plain arrival on the mbarrier
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
+
 // registers -> 32 lanes x 16 consecutive 32-bit columns; completion is awaited by tmem_wait_st
 __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16])
 {
@@ -151,7 +179,43 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float (&v)[16])
         : "memory");
 }
 
+// the same from four float4 registers (columns 4i .. 4i+3 from v[i])
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const float4 (&v)[4])
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+        "%15, %16};" ::"r"(taddr),
+        "r"(__float_as_uint(v[0].x)), "r"(__float_as_uint(v[0].y)), "r"(__float_as_uint(v[0].z)),
+        "r"(__float_as_uint(v[0].w)), "r"(__float_as_uint(v[1].x)), "r"(__float_as_uint(v[1].y)),
+        "r"(__float_as_uint(v[1].z)), "r"(__float_as_uint(v[1].w)), "r"(__float_as_uint(v[2].x)),
+        "r"(__float_as_uint(v[2].y)), "r"(__float_as_uint(v[2].z)), "r"(__float_as_uint(v[2].w)),
+        "r"(__float_as_uint(v[3].x)), "r"(__float_as_uint(v[3].y)), "r"(__float_as_uint(v[3].z)),
+        "r"(__float_as_uint(v[3].w))
+        : "memory");
+}
+
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// ---- bulk (non-tensor) async copies global -> shared, completing on an mbarrier ----
+
+// make mbarrier initialisations visible to the async proxy before the first copy
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+// one arrival on the mbarrier that also expects `bytes` of transaction count
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+                 : "memory");
+}
+
+// bytes (multiple of 16) from global src (16-byte aligned) to shared dst (16-byte aligned)
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint64_t* mbar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+        "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+        : "memory");
+}
 
 // registers -> 32 lanes x 32 consecutive 32-bit columns (the inverse of tmem_ld32)
 __device__ __forceinline__ void tmem_st32(uint32_t taddr, const float (&v)[32])

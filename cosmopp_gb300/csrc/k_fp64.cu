@@ -152,6 +152,67 @@ __global__ void __launch_bounds__(kThreads) build_c_packed(int n, int N, int lma
         if (kk[q] < np) out[(size_t)b * np + kk[q]] = v[q];
 }
 
+// CMatrixGenerator::getFiducialMatrix (source/c_matrix_generator.cpp:706-772), packed i <= j:
+//   element = sum_{l=lo}^{hi} (((fc_l * P_l) * B_l) * B_l) + (((m0 * (1 + x)) * B_2) * B_2)
+// with fc_l = cl_l * ((2l+1)/(4 pi)) and m0 = 100 cl_2 formed on the host as the reference
+// forms them; tab = [a | b | fc | beam], hi + 1 entries each; lo >= 2.
+__global__ void __launch_bounds__(kThreads) build_fid_packed(int n, int N, int lo, int hi,
+                                                             const double* __restrict__ xyz,
+                                                             const double* __restrict__ tab, double m0,
+                                                             double* __restrict__ out)
+{
+    extern __shared__ double sconst[];
+    const int L1 = hi + 1;
+    for (int e = threadIdx.x; e < 4 * L1; e += blockDim.x) sconst[e] = tab[e];
+    __syncthreads();
+    const double* sa = sconst;
+    const double* sb = sa + L1;
+    const double* sf = sb + L1;
+    const double* sbeam = sf + L1;
+    const long np = (long)n * (n + 1) / 2;
+    const long k0 = 4 * ((long)blockIdx.x * kThreads + threadIdx.x);
+    if (k0 >= np) return;
+    long j = (long)((sqrt(8.0 * (double)k0 + 1.0) - 1.0) * 0.5);
+    while (j * (j + 1) / 2 > k0) --j;
+    while ((j + 1) * (j + 2) / 2 <= k0) ++j;
+    long i = k0 - j * (j + 1) / 2;
+    double x[4], p0[4], p1[4], acc[4];
+    long kk[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        kk[q] = k0 + q;
+        x[q] = (kk[q] < np) ? pair_dot(xyz, N, (int)i, (int)j) : 0.0;
+        if (++i > j) { ++j; i = 0; }
+        p0[q] = 1.0;
+        p1[q] = x[q];
+        acc[q] = 0.0;
+    }
+    for (int l = 2; l < lo; ++l) {  // recurrence only (include/legendre.hpp:34)
+        const double a = sa[l], b = sb[l];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const double p = __dsub_rn(__dmul_rn(__dmul_rn(a, x[q]), p1[q]), __dmul_rn(b, p0[q]));
+            p0[q] = p1[q];
+            p1[q] = p;
+        }
+    }
+    for (int l = lo; l <= hi; ++l) {
+        const double a = sa[l], b = sb[l], f = sf[l], bm = sbeam[l];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const double p = __dsub_rn(__dmul_rn(__dmul_rn(a, x[q]), p1[q]), __dmul_rn(b, p0[q]));
+            acc[q] = __dadd_rn(acc[q], __dmul_rn(__dmul_rn(__dmul_rn(f, p), bm), bm));
+            p0[q] = p1[q];
+            p1[q] = p;
+        }
+    }
+    const double b2 = sbeam[2];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        if (kk[q] < np)
+            out[kk[q]] = __dadd_rn(acc[q], __dmul_rn(__dmul_rn(__dmul_rn(m0, __dadd_rn(1.0, x[q])), b2), b2));
+}
+
 // ln det = 2 sum_i ln L_ii over the n real pixels (source/matrix_impl.cpp:322-338), grid B
 __global__ void __launch_bounds__(kThreads) logdet_reduce(int n, int N, const double* __restrict__ diag,
                                                           double* __restrict__ logdet)
@@ -429,6 +490,19 @@ int fp64_build_packed(cg_ctx* ctx, int B, const double* d_cl, double* d_out, cud
     const long np = (long)ctx->n * (ctx->n + 1) / 2;
     build_c_packed<<<dim3((unsigned)((np + 4 * kThreads - 1) / (4 * kThreads)), B), kThreads, const_smem(ctx->lmax), s>>>(
         ctx->n, ctx->N, ctx->lmax, ctx->d_xyz, ctx->d_lega, ctx->d_legb, ctx->d_beam, d_cl, d_out);
+    count_launch(ctx);
+    CG_CUDA_TRY(ctx, cudaGetLastError());
+    return CG_OK;
+}
+
+int fp64_build_fiducial(cg_ctx* ctx, int lo, int hi, const double* d_tab, double m0, double* d_out, cudaStream_t s)
+{
+    const long np = (long)ctx->n * (ctx->n + 1) / 2;
+    const int smem = (int)(sizeof(double) * 4 * (hi + 1));
+    if (smem > 48 * 1024)
+        CG_CUDA_TRY(ctx, cudaFuncSetAttribute(build_fid_packed, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    build_fid_packed<<<(unsigned)((np + 4 * kThreads - 1) / (4 * kThreads)), kThreads, smem, s>>>(
+        ctx->n, ctx->N, lo, hi, ctx->d_xyz, d_tab, m0, d_out);
     count_launch(ctx);
     CG_CUDA_TRY(ctx, cudaGetLastError());
     return CG_OK;

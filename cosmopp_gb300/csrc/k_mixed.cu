@@ -212,11 +212,11 @@ __global__ void init_status(int B, const double* __restrict__ cl, int lmax, int*
 }
 
 // Forward contraction: A_b[t][e] = [e on the diagonal] + sum_l Ubar[t][e][l] eps[b][l],
-// written to A (factorised in place) and Acopy (kept for the refinement residual).
+// written to A.
 // grid (tiles * TILE_ELEMS / 128, ceil(B / 128)); 256 threads, 8 entries x 8 batch each.
 __global__ void __launch_bounds__(256) contract_fwd(int B, int lp, const float* __restrict__ U,
                                                     const float* __restrict__ eps, float* __restrict__ A,
-                                                    float* __restrict__ Acopy, size_t strideA)
+                                                    size_t strideA)
 {
     extern __shared__ float fsm[];
     float* sU = fsm;             // [lp][128]
@@ -267,10 +267,8 @@ __global__ void __launch_bounds__(256) contract_fwd(int B, int lp, const float* 
         }
         const size_t off = (size_t)bb * strideA + e_begin + e0;
         float4* pa = reinterpret_cast<float4*>(A + off);
-        float4* pc = reinterpret_cast<float4*>(Acopy + off);
-        const float4 v0 = make_float4(v[0], v[1], v[2], v[3]), v1 = make_float4(v[4], v[5], v[6], v[7]);
-        pa[0] = v0; pa[1] = v1;
-        pc[0] = v0; pc[1] = v1;
+        pa[0] = make_float4(v[0], v[1], v[2], v[3]);
+        pa[1] = make_float4(v[4], v[5], v[6], v[7]);
     }
 }
 
@@ -424,8 +422,8 @@ void mixed_free(cg_ctx* ctx)
 {
     MixedWork& w = ctx->wmx;
     cudaFree(w.Lref); cudaFree(w.Mref); cudaFree(w.Dinv_ref); cudaFree(w.diag_ref); cudaFree(w.Y); cudaFree(w.Z);
-    cudaFree(w.U); cudaFree(w.A); cudaFree(w.M); cudaFree(w.Dinv); cudaFree(w.diag); cudaFree(w.eps); cudaFree(w.y);
-    cudaFree(w.x); cudaFree(w.r); cudaFree(w.gpart); cudaFree(w.st); cudaFree(w.Acopy); cudaFree(w.cref);
+    cudaFree(w.U); cudaFree(w.A); cudaFree(w.Ms); cudaFree(w.Linv); cudaFree(w.diag); cudaFree(w.eps); cudaFree(w.y);
+    cudaFree(w.x); cudaFree(w.r); cudaFree(w.gpart); cudaFree(w.st); cudaFree(w.V); cudaFree(w.Ls); cudaFree(w.cref);
     cudaFree(w.ldref); cudaFree(w.part); cudaFree(w.ld); cudaFree(w.tcerr);
     w = MixedWork();
 }
@@ -456,18 +454,19 @@ static int ensure_batch_bufs(cg_ctx* ctx, int B)
 {
     MixedWork& w = ctx->wmx;
     if (w.cap >= B) return CG_OK;
-    cudaFree(w.A); cudaFree(w.Acopy); cudaFree(w.M); cudaFree(w.Dinv); cudaFree(w.diag); cudaFree(w.eps);
+    cudaFree(w.A); cudaFree(w.V); cudaFree(w.Ls); cudaFree(w.Ms); cudaFree(w.Linv); cudaFree(w.diag); cudaFree(w.eps);
     cudaFree(w.y); cudaFree(w.x); cudaFree(w.r); cudaFree(w.part); cudaFree(w.gpart); cudaFree(w.st); cudaFree(w.ld);
-    w.A = w.Acopy = w.M = w.Dinv = w.diag = w.eps = w.gpart = nullptr;
+    w.A = w.V = w.Ls = w.Ms = w.Linv = w.diag = w.eps = w.gpart = nullptr;
     w.y = w.x = w.r = w.part = w.ld = nullptr;
     w.st = nullptr;
     w.cap = 0;
     const size_t tiled = tiled_elems(ctx->nt);
     const int N = ctx->N, nt = ctx->nt, lp = lpad_of(ctx->lmax), ntile = ntiles_lower(nt);
     int rc = dalloc(ctx, &w.A, tiled * B);
-    if (!rc) rc = dalloc(ctx, &w.Acopy, tiled * B);
-    if (!rc) rc = dalloc(ctx, &w.M, tiled * B);
-    if (!rc) rc = dalloc(ctx, &w.Dinv, (size_t)B * (nt / 2) * 128 * 128);
+    if (!rc) rc = dalloc(ctx, &w.V, tiled * B);
+    if (!rc) rc = dalloc(ctx, &w.Ls, tc_split_elems(nt) * B);
+    if (!rc) rc = dalloc(ctx, &w.Ms, tc_split_elems(nt) * B);
+    if (!rc) rc = dalloc(ctx, &w.Linv, tc_linv_elems(nt) * B);
     if (!rc) rc = dalloc(ctx, &w.diag, (size_t)B * N);
     if (!rc) rc = dalloc(ctx, &w.eps, (size_t)B * lp);
     if (!rc) rc = dalloc(ctx, &w.y, (size_t)B * N);
@@ -608,23 +607,23 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
         const size_t smem = sizeof(float) * 2 * 128 * lp;
         cudaFuncSetAttribute(contract_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         contract_fwd<<<dim3((unsigned)(tiled / 128), (B + 127) / 128), 256, smem, s>>>(B, lp, w.U, w.eps, w.A,
-                                                                                        w.Acopy, tiled);
+                                                                                        tiled);
     }
     stage_mark(ctx, ST_CHOL, s);
-    if ((rc = tiled_cholesky_tc(ctx, B, nt, w.A, w.Dinv, w.diag, w.st, tiled, w.tcerr, s))) return rc;
+    if ((rc = tiled_cholesky_tc(ctx, B, nt, w.A, w.Ls, w.Linv, w.Ms, w.diag, w.st, w.tcerr, s))) return rc;
     logdet_mixed<<<B, 256, 0, s>>>(n, N, w.diag, w.ldref, w.ld);
     count_launch(ctx);
     stage_mark(ctx, ST_TRTRI, s);
-    if ((rc = tiled_trtri_tc(ctx, B, nt, w.A, w.Dinv, w.M, tiled, w.tcerr, s))) return rc;
+    if ((rc = tiled_trtri_tc(ctx, B, nt, w.Ls, w.Linv, w.Ms, w.tcerr, s))) return rc;
     stage_mark(ctx, ST_LAUUM, s);
-    if ((rc = tiled_lauum_tc(ctx, B, nt, w.M, w.A, tiled, w.tcerr, s))) return rc;
+    if ((rc = tiled_lauum_tc(ctx, B, nt, w.Ms, w.V, w.tcerr, s))) return rc;
     stage_mark(ctx, ST_SOLVE, s);
     // x = V y; r = y - A x; x += V r
-    symv_partials<false><<<dim3(ntile, B), 256, 0, s>>>(nt, w.A, tiled, w.y, N, w.part);
+    symv_partials<false><<<dim3(ntile, B), 256, 0, s>>>(nt, w.V, tiled, w.y, N, w.part);
     symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, w.part, w.x, N, nullptr, 1.0);
-    symv_partials<true><<<dim3(ntile, B), 256, 0, s>>>(nt, w.Acopy, tiled, w.x, N, w.part);
+    symv_partials<true><<<dim3(ntile, B), 256, 0, s>>>(nt, w.A, tiled, w.x, N, w.part);
     symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, w.part, w.r, N, w.y, -1.0);
-    symv_partials<false><<<dim3(ntile, B), 256, 0, s>>>(nt, w.A, tiled, w.r, N, w.part);
+    symv_partials<false><<<dim3(ntile, B), 256, 0, s>>>(nt, w.V, tiled, w.r, N, w.part);
     symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, w.part, w.x, N, w.x, 1.0);
     chi2_mixed<<<B, 256, 0, s>>>(n, N, N, w.y, w.x, w.ld, d_m2lnl, d_chi2, d_logdet);
     count_launch(ctx, 7);
@@ -632,7 +631,7 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
     if (d_grad) {
         const size_t sma = sizeof(float) * (64 * 49 + 64 * 65 + 2 * 64 * 64);
         cudaFuncSetAttribute(contract_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma);
-        contract_adj<<<dim3(ntile, (B + 63) / 64), 256, sma, s>>>(B, N, lp, w.U, w.A, tiled, w.x, w.gpart);
+        contract_adj<<<dim3(ntile, (B + 63) / 64), 256, sma, s>>>(B, N, lp, w.U, w.V, tiled, w.x, w.gpart);
         adj_finish<<<B, 64, 0, s>>>(B, ntile, lmax, lp, w.gpart, w.cref, d_grad);
         count_launch(ctx, 2);
     }

@@ -10,25 +10,41 @@
 // chunk) are ~2^-11 of the sum, so their drift is negligible and they
 // accumulate in one tensor-memory accumulator over the whole K loop.
 //
-// One CTA (256 threads) owns a 128x128 output supertile (2x2 of the 64x64
-// storage tiles) and runs a K loop over 32-wide chunks.  Thread t loads row
-// t % 128, K half t / 128 of the A and B chunks into registers two chunks
-// ahead; A is split hi/lo straight into tensor memory (tcgen05.st, lane = row),
-// B into a double-buffered shared-memory stage in the K-major canonical layout.
-// One thread issues the 12 MMAs (M128 N128 K8, A from tensor memory) of a chunk
-// and commits them to the stage's mbarrier.  Keeping A out of shared memory
-// removes its stores and the MMAs' re-reads of it there (shared-memory bandwidth
-// bounds this loop).
+// Operand storage ("split canonical", SC): every factor these kernels consume
+// is stored already split, hi and lo planes, each 64-row x 32-K block in the
+// MMA's K-major no-swizzle canonical layout (8-row x 16-byte core matrices,
+// LBO 128 B along K, SBO 1024 B between row groups).  An SC tile (64 x 64) is
+// [plane][K chunk][64 x 32 block] = 32 KB; two tiles stacked vertically give
+// the 128-row operand block of one chunk.  So the B operand of a chunk is four
+// (or two) contiguous bulk copies (cp.async.bulk) straight into shared memory,
+// and the A operand is eight coalesced 16-byte loads per thread that go
+// unchanged into tensor memory (tcgen05.st, lane = row): no per-element split
+// or layout work in the K loop.
+//
+// One CTA owns a 128x128 output supertile (2x2 storage tiles) and runs a
+// warp-specialised K loop over 32-wide chunks, the roles handing off through
+// mbarriers only:
+//   warps 0-7  (A producers): thread t loads row t % 128, K half t / 128 of the A
+//              chunk two chunks ahead into registers, stores it into one of two
+//              tensor-memory stages once the MMAs that last read that stage are
+//              done, and folds the finished hi*hi accumulator into its registers;
+//   warp 8     (MMA issue): one thread issues the 12 MMAs (M128 N128 K8, A from
+//              tensor memory, B from shared memory) of each chunk as soon as its A
+//              and B are in place, and commits them to the chunk's mbarriers; the
+//              tensor pipe throttles this thread, so it does nothing else;
+//   warp 9     (B copies): one thread keeps a ring of NSTB shared-memory stages
+//              filled with bulk copies, refilling a stage when its MMAs are done.
 //
 //   chol_tc_update: left-looking Cholesky, column block J: S_IJ = A_IJ - sum_{k<J} L_Ik L_Jk^T;
-//                   the diagonal CTA factors S_JJ = L_JJ L_JJ^T and inverts L_JJ in shared memory
-//   chol_tc_panel:  L_IJ = S_IJ L_JJ^-T                        (I > J)
-//   trtri_tc_row:   M_IJ = -L_II^-1 sum_{k=J}^{I-1} L_Ik M_kJ, M_II = L_II^-1   (M = L^-1)
-//   lauum_tc:       V_IJ = sum_{k >= row} M_kI^T M_kJ = (L L^T)^-1
-// (I, J in 128-row blocks; A, L and V in 64x64 column-major storage tiles, M in
-// transposed (row-major) tiles and the 128x128 inverses of L's diagonal blocks
-// column-major in Linv.  With these layouts every operand the K loops read has
-// element (r, k) at r + ld k: consecutive threads (rows) read consecutive words.)
+//                   the diagonal CTA factors S_JJ = L_JJ L_JJ^T, inverts L_JJ in shared memory and
+//                   writes L_JJ, Linv_J = L_JJ^-1 and (M_JJ)^T = Linv_J^T
+//   chol_tc_panel:  L_IJ = S_IJ Linv_J^T                       (I > J)
+//   trtri_tc_row:   (M_IJ)^T = -(sum_{k=J}^{I-1} M_kJ^T L_Ik^T) Linv_I^T    (M = L^-1, I > J)
+//   lauum_tc:       V_IJ = sum_{k >= I} M_kI^T M_kJ = (L L^T)^-1
+// Layouts: A (input, I + K_b) and V (output) in FP32 64x64 column-major tiles;
+// L and S in SC tiles (rows = L's rows, K = L's columns); M in SC tiles of M^T
+// (SC tile (I, J) holds (M_IJ)^T: rows = M's columns in tile J, K = M's rows in
+// tile I); Linv_J as a 128x128 SC block [K chunk][plane][128 x 32].
 #include "cg_internal.h"
 #include "cg_tc.cuh"
 
@@ -38,24 +54,26 @@ using namespace tc;
 
 namespace {
 
-constexpr int KC = 32;                     // K columns per chunk
-constexpr int STAGE_FLOATS = 128 * KC;     // one operand half (hi or lo) per stage
+constexpr int KC = 32;                          // K columns per chunk
 constexpr uint32_t LBO = 128, SBO = KC / 4 * 128;
 constexpr uint32_t IDESC = idesc_tf32(128, 128);
+constexpr int NPROD = 256;                      // A producers (warps 0-7)
+constexpr int NTH = NPROD + 64;                 // + the MMA warp and the copy warp
+constexpr int NSTB = 5;                         // B stages (bulk copies run NSTB - 2 chunks ahead)
+constexpr uint32_t STB_BYTES = 2u * 128 * KC * 4;  // one B stage: hi + lo, 128 rows x 32 K (32 KB)
+constexpr int SC_PLANE = TS * TS;               // floats per plane of an SC tile
+constexpr int SC_CHUNK = TS * KC;               // floats per 64 x 32 block
+constexpr int SC_TILE = 2 * SC_PLANE;           // floats per SC tile (32 KB)
+constexpr int LI_CHUNK = 2 * 128 * KC;          // floats per K chunk of a Linv block (hi + lo)
+constexpr int LINV_SC = 4 * LI_CHUNK;           // floats per Linv block (128 KB)
 
-struct TcSmem {
-    float buf[2][2][STAGE_FLOATS];         // [stage][b_hi, b_lo]
-};
+static_assert(SC_CHUNK * 4 == 8192 && LI_CHUNK * 4 == (int)STB_BYTES, "layout sizes");
 
-// stores one float4 (row r, K columns 4q..4q+3 of the chunk) as hi and lo parts
-__device__ __forceinline__ void put4(float* hi, float* lo, int r, int q, float4 v)
-{
-    const uint32_t o = kmajor_offset(r, 4 * q, KC) / 4;
-    const float4 h = make_float4(tf32_rn(v.x), tf32_rn(v.y), tf32_rn(v.z), tf32_rn(v.w));
-    *reinterpret_cast<float4*>(hi + o) = h;
-    *reinterpret_cast<float4*>(lo + o) =
-        make_float4(tf32_rn(v.x - h.x), tf32_rn(v.y - h.y), tf32_rn(v.z - h.z), tf32_rn(v.w - h.w));
-}
+// zero 64 x 32 block: the source of bulk copies for operand tiles above the diagonal
+__device__ __align__(128) float g_zero_block[SC_CHUNK];
+
+// float offset of element (r, k) inside one canonical block (r < 128, k < 32)
+__device__ __forceinline__ int canon_off(int r, int k) { return (r >> 3) * 256 + (k >> 2) * 32 + (r & 7) * 4 + (k & 3); }
 
 // Tensor-memory columns (512): hi*hi accumulators for the two chunk parities, the correction
 // accumulator, and the A operand (hi, lo) of the two stages.
@@ -71,161 +89,42 @@ __device__ __forceinline__ uint32_t lane_base() { return (uint32_t)(32 * ((threa
 // R[j] += accumulator at column col of this thread's row, columns 64 (t / 128) + j
 __device__ __forceinline__ void drain(uint32_t tm, uint32_t col, float (&R)[64])
 {
-    const uint32_t c0 = 64 * (threadIdx.x / 128);
 #pragma unroll
-    for (int part = 0; part < 4; ++part) {
-        float m[16];
-        tmem_ld16(tm + lane_base() + col + c0 + 16 * part, m);
+    for (int half = 0; half < 2; ++half) {
+        float m[32];
+        tmem_ld32w(tm + lane_base() + col + 64 * (threadIdx.x / 128) + 32 * half, m);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) R[16 * part + i] += m[i];
+        for (int i = 0; i < 32; ++i) R[32 * half + i] += m[i];
     }
-}
-
-constexpr int NTH = 256;  // threads per CTA: row r = t % 128, K half h = t / 128 (q in 4h .. 4h+3)
-
-// K loop: nchunks chunks; fa(c, r, q) / fb(c, r, q) return the float4 of row r, K columns
-// 4q..4q+3 of chunk c.  Loads run two chunks ahead of the MMAs.  On return R[j] holds the
-// product for row t % 128, column 64 (t / 128) + j (0 if nchunks == 0).  Returns false if an
-// mbarrier wait gave up.
-template <class FA, class FB>
-__device__ bool tc_kloop(int nchunks, FA fa, FB fb, TcSmem& sm, uint64_t* bars, uint32_t tm, float (&R)[64])
-{
-    const int r = threadIdx.x % 128, h = threadIdx.x / 128;
-#pragma unroll
-    for (int j = 0; j < 64; ++j) R[j] = 0.f;
-    float4 pa0[4], pb0[4], pa1[4], pb1[4];
-    bool ok = true;
-    if (nchunks > 0) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) { pa0[q] = fa(0, r, 4 * h + q); pb0[q] = fb(0, r, 4 * h + q); }
-    }
-    if (nchunks > 1) {
-#pragma unroll
-        for (int q = 0; q < 4; ++q) { pa1[q] = fa(1, r, 4 * h + q); pb1[q] = fb(1, r, 4 * h + q); }
-    }
-    auto step = [&](int c, float4 (&qa)[4], float4 (&qb)[4]) {
-        const int st = c & 1;
-        if (c >= 2) {
-            // MMAs of chunk c-2 done: its A columns and B stage are free, its hi*hi sum goes to R
-            ok &= mbar_wait(&bars[st], ((c - 2) >> 1) & 1);
-            fence_after();
-            drain(tm, col_main(st), R);
-        }
-        {
-            float ahi[16], alo[16];
-#pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                const float v[4] = {qa[q].x, qa[q].y, qa[q].z, qa[q].w};
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    ahi[4 * q + i] = tf32_rn(v[i]);
-                    alo[4 * q + i] = tf32_rn(v[i] - ahi[4 * q + i]);
-                }
-            }
-            tmem_st16(tm + lane_base() + col_a_hi(st) + 16 * h, ahi);
-            tmem_st16(tm + lane_base() + col_a_lo(st) + 16 * h, alo);
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q) put4(sm.buf[st][0], sm.buf[st][1], r, 4 * h + q, qb[q]);
-        if (c + 2 < nchunks) {
-#pragma unroll
-            for (int q = 0; q < 4; ++q) { qa[q] = fa(c + 2, r, 4 * h + q); qb[q] = fb(c + 2, r, 4 * h + q); }
-        }
-        tmem_wait_st();
-        fence_proxy_async();
-        fence_before();
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            fence_after();
-            const uint32_t bh = smem_u32(sm.buf[st][0]), bl = smem_u32(sm.buf[st][1]);
-            const uint32_t ah = tm + col_a_hi(st), al = tm + col_a_lo(st);
-#pragma unroll
-            for (int kk = 0; kk < KC / 8; ++kk) {
-                const uint32_t off = kk * 2 * LBO;
-                mma_tf32_ta(tm + COL_CORR, al + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, (c | kk) ? 1u : 0u);
-                mma_tf32_ta(tm + COL_CORR, ah + 8 * kk, smem_desc(bl + off, LBO, SBO), IDESC, 1u);
-                mma_tf32_ta(tm + col_main(st), ah + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, kk ? 1u : 0u);
-            }
-            mma_commit(&bars[st]);
-        }
-    };
-    for (int c = 0; c < nchunks; c += 2) {
-        step(c, pa0, pb0);
-        if (c + 1 < nchunks) step(c + 1, pa1, pb1);
-    }
-    // the last one or two chunks and the corrections: wait for the last commit (it tracks every
-    // earlier MMA) and fold
-    if (nchunks > 0) {
-        ok &= mbar_wait(&bars[(nchunks - 1) & 1], ((nchunks - 1) >> 1) & 1);
-        fence_after();
-        if (nchunks >= 2) drain(tm, col_main((nchunks - 2) & 1), R);
-        drain(tm, col_main((nchunks - 1) & 1), R);
-        drain(tm, COL_CORR, R);
-        fence_before();
-    }
-    return ok;
-}
-
-// element (r, m..m+3) of a column-major 64x64 tile (or of the transpose of a row-major one): four
-// loads, each coalesced across the warp's rows
-__device__ __forceinline__ float4 ld4_col(const float* t, int r, int m)
-{
-    return make_float4(t[r + TS * m], t[r + TS * (m + 1)], t[r + TS * (m + 2)], t[r + TS * (m + 3)]);
-}
-
-// the same for data written earlier in the same kernel: coherent L2 loads, not the read-only path
-__device__ __forceinline__ float4 ld4_col_cg(const float* t, int r, int m)
-{
-    return make_float4(__ldcg(t + r + TS * m), __ldcg(t + r + TS * (m + 1)), __ldcg(t + r + TS * (m + 2)),
-                       __ldcg(t + r + TS * (m + 3)));
-}
-
-// element (r, m..m+3) of a column-major 128x128 block (Linv)
-__device__ __forceinline__ float4 ld4_linv(const float* li, int r, int m)
-{
-    return make_float4(li[r + 128 * m], li[r + 128 * (m + 1)], li[r + 128 * (m + 2)], li[r + 128 * (m + 3)]);
-}
-
-constexpr float4 kZero4 = {0.f, 0.f, 0.f, 0.f};
-constexpr int LINV = 128 * 128;  // floats per 128x128 diagonal-block inverse
-
-
-// write the 128x128 result (this thread: row t % 128, columns 64 (t / 128) + j in R) times sgn
-// into the column-major tiles of supertile (I2, J2), skipping the tile above the diagonal
-__device__ __forceinline__ void store_block(const float (&R)[64], float* base, int I2, int J2, float sgn)
-{
-    const int row = threadIdx.x % 128, h = threadIdx.x / 128;
-    const int ti = 2 * I2 + row / 64, tj = 2 * J2 + h;
-    if (tj > ti) return;
-    float* t = base + (size_t)tile_index(ti, tj) * TILE_ELEMS;
-#pragma unroll
-    for (int j = 0; j < 64; ++j) t[(row % 64) + TS * j] = sgn * R[j];
-}
-
-// the same into row-major (transposed) tiles: this thread's row is 64 contiguous floats
-__device__ __forceinline__ void store_block_t(const float (&R)[64], float* base, int I2, int J2, float sgn)
-{
-    const int row = threadIdx.x % 128, h = threadIdx.x / 128;
-    const int ti = 2 * I2 + row / 64, tj = 2 * J2 + h;
-    if (tj > ti) return;
-    float4* t = reinterpret_cast<float4*>(base + (size_t)tile_index(ti, tj) * TILE_ELEMS + (row % 64) * TS);
-#pragma unroll
-    for (int j = 0; j < 16; ++j)
-        t[j] = make_float4(sgn * R[4 * j], sgn * R[4 * j + 1], sgn * R[4 * j + 2], sgn * R[4 * j + 3]);
 }
 
 struct TcCtl {
-    uint64_t bars[2];
+    uint64_t mma_bar[2];      // chunk parity: the chunk's MMAs completed (A stage free, hi*hi sum ready)
+    uint64_t a_full[2];       // chunk parity: the chunk's A is in tensor memory (one arrival per producer warp)
+    uint64_t b_full[NSTB];    // B stage landed
+    uint64_t b_empty[NSTB];   // B stage's MMAs completed
     uint32_t tbase;
     int bad;
 };
+
+__device__ __forceinline__ void init_bars(TcCtl& ctl)
+{
+    for (int i = 0; i < 2; ++i) {
+        mbar_init(&ctl.mma_bar[i], 1);
+        mbar_init(&ctl.a_full[i], NPROD / 32);
+    }
+    for (int i = 0; i < NSTB; ++i) {
+        mbar_init(&ctl.b_full[i], 1);
+        mbar_init(&ctl.b_empty[i], 1);
+    }
+    fence_mbar_init();
+}
 
 __device__ __forceinline__ uint32_t tc_begin(TcCtl& ctl)
 {
     if (threadIdx.x < 32) tmem_alloc(&ctl.tbase, TMEM_COLS);
     if (threadIdx.x == 0) {
-        mbar_init(&ctl.bars[0], 1);
-        mbar_init(&ctl.bars[1], 1);
+        init_bars(ctl);
         ctl.bad = 0;
     }
     fence_before();
@@ -241,21 +140,197 @@ __device__ __forceinline__ void tc_end(uint32_t tm)
     if (threadIdx.x < 32) tmem_dealloc(tm, TMEM_COLS);
 }
 
-// re-arm the two stage barriers for a second K loop in the same CTA (all earlier MMAs completed)
+// re-arm the barriers for a second K loop in the same CTA (every MMA and copy of the first completed)
 __device__ __forceinline__ void tc_rearm(TcCtl& ctl)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&ctl.bars[0])));
-        asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(&ctl.bars[1])));
-        mbar_init(&ctl.bars[0], 1);
-        mbar_init(&ctl.bars[1], 1);
+        uint64_t* all = &ctl.mma_bar[0];  // mma_bar, a_full, b_full, b_empty are contiguous
+        for (int i = 0; i < 4 + 2 * NSTB; ++i) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(all + i)));
+        init_bars(ctl);
     }
     __syncthreads();
 }
 
+// ---- operand access --------------------------------------------------------
+
+// A operand: row rr of SC tile t, K chunk kc, K columns 16h .. 16h+15, hi and lo.  Across a
+// warp (32 consecutive rows) every load covers four whole 128-byte core-matrix rows.
+template <bool COHERENT>
+__device__ __forceinline__ void ld_sc(const float* t, int rr, int kc, int h, float4 (&hi)[4], float4 (&lo)[4])
+{
+    const float* p = t + kc * SC_CHUNK + (rr >> 3) * 256 + (rr & 7) * 4 + 4 * h * 32;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float4* ph = reinterpret_cast<const float4*>(p + i * 32);
+        const float4* pl = reinterpret_cast<const float4*>(p + SC_PLANE + i * 32);
+        hi[i] = COHERENT ? __ldcg(ph) : __ldg(ph);
+        lo[i] = COHERENT ? __ldcg(pl) : __ldg(pl);
+    }
+}
+
+__device__ __forceinline__ void zero8(float4 (&hi)[4], float4 (&lo)[4])
+{
+#pragma unroll
+    for (int i = 0; i < 4; ++i) hi[i] = lo[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// B operand of one chunk from two stacked SC tiles (rows 0-63: top, 64-127: bot; nullptr = zero)
+__device__ __forceinline__ void bulk_tiles(const float* top, const float* bot, int kc, uint32_t dst, uint64_t* bar)
+{
+    mbar_arrive_expect_tx(bar, STB_BYTES);
+    const float* z = g_zero_block;
+    const uint32_t blk = SC_CHUNK * 4;
+    bulk_g2s(dst, top ? top + kc * SC_CHUNK : z, blk, bar);
+    bulk_g2s(dst + blk, bot ? bot + kc * SC_CHUNK : z, blk, bar);
+    bulk_g2s(dst + 2 * blk, top ? top + SC_PLANE + kc * SC_CHUNK : z, blk, bar);
+    bulk_g2s(dst + 3 * blk, bot ? bot + SC_PLANE + kc * SC_CHUNK : z, blk, bar);
+}
+
+// B operand of one chunk from a Linv block (K chunk kc: hi then lo, 16 KB each)
+__device__ __forceinline__ void bulk_linv(const float* li, int kc, uint32_t dst, uint64_t* bar)
+{
+    mbar_arrive_expect_tx(bar, STB_BYTES);
+    bulk_g2s(dst, li + kc * LI_CHUNK, STB_BYTES / 2, bar);
+    bulk_g2s(dst + STB_BYTES / 2, li + kc * LI_CHUNK + LI_CHUNK / 2, STB_BYTES / 2, bar);
+}
+
+// split row rr (K values v[0..63] times sgn) into a split canonical store: element (rr, k) at
+// base + (k / 32) * chunk_stride + plane * plane_stride + canon_off(rr, k % 32)
+__device__ __forceinline__ void st_split_row(float* base, int chunk_stride, int plane_stride, int rr,
+                                             const float (&v)[64], float sgn)
+{
+#pragma unroll
+    for (int kc = 0; kc < 2; ++kc)
+#pragma unroll
+        for (int k4 = 0; k4 < 8; ++k4) {
+            const int k = 32 * kc + 4 * k4;
+            const float4 x = make_float4(sgn * v[k], sgn * v[k + 1], sgn * v[k + 2], sgn * v[k + 3]);
+            const float4 h = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
+            const float4 l = make_float4(tf32_rn(x.x - h.x), tf32_rn(x.y - h.y), tf32_rn(x.z - h.z), tf32_rn(x.w - h.w));
+            float* p = base + kc * chunk_stride + (rr >> 3) * 256 + k4 * 32 + (rr & 7) * 4;
+            *reinterpret_cast<float4*>(p) = h;
+            *reinterpret_cast<float4*>(p + plane_stride) = l;
+        }
+}
+
+__device__ __forceinline__ void st_sc_row(float* tile, int rr, const float (&v)[64], float sgn)
+{
+    st_split_row(tile, SC_CHUNK, SC_PLANE, rr, v, sgn);
+}
+
+// ---- the K loop --------------------------------------------------------------
+
+// nchunks chunks; fa(c, r, h, hi, lo) loads the A chunk (row r, K half h); fb(c, dst, bar) issues
+// the B chunk's bulk copies into shared memory at dst.  Called by every thread of the CTA.  On
+// return the producer threads (t < NPROD) hold in R[j] the product for row t % 128, column
+// 64 (t / 128) + j (0 if nchunks == 0).  Returns false if an mbarrier wait gave up; waits give up
+// early once *err is set (by this or any other CTA), and a thread whose wait gave up skips its
+// later waits, so a failure ends the launch quickly.
+template <class FA, class FB>
+__device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& ctl, uint32_t tm, float (&R)[64],
+                         int* err)
+{
+    constexpr uint32_t kMaxIter = 1u << 22;
+    bool ok = true;
+    auto wait = [&](uint64_t* bar, uint32_t parity) {
+        if (!ok) return;
+        ok = mbar_wait(bar, parity, kMaxIter, err);
+        if (!ok) atomicExch(err, 1);
+    };
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const uint32_t sb = smem_u32(sbuf);
+#pragma unroll
+    for (int j = 0; j < 64; ++j) R[j] = 0.f;
+    if (warp < NPROD / 32) {
+        // ---- A producers: tensor-memory stage c & 1, then fold chunk c - 2's hi*hi sum
+        const int r = threadIdx.x % 128, h = threadIdx.x / 128;
+        float4 a0h[4], a0l[4], a1h[4], a1l[4];
+        if (nchunks > 0) fa(0, r, h, a0h, a0l);
+        if (nchunks > 1) fa(1, r, h, a1h, a1l);
+        auto step = [&](int c, float4 (&qh)[4], float4 (&ql)[4]) {
+            const int st = c & 1;
+            if (c >= 2) {  // chunk c-2's MMAs done: its A stage is free, its hi*hi sum goes to R
+                wait(&ctl.mma_bar[st], ((c - 2) >> 1) & 1);
+                fence_after();
+                drain(tm, col_main(st), R);
+            }
+            tmem_st16(tm + lane_base() + col_a_hi(st) + 16 * h, qh);
+            tmem_st16(tm + lane_base() + col_a_lo(st) + 16 * h, ql);
+            if (c + 2 < nchunks) fa(c + 2, r, h, qh, ql);
+            tmem_wait_st();
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&ctl.a_full[st]);
+        };
+        for (int c = 0; c < nchunks; c += 2) {
+            step(c, a0h, a0l);
+            if (c + 1 < nchunks) step(c + 1, a1h, a1l);
+        }
+        if (nchunks > 0) {
+            // every MMA is issued whatever happened, so the last commit always arrives: wait for it
+            // (bounded) even after a failure, so that no MMA still runs when tensor memory is freed
+            if (!mbar_wait(&ctl.mma_bar[(nchunks - 1) & 1], ((nchunks - 1) >> 1) & 1, kMaxIter)) {
+                ok = false;
+                atomicExch(err, 1);
+            }
+            fence_after();
+            if (nchunks >= 2) drain(tm, col_main((nchunks - 2) & 1), R);
+            drain(tm, col_main((nchunks - 1) & 1), R);
+            drain(tm, COL_CORR, R);
+            fence_before();
+        }
+    } else if (warp == NPROD / 32) {
+        // ---- MMA issue: one thread; the tensor pipe throttles it
+        if (lane == 0) {
+            for (int c = 0; c < nchunks; ++c) {
+                const int st = c & 1, sbi = c % NSTB;
+                wait(&ctl.a_full[st], (c >> 1) & 1);
+                wait(&ctl.b_full[sbi], (c / NSTB) & 1);
+                fence_after();
+                const uint32_t bh = sb + sbi * STB_BYTES, bl = bh + STB_BYTES / 2;
+                const uint32_t ah = tm + col_a_hi(st), al = tm + col_a_lo(st);
+#pragma unroll
+                for (int kk = 0; kk < KC / 8; ++kk) {
+                    const uint32_t off = kk * 2 * LBO;
+                    mma_tf32_ta(tm + COL_CORR, al + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, (c | kk) ? 1u : 0u);
+                    mma_tf32_ta(tm + COL_CORR, ah + 8 * kk, smem_desc(bl + off, LBO, SBO), IDESC, 1u);
+                    mma_tf32_ta(tm + col_main(st), ah + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, kk ? 1u : 0u);
+                }
+                mma_commit(&ctl.mma_bar[st]);
+                mma_commit(&ctl.b_empty[sbi]);
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---- B copies: one thread keeps the ring of NSTB stages full
+        if (lane == 0) {
+            for (int c = 0; c < nchunks; ++c) {
+                const int sbi = c % NSTB;
+                if (c >= NSTB) wait(&ctl.b_empty[sbi], ((c / NSTB) - 1) & 1);
+                fb(c, sb + sbi * STB_BYTES, &ctl.b_full[sbi]);
+            }
+        }
+        __syncwarp();
+    }
+    return ok;
+}
+
+// write the 128x128 result (this thread: row t % 128, columns 64 (t / 128) + j in R) times sgn
+// into the FP32 column-major tiles of supertile (I2, J2), skipping the tile above the diagonal
+__device__ __forceinline__ void store_block(const float (&R)[64], float* base, int I2, int J2, float sgn)
+{
+    if (threadIdx.x >= NPROD) return;
+    const int row = threadIdx.x % 128, h = threadIdx.x / 128;
+    const int ti = 2 * I2 + row / 64, tj = 2 * J2 + h;
+    if (tj > ti) return;
+    float* t = base + (size_t)tile_index(ti, tj) * TILE_ELEMS;
+#pragma unroll
+    for (int j = 0; j < 64; ++j) t[(row % 64) + TS * j] = sgn * R[j];
+}
+
 // Cholesky of the 128x128 block in s (column-major, leading dimension 129, lower part used)
-// and the inverse of its factor into inv (same layout); 256 threads.  Panels of 8 columns
+// and the inverse of its factor into inv (same layout); all NTH threads.  Panels of 8 columns
 // factorised column by column, then one rank-8 update of the trailing block.  The inverse is
 // block-recursive: inv11 = L11^-1, inv22 = L22^-1 (in parallel), inv21 = -inv22 (L21 inv11),
 // with tmp a 64x65 scratch block.  Sets *bad on a non-positive pivot.
@@ -329,37 +404,42 @@ __device__ void factor_block128(float* s, float* inv, float* tmp, int* bad)
     __syncthreads();
 }
 
+
 // Left-looking Cholesky, column block J2, row block I2 = J2 + blockIdx.x; grid (nt2 - J2, B).
-// Off-diagonal blocks: A_IJ <- A_IJ - sum_{k < 2 J2} L_I,k L_J,k^T (S, stored in place).
-// Diagonal block: S_JJ factorised to L_JJ (in place), its diagonal to diag, its inverse to Linv.
-__global__ void __launch_bounds__(NTH) chol_tc_update(int J2, int nt, float* __restrict__ A, size_t strideA,
-                                                      float* __restrict__ Linv, float* __restrict__ diag,
+// Off-diagonal blocks: S_IJ = A_IJ - sum_{k < 2 J2} L_I,k L_J,k^T into the L storage (SC).
+// Diagonal block: S_JJ factorised, L_JJ into the L storage, its inverse into Linv and, transposed,
+// into the M storage, its diagonal into diag.
+__global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, const float* __restrict__ A,
+                                                      float* __restrict__ Ls, float* __restrict__ Linv,
+                                                      float* __restrict__ Ms, float* __restrict__ diag,
                                                       int* __restrict__ status, int* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    TcSmem& sm = *reinterpret_cast<TcSmem*>(smem_raw);
     __shared__ TcCtl ctl;
     const int I2 = J2 + blockIdx.x, b = blockIdx.y, nt2 = nt / 2;
-    float* Ab = A + (size_t)b * strideA;
+    const size_t ntile = (size_t)ntiles_lower(nt);
+    const float* Ab = A + (size_t)b * ntile * TILE_ELEMS;
+    float* Lb = Ls + (size_t)b * ntile * SC_TILE;
     const uint32_t tm = tc_begin(ctl);
     const int nchunks = 2 * J2 * (TS / KC);
-    auto fa = [&](int c, int r, int q) -> float4 {
-        const float* t = Ab + (size_t)tile_index(2 * I2 + r / 64, c / 2) * TILE_ELEMS;
-        return ld4_col(t, r % 64, (c % 2) * KC + 4 * q);
+    auto fa = [&](int c, int r, int h, float4 (&hi)[4], float4 (&lo)[4]) {
+        ld_sc<false>(Lb + (size_t)tile_index(2 * I2 + r / 64, c / 2) * SC_TILE, r % 64, c % 2, h, hi, lo);
     };
-    auto fb = [&](int c, int r, int q) -> float4 {
-        const float* t = Ab + (size_t)tile_index(2 * J2 + r / 64, c / 2) * TILE_ELEMS;
-        return ld4_col(t, r % 64, (c % 2) * KC + 4 * q);
+    auto fb = [&](int c, uint32_t dst, uint64_t* bar) {
+        bulk_tiles(Lb + (size_t)tile_index(2 * J2, c / 2) * SC_TILE, Lb + (size_t)tile_index(2 * J2 + 1, c / 2) * SC_TILE,
+                   c % 2, dst, bar);
     };
     float R[64];
-    const bool ok = tc_kloop(nchunks, fa, fb, sm, ctl.bars, tm, R);
-    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
-    const int row = threadIdx.x % 128, c0 = 64 * (threadIdx.x / 128);
+    tc_kloop(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
+    const int row = threadIdx.x % 128, h = threadIdx.x / 128;
+    const bool prod = threadIdx.x < NPROD;
     if (I2 > J2) {
-        if (nchunks > 0) {
-            float* t = Ab + (size_t)tile_index(2 * I2 + row / 64, 2 * J2 + c0 / 64) * TILE_ELEMS;
+        if (prod) {
+            const int ti = 2 * I2 + row / 64, tj = 2 * J2 + h;
+            const float* a = Ab + (size_t)tile_index(ti, tj) * TILE_ELEMS + row % 64;
 #pragma unroll
-            for (int j = 0; j < 64; ++j) t[(row % 64) + TS * j] -= R[j];
+            for (int j = 0; j < 64; ++j) R[j] = a[TS * j] - R[j];
+            st_sc_row(Lb + (size_t)tile_index(ti, tj) * SC_TILE, row % 64, R, 1.f);
         }
         tc_end(tm);
         return;
@@ -368,176 +448,182 @@ __global__ void __launch_bounds__(NTH) chol_tc_update(int J2, int nt, float* __r
     float* s = reinterpret_cast<float*>(smem_raw);
     float* inv = s + 128 * 129;
     float* tmp = inv + 128 * 129;
-    __syncthreads();
-    {
-        const int ti = 2 * J2 + row / 64, tj = 2 * J2 + c0 / 64;
+    __syncthreads();  // every MMA and copy of the K loop is complete: the stages may be reused
+    if (prod) {
+        const int ti = 2 * J2 + row / 64, tj = 2 * J2 + h;
         if (tj <= ti) {
             const float* t = Ab + (size_t)tile_index(ti, tj) * TILE_ELEMS;
 #pragma unroll
-            for (int j = 0; j < 64; ++j) s[(c0 + j) * 129 + row] = t[(row % 64) + TS * j] - R[j];
+            for (int j = 0; j < 64; ++j) s[(64 * h + j) * 129 + row] = t[(row % 64) + TS * j] - R[j];
         }
     }
     __syncthreads();
     factor_block128(s, inv, tmp, &ctl.bad);
-    // L_JJ into the three lower tiles (strict upper of the diagonal tiles zeroed), diag, Linv column-major
-    for (int col = c0; col < c0 + 64; ++col) {
-        const int ti = 2 * J2 + row / 64, tj = 2 * J2 + col / 64;
-        if (tj > ti) continue;
-        float* t = Ab + (size_t)tile_index(ti, tj) * TILE_ELEMS;
-        t[(row % 64) + TS * (col % 64)] = (row >= col) ? s[col * 129 + row] : 0.f;
+    float v[64];
+    if (prod) {   // L_JJ into the three lower SC tiles, strict upper of the diagonal tiles zeroed
+        const int ti = 2 * J2 + row / 64, tj = 2 * J2 + h;
+        if (tj <= ti) {
+#pragma unroll
+            for (int j = 0; j < 64; ++j) v[j] = (row >= 64 * h + j) ? s[(64 * h + j) * 129 + row] : 0.f;
+            st_sc_row(Lb + (size_t)tile_index(ti, tj) * SC_TILE, row % 64, v, 1.f);
+        }
     }
     if (threadIdx.x < 128) diag[(size_t)b * nt * TS + J2 * 128 + row] = s[row * 129 + row];
-    float* li = Linv + ((size_t)b * nt2 + J2) * LINV;
-    for (int col = c0; col < c0 + 64; ++col) li[col * 128 + row] = inv[col * 129 + row];
+    if (prod) {   // Linv_J: row `row`, K columns 64h .. 64h+63 (chunks 2h, 2h+1)
+        float* li = Linv + ((size_t)b * nt2 + J2) * LINV_SC;
+#pragma unroll
+        for (int j = 0; j < 64; ++j) v[j] = inv[(64 * h + j) * 129 + row];
+        st_split_row(li + 2 * h * LI_CHUNK, LI_CHUNK, LI_CHUNK / 2, row, v, 1.f);
+    }
+    if (prod) {   // (M_JJ)^T = Linv_J^T: SC tile (2J2 + h, 2J2 + cc/64), row cc % 64 (M's column), K = M's rows
+        const int cc = row;
+        const int ti = 2 * J2 + h, tj = 2 * J2 + cc / 64;
+        if (tj <= ti) {
+            float* Mb = Ms + (size_t)b * ntile * SC_TILE;
+#pragma unroll
+            for (int j = 0; j < 64; ++j) v[j] = inv[cc * 129 + 64 * h + j];
+            st_sc_row(Mb + (size_t)tile_index(ti, tj) * SC_TILE, cc % 64, v, 1.f);
+        }
+    }
     if (threadIdx.x == 0 && ctl.bad && status && status[b] == CG_OK) status[b] = CG_ERR_NOT_PD;
     tc_end(tm);
 }
 
 // L_IJ = S_IJ Linv_J^T for I2 = J2 + 1 + blockIdx.x; grid (nt2 - J2 - 1, B)
-__global__ void __launch_bounds__(NTH) chol_tc_panel(int J2, int nt, float* __restrict__ A, size_t strideA,
+__global__ void __launch_bounds__(NTH, 1) chol_tc_panel(int J2, int nt, float* __restrict__ Ls,
                                                      const float* __restrict__ Linv, int* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    TcSmem& sm = *reinterpret_cast<TcSmem*>(smem_raw);
     __shared__ TcCtl ctl;
     const int I2 = J2 + 1 + blockIdx.x, b = blockIdx.y, nt2 = nt / 2;
-    float* Ab = A + (size_t)b * strideA;
-    const float* li = Linv + ((size_t)b * nt2 + J2) * LINV;
+    float* Lb = Ls + (size_t)b * ntiles_lower(nt) * SC_TILE;
+    const float* li = Linv + ((size_t)b * nt2 + J2) * LINV_SC;
     const uint32_t tm = tc_begin(ctl);
-    // A(r, m) = S(r, m): block column m/64 of row block I2; B(c, m) = Linv(c, m) column-major
-    auto fa = [&](int c, int r, int q) -> float4 {
-        const int m = c * KC + 4 * q;
-        const float* t = Ab + (size_t)tile_index(2 * I2 + r / 64, 2 * J2 + m / 64) * TILE_ELEMS;
-        return ld4_col(t, r % 64, m % 64);
+    // A(r, m) = S_IJ(r, m), SC tiles (2 I2 + r/64, 2 J2 + m/64); B(c, m) = Linv_J(c, m)
+    auto fa = [&](int c, int r, int h, float4 (&hi)[4], float4 (&lo)[4]) {
+        ld_sc<false>(Lb + (size_t)tile_index(2 * I2 + r / 64, 2 * J2 + c / 2) * SC_TILE, r % 64, c % 2, h, hi, lo);
     };
-    auto fb = [&](int c, int r, int q) -> float4 { return ld4_linv(li, r, c * KC + 4 * q); };
+    auto fb = [&](int c, uint32_t dst, uint64_t* bar) { bulk_linv(li, c, dst, bar); };
     float R[64];
-    const bool ok = tc_kloop(128 / KC, fa, fb, sm, ctl.bars, tm, R);
-    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+    tc_kloop(128 / KC, fa, fb, smem_raw, ctl, tm, R, err);
     __syncthreads();  // every S read is done before the tiles are overwritten
-    store_block(R, Ab, I2, J2, 1.f);
+    const int row = threadIdx.x % 128, h = threadIdx.x / 128;
+    if (threadIdx.x < NPROD)
+        st_sc_row(Lb + (size_t)tile_index(2 * I2 + row / 64, 2 * J2 + h) * SC_TILE, row % 64, R, 1.f);
     tc_end(tm);
 }
 
-// Row block I2 of M = L^-1; CTA J2 = blockIdx.x <= I2; grid (I2 + 1, B)
-__global__ void __launch_bounds__(NTH) trtri_tc_row(int I2, int nt, const float* __restrict__ Lm,
-                                                    const float* __restrict__ Linv, float* __restrict__ M,
-                                                    size_t strideA, int* __restrict__ err)
+// Row block I2 of M = L^-1, off-diagonal blocks J2 = blockIdx.x < I2; grid (I2, B).  Computes
+// the transposes: S^T = sum_{k=2 J2}^{2 I2 - 1} M_kJ^T L_Ik^T, then (M_IJ)^T = -S^T Linv_I^T.
+__global__ void __launch_bounds__(NTH, 1) trtri_tc_row(int I2, int nt, const float* __restrict__ Ls,
+                                                    const float* __restrict__ Linv, float* __restrict__ Ms,
+                                                    int* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    TcSmem& sm = *reinterpret_cast<TcSmem*>(smem_raw);
     __shared__ TcCtl ctl;
     const int J2 = blockIdx.x, b = blockIdx.y, nt2 = nt / 2;
-    const float* Lb = Lm + (size_t)b * strideA;
-    float* Mb = M + (size_t)b * strideA;
-    const float* li = Linv + ((size_t)b * nt2 + I2) * LINV;
-    const int row = threadIdx.x % 128, c0 = 64 * (threadIdx.x / 128);
-    if (J2 == I2) {  // M_II = Linv_I, into the three lower row-major tiles
-        for (int col = c0; col < c0 + 64; ++col) {
-            const int ti = 2 * I2 + row / 64, tj = 2 * I2 + col / 64;
-            if (tj > ti) continue;
-            Mb[(size_t)tile_index(ti, tj) * TILE_ELEMS + (row % 64) * TS + (col % 64)] = li[col * 128 + row];
-        }
-        return;
-    }
+    const size_t ntile = (size_t)ntiles_lower(nt);
+    const float* Lb = Ls + (size_t)b * ntile * SC_TILE;
+    float* Mb = Ms + (size_t)b * ntile * SC_TILE;
+    const float* li = Linv + ((size_t)b * nt2 + I2) * LINV_SC;
+    const int row = threadIdx.x % 128, h = threadIdx.x / 128;
     const uint32_t tm = tc_begin(ctl);
-    // S = sum_{k=2 J2}^{2 I2 - 1} L_{I,k} M_{k,J}: A(r, m) = L tile (2 I2 + r/64, k)(r%64, m) column-major,
-    // B(c, m) = M tile (k, 2 J2 + c/64)(m, c%64) row-major, at c%64 + 64 m
+    // A(c, m) = M_kJ(m, c): SC tile (k, 2 J2 + c/64) of M^T (zero above the diagonal);
+    // B(r, m) = L_Ik(r, m): SC tiles (2 I2, k), (2 I2 + 1, k)
     const int k0 = 2 * J2;
     const int nchunks = (2 * I2 - k0) * (TS / KC);
-    auto fa = [&](int c, int r, int q) -> float4 {
-        const int k = k0 + c / 2;
-        const float* t = Lb + (size_t)tile_index(2 * I2 + r / 64, k) * TILE_ELEMS;
-        return ld4_col(t, r % 64, (c % 2) * KC + 4 * q);
-    };
-    auto fb = [&](int c, int r, int q) -> float4 {
+    auto fa = [&](int c, int r, int hh, float4 (&hi)[4], float4 (&lo)[4]) {
         const int k = k0 + c / 2, col = 2 * J2 + r / 64;
-        if (k < col) return kZero4;
-        const float* t = Mb + (size_t)tile_index(k, col) * TILE_ELEMS;
-        return ld4_col(t, r % 64, (c % 2) * KC + 4 * q);
+        if (k < col) zero8(hi, lo);
+        else ld_sc<false>(Mb + (size_t)tile_index(k, col) * SC_TILE, r % 64, c % 2, hh, hi, lo);
+    };
+    auto fb = [&](int c, uint32_t dst, uint64_t* bar) {
+        const int k = k0 + c / 2;
+        bulk_tiles(Lb + (size_t)tile_index(2 * I2, k) * SC_TILE, Lb + (size_t)tile_index(2 * I2 + 1, k) * SC_TILE,
+                   c % 2, dst, bar);
     };
     float R[64];
-    bool ok = tc_kloop(nchunks, fa, fb, sm, ctl.bars, tm, R);
-    // S into the M tiles of block (I2, J2) (not read by any other block of this launch)
-    store_block_t(R, Mb, I2, J2, 1.f);
-    __syncthreads();
-    tc_rearm(ctl);
-    // M_IJ = -Linv_I S: A(r, m) = Linv(r, m) column-major; B(c, m) = S(m, c), row-major tiles
-    auto fa2 = [&](int c, int r, int q) -> float4 { return ld4_linv(li, r, c * KC + 4 * q); };
-    auto fb2 = [&](int c, int r, int q) -> float4 {
-        const int m = c * KC + 4 * q;
-        const float* t = Mb + (size_t)tile_index(2 * I2 + m / 64, 2 * J2 + r / 64) * TILE_ELEMS;
-        return ld4_col_cg(t, r % 64, m % 64);
+    tc_kloop(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
+    // S^T into the M storage of block (I2, J2): row = M's column, K = M's rows 64h .. 64h+63
+    if (threadIdx.x < NPROD)
+        st_sc_row(Mb + (size_t)tile_index(2 * I2 + h, 2 * J2 + row / 64) * SC_TILE, row % 64, R, 1.f);
+    tc_rearm(ctl);  // its __syncthreads also makes the S^T stores visible to the whole CTA
+    // A(c, m) = S^T(c, m): written above by this CTA (coherent loads); B(r, m) = Linv_I(r, m)
+    auto fa2 = [&](int c, int r, int hh, float4 (&hi)[4], float4 (&lo)[4]) {
+        ld_sc<true>(Mb + (size_t)tile_index(2 * I2 + c / 2, 2 * J2 + r / 64) * SC_TILE, r % 64, c % 2, hh, hi, lo);
     };
-    ok &= tc_kloop(128 / KC, fa2, fb2, sm, ctl.bars, tm, R);
-    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
-    __syncthreads();
-    store_block_t(R, Mb, I2, J2, -1.f);
+    auto fb2 = [&](int c, uint32_t dst, uint64_t* bar) { bulk_linv(li, c, dst, bar); };
+    tc_kloop(128 / KC, fa2, fb2, smem_raw, ctl, tm, R, err);
+    __syncthreads();  // every S^T read is done before the tiles are overwritten
+    if (threadIdx.x < NPROD)
+        st_sc_row(Mb + (size_t)tile_index(2 * I2 + h, 2 * J2 + row / 64) * SC_TILE, row % 64, R, -1.f);
     tc_end(tm);
 }
 
-
-// V_IJ (128x128 supertile, lower) = sum over k of M_k,I^T M_k,J with M in row-major tiles; V in
-// column-major tiles.
-// grid (supertiles of the lower triangle, B), 256 threads.
-__global__ void __launch_bounds__(NTH) lauum_tc(int nt, const float* __restrict__ M, float* __restrict__ V,
-                                                size_t strideA, int* __restrict__ err)
+// V_IJ (128x128 supertile, lower) = sum over k of M_k,I^T M_k,J from the M^T storage; V in FP32
+// column-major tiles.  grid (supertiles of the lower triangle, B).
+__global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restrict__ Ms, float* __restrict__ V,
+                                                int* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    TcSmem& sm = *reinterpret_cast<TcSmem*>(smem_raw);
     __shared__ TcCtl ctl;
     int I2, J2;
     tile_coords(blockIdx.x, I2, J2);
     const int b = blockIdx.y;
-    const float* Mb = M + (size_t)b * strideA;
+    const size_t ntile = (size_t)ntiles_lower(nt);
+    const float* Mb = Ms + (size_t)b * ntile * SC_TILE;
     const uint32_t tm = tc_begin(ctl);
-    const int k0 = 2 * I2;                     // first tile row with a non-zero M_k,row
+    const int k0 = 2 * I2;  // first tile row with a non-zero M_k,I
     const int nchunks = (nt - k0) * (TS / KC);
-    // A(r, m) = M_{k, 2I2 + r/64}(m, r%64): tile (k, col) row-major, element (m, r') at r' + 64 m
-    auto fa = [&](int c, int r, int q) -> float4 {
+    // A(r, m) = M_{k, 2I2 + r/64}(m, r%64); B(c, m) = M_{k, 2J2 + c/64}(m, c%64); zero above the diagonal
+    auto fa = [&](int c, int r, int h, float4 (&hi)[4], float4 (&lo)[4]) {
         const int k = k0 + c / 2, col = 2 * I2 + r / 64;
-        if (k < col) return make_float4(0.f, 0.f, 0.f, 0.f);
-        const float* t = Mb + (size_t)tile_index(k, col) * TILE_ELEMS;
-        return ld4_col(t, r % 64, (c % 2) * KC + 4 * q);
+        if (k < col) zero8(hi, lo);
+        else ld_sc<false>(Mb + (size_t)tile_index(k, col) * SC_TILE, r % 64, c % 2, h, hi, lo);
     };
-    auto fb = [&](int c, int r, int q) -> float4 {
-        const int k = k0 + c / 2, col = 2 * J2 + r / 64;
-        if (k < col) return make_float4(0.f, 0.f, 0.f, 0.f);
-        const float* t = Mb + (size_t)tile_index(k, col) * TILE_ELEMS;
-        return ld4_col(t, r % 64, (c % 2) * KC + 4 * q);
+    auto fb = [&](int c, uint32_t dst, uint64_t* bar) {
+        const int k = k0 + c / 2;
+        const float* top = (k >= 2 * J2) ? Mb + (size_t)tile_index(k, 2 * J2) * SC_TILE : nullptr;
+        const float* bot = (k >= 2 * J2 + 1) ? Mb + (size_t)tile_index(k, 2 * J2 + 1) * SC_TILE : nullptr;
+        bulk_tiles(top, bot, c % 2, dst, bar);
     };
     float R[64];
-    const bool ok = tc_kloop(nchunks, fa, fb, sm, ctl.bars, tm, R);
-    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
-    store_block(R, V + (size_t)b * strideA, I2, J2, 1.f);
+    tc_kloop(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
+    store_block(R, V + (size_t)b * ntile * TILE_ELEMS, I2, J2, 1.f);
     tc_end(tm);
 }
 
 }  // namespace
 
-static size_t tc_smem()
+static int tc_smem()
 {
-    const size_t fac = (2 * 128 * 129 + 64 * 65) * sizeof(float);  // block, its inverse, scratch
-    return sizeof(TcSmem) > fac ? sizeof(TcSmem) : fac;
+    const int fac = (2 * 128 * 129 + 64 * 65) * (int)sizeof(float);  // block, its inverse, scratch
+    const int ring = NSTB * (int)STB_BYTES;
+    return (ring > fac ? ring : fac) + 1024;
 }
 
-int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, float* A, float* Linv, float* diag, int* status, size_t strideA,
-                      int* d_err, cudaStream_t s)
+template <class K>
+static int set_smem(cg_ctx* ctx, K kern)
+{
+    CG_CUDA_TRY(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, tc_smem()));
+    return CG_OK;
+}
+
+size_t tc_split_elems(int nt) { return (size_t)ntiles_lower(nt) * SC_TILE; }
+size_t tc_linv_elems(int nt) { return (size_t)(nt / 2) * LINV_SC; }
+
+int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, float* Linv, float* Ms, float* diag,
+                      int* status, int* d_err, cudaStream_t s)
 {
     if (nt % 2) { ctx->err = "tensor-core Cholesky needs an even tile count"; return CG_ERR_BAD_ARG; }
-    const int smem = (int)tc_smem() + 1024;
-    static bool attr = false;
-    if (!attr) {
-        CG_CUDA_TRY(ctx, cudaFuncSetAttribute(chol_tc_update, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        CG_CUDA_TRY(ctx, cudaFuncSetAttribute(chol_tc_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        attr = true;
-    }
+    int rc;
+    if ((rc = set_smem(ctx, chol_tc_update)) || (rc = set_smem(ctx, chol_tc_panel))) return rc;
     const int nt2 = nt / 2;
     for (int J2 = 0; J2 < nt2; ++J2) {
-        chol_tc_update<<<dim3(nt2 - J2, B), NTH, smem, s>>>(J2, nt, A, strideA, Linv, diag, status, d_err);
+        chol_tc_update<<<dim3(nt2 - J2, B), NTH, tc_smem(), s>>>(J2, nt, A, Ls, Linv, Ms, diag, status, d_err);
         count_launch(ctx);
         if (J2 + 1 < nt2) {
-            chol_tc_panel<<<dim3(nt2 - J2 - 1, B), NTH, smem, s>>>(J2, nt, A, strideA, Linv, d_err);
+            chol_tc_panel<<<dim3(nt2 - J2 - 1, B), NTH, tc_smem(), s>>>(J2, nt, Ls, Linv, d_err);
             count_launch(ctx);
         }
     }
@@ -545,36 +631,28 @@ int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, float* A, float* Linv, float* 
     return CG_OK;
 }
 
-int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* L, const float* Linv, float* M, size_t strideA, int* d_err,
+int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* Ls, const float* Linv, float* Ms, int* d_err,
                    cudaStream_t s)
 {
     if (nt % 2) { ctx->err = "tensor-core trtri needs an even tile count"; return CG_ERR_BAD_ARG; }
-    const int smem = (int)tc_smem() + 1024;
-    static bool attr = false;
-    if (!attr) {
-        CG_CUDA_TRY(ctx, cudaFuncSetAttribute(trtri_tc_row, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        attr = true;
-    }
+    int rc;
+    if ((rc = set_smem(ctx, trtri_tc_row))) return rc;
     const int nt2 = nt / 2;
-    for (int I2 = 0; I2 < nt2; ++I2) {
-        trtri_tc_row<<<dim3(I2 + 1, B), NTH, smem, s>>>(I2, nt, L, Linv, M, strideA, d_err);
+    for (int I2 = 1; I2 < nt2; ++I2) {  // the diagonal blocks M_II come from the Cholesky
+        trtri_tc_row<<<dim3(I2, B), NTH, tc_smem(), s>>>(I2, nt, Ls, Linv, Ms, d_err);
         count_launch(ctx);
     }
     CG_CUDA_TRY(ctx, cudaGetLastError());
     return CG_OK;
 }
 
-int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* M, float* V, size_t strideA, int* d_err, cudaStream_t s)
+int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, float* V, int* d_err, cudaStream_t s)
 {
     if (nt % 2) { ctx->err = "tensor-core lauum needs an even tile count"; return CG_ERR_BAD_ARG; }
-    const int smem = (int)tc_smem() + 1024;
-    static bool attr = false;
-    if (!attr) {
-        CG_CUDA_TRY(ctx, cudaFuncSetAttribute(lauum_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-        attr = true;
-    }
+    int rc;
+    if ((rc = set_smem(ctx, lauum_tc))) return rc;
     const int nt2 = nt / 2;
-    lauum_tc<<<dim3(nt2 * (nt2 + 1) / 2, B), NTH, smem, s>>>(nt, M, V, strideA, d_err);
+    lauum_tc<<<dim3(nt2 * (nt2 + 1) / 2, B), NTH, tc_smem(), s>>>(nt, Ms, V, d_err);
     count_launch(ctx);
     CG_CUDA_TRY(ctx, cudaGetLastError());
     return CG_OK;

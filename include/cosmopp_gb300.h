@@ -84,6 +84,16 @@ int cg_unit_vectors(const cg_ctx* ctx, double* xyz);             /* [n][3] */
 int cg_build_cmatrix(cg_ctx* ctx, const double* cl, double* out_packed);
 /* the same for B C_l vectors ([B][lmax+1] -> [B][n(n+1)/2]) */
 int cg_build_cmatrix_batched(cg_ctx* ctx, int B, const double* cl, double* out_packed);
+/* CMatrixGenerator::getFiducialMatrix (include/c_matrix_generator.hpp:126,
+   source/c_matrix_generator.cpp:706-772): packed sum over l = lmax+1 .. lmax_max of
+   C_l (2l+1)/(4pi) B_l^2 P_l(x_ij), plus the monopole/dipole marginalisation term
+   100 C_2 (1 + x_ij) B_2^2, for this context's pixels.  The reference uses
+   lmax_max = 4 nside; cl has lmax_max + 1 entries.  beam [lmax_max + 1] is nullable:
+   NULL = the Gaussian beam of the context's fwhm_deg (unit pixel window).
+   Bit-identical to the reference.  1 <= lmax < lmax_max <= CG_FIDUCIAL_LMAX_MAX. */
+#define CG_FIDUCIAL_LMAX_MAX 4096
+int cg_fiducial_matrix(cg_ctx* ctx, const double* cl, int lmax, int lmax_max, const double* beam,
+                       double* out_packed);
 
 /* ---- likelihood + gradient ---------------------------------------------- */
 /* -2lnL = d^T C^-1 d + ln det C for B C_l vectors, C = C(cl_b) + noise

@@ -177,6 +177,39 @@ public:
         }
         return m;
     }
+    /// source/c_matrix_generator.cpp:706-772: sum over l = lMax+1 .. 4 nSide plus the
+    /// monopole/dipole term 100 C_2 (1 + x) B_2^2; cl must reach l = 4 nSide.  Bit-identical
+    /// to the reference.  Returns a new CMatrix the caller deletes.
+    static CMatrix* getFiducialMatrix(const std::vector<double>& cl, long nSide, int lMax, double fwhm,
+                                      const std::vector<int>* goodPixels = NULL, const void* /*lp*/ = NULL,
+                                      int device = 0)
+    {
+        const int lMaxMax = (int)(4 * nSide);
+        if ((long)cl.size() < lMaxMax + 1) cosmopp_gb300_detail::raise("getFiducialMatrix: cl must reach l = 4 nSide");
+        cg_config cfg;
+        cg_config_init(&cfg);
+        cfg.nside = nSide;
+        cfg.scheme = CG_SCHEME_NEST;
+        if (goodPixels) {
+            cfg.good_pixels = goodPixels->data();
+            cfg.n = (int)goodPixels->size();
+        }
+        cfg.lmax = lMax;
+        cfg.fwhm_deg = fwhm;
+        cfg.device = device;
+        cg_ctx* ctx = NULL;
+        cosmopp_gb300_detail::check(cg_create(&ctx, &cfg), "getFiducialMatrix", cg_last_error(NULL));
+        CMatrix* m = new CMatrix(cg_get_n(ctx));
+        m->comment() = "fiducial matrix";
+        const int rc = cg_fiducial_matrix(ctx, cl.data(), lMax, lMaxMax, NULL, m->data());
+        std::string err = rc ? cg_last_error(ctx) : "";
+        cg_destroy(ctx);
+        if (rc) {
+            delete m;
+            cosmopp_gb300_detail::check(rc, "getFiducialMatrix", err.c_str());
+        }
+        return m;
+    }
     /// source/c_matrix_generator.cpp:774-787 (full sky, noise^2 on the diagonal)
     static CMatrix* generateNoiseMatrix(long nSide, double noise = 1e-3)
     {

@@ -2,7 +2,10 @@
 // C++ drop-in classes: clToCMatrix -> generateNoiseMatrix + maskMatrix ->
 // Likelihood(C, zero fiducial, N, goodPixels, {}) -> calculate(d), then a few
 // HMC-style leapfrog steps on PixelLikelihoodWithDerivs (source/hmc.cpp:78-96).
-// Input (argv[1]): nside lmax fwhm sigma n, goodPixels[n], cl[lmax+1], d[n].
+// Input (argv[1]): nside lmax fwhm sigma n, goodPixels[n], cl[lmax+1], d[n], and
+// optionally lmaxmax clFull[lmaxmax+1]: then the fiducial matrix is
+// getFiducialMatrix(clFull, nside, lmax, fwhm, &goodPixels) as the reference's
+// test builds it (written raw into argv[3]), else zero.
 // Output: the packed C as raw doubles into argv[2], then one line
 // "like chi2 logDet" and "hmc <final -2lnL> <accepted>" on stdout.
 #include <cmath>
@@ -26,6 +29,12 @@ int main(int argc, char** argv)
     std::vector<double> cl(lmax + 1), d(n);
     for (double& c : cl) in >> c;
     for (double& v : d) in >> v;
+    int lmaxmax = 0;
+    std::vector<double> clFull;
+    if (in >> lmaxmax) {
+        clFull.resize(lmaxmax + 1);
+        for (double& c : clFull) in >> c;
+    }
     try {
         CMatrix* c = CMatrixGenerator::clToCMatrix(cl, nside, fwhm, &good);
         {
@@ -34,8 +43,14 @@ int main(int argc, char** argv)
         }
         CMatrix* noise = CMatrixGenerator::generateNoiseMatrix(nside, sigma);
         noise->maskMatrix(good);
-        CMatrix fid(n);
-        Likelihood like(*c, fid, *noise, good, std::vector<double>());
+        CMatrix* fid = clFull.empty() ? new CMatrix(n)
+                                      : CMatrixGenerator::getFiducialMatrix(clFull, nside, lmax, fwhm, &good);
+        if (!clFull.empty() && argc > 3) {
+            std::ofstream out(argv[3], std::ios::binary);
+            out.write((const char*)fid->data(), sizeof(double) * (size_t)n * (n + 1) / 2);
+        }
+        Likelihood like(*c, *fid, *noise, good, std::vector<double>());
+        delete fid;
         double chi2, logDet;
         const double l = like.calculate(d, chi2, logDet);
         std::printf("%.17g %.17g %.17g\n", l, chi2, logDet);

@@ -13,6 +13,9 @@ them through ctypes.  Every number stored below comes from the reference:
   fiducial and a few lognormal-perturbed C_l vectors;
 * central finite differences (step 1e-4 C_l) of the reference's -2lnL, which
   pin the adjoint gradient the reference does not have.
+* getFiducialMatrix (l = lmax+1 .. 4 nside plus the monopole/dipole term) and
+  the full low-l flow Likelihood(C, fiducial, N, goodPixels).calculate(d) of
+  source/test_like_low.cpp:181-193 that uses it.
 
 Usage:  python tests/golden/make_golden.py
 """
@@ -42,6 +45,57 @@ CASES = [
     ("nside8_lmax24", 8, 24, 440.0, 0.8, 1.0, 3, [2, 3, 10, 17, 24], False),
     ("nside16_lmax47", 16, 47, 220.0, 0.8, 1.0, 2, [2, 30, 47], False),
 ]
+
+
+FID_CASES = [
+    # name, nside, lmax, fwhm_arcmin, keep, sigma, store_full
+    ("fid_nside4", 4, 10, 440.0, 0.8, 1.0, True),
+    ("fid_nside8", 8, 24, 440.0, 0.8, 1.0, False),
+]
+
+
+def ref_fiducial(R, cl, nside, lmax, fwhm, nest):
+    n = len(nest)
+    out = np.zeros(n * (n + 1) // 2)
+    rc = R.ref_fiducial_matrix(cl.ctypes.data_as(dp), len(cl), nside, lmax, fwhm, nest.ctypes.data_as(ip), n,
+                               out.ctypes.data_as(dp))
+    assert rc == 0, R.ref_last_error()
+    return out
+
+
+def ref_like_packed(R, c, fid, noise, d):
+    chi2, ld, lk = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    rc = R.ref_likelihood_packed(c.ctypes.data_as(dp), fid.ctypes.data_as(dp), noise.ctypes.data_as(dp), len(d),
+                                 d.ctypes.data_as(dp), None, ctypes.byref(chi2), ctypes.byref(ld), ctypes.byref(lk))
+    assert rc == 0, R.ref_last_error()
+    return chi2.value, ld.value, lk.value
+
+
+def fiducial_cases(R):
+    for name, nside, lmax, fwhm_am, keep, sigma, store_full in FID_CASES:
+        fwhm = fwhm_am / 60.0
+        ring = W.bernoulli_mask(nside, keep, 1234)
+        nest = O.ring2nest(nside, ring)
+        n = len(nest)
+        lmax_max = 4 * nside
+        cl_full = W.fiducial_cl(lmax_max)
+        fid = ref_fiducial(R, cl_full, nside, lmax, fwhm, nest)
+        c = ref_cmatrix(R, cl_full[:lmax + 1].copy(), nside, fwhm, nest)
+        noise = np.zeros_like(c)
+        noise[[j * (j + 1) // 2 + j for j in range(n)]] = sigma ** 2
+        z = np.random.default_rng(0).standard_normal(n)
+        full = W.packed_to_full(c + fid, n) + sigma ** 2 * np.eye(n)
+        d = W.draw_data(full, z)
+        chi2, ld, lk = ref_like_packed(R, c, fid, noise, d)
+        out = dict(nside=nside, lmax=lmax, lmax_max=lmax_max, fwhm_deg=fwhm, sigma=sigma, ring_kept=ring,
+                   nest_good=nest, cl_full=cl_full, d=d, chi2=chi2, logdet_ref=ld, like_ref=lk,
+                   fid_sha256=np.array(hashlib.sha256(fid.tobytes()).hexdigest()),
+                   fid_diag=np.array([fid[j * (j + 1) // 2 + j] for j in range(n)]), fid_head=fid[:4096].copy(),
+                   c_sha256=np.array(hashlib.sha256(c.tobytes()).hexdigest()))
+        if store_full:
+            out["fid_packed"] = fid
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
+        print(name, "n", n, "like", lk, "chi2", chi2)
 
 
 def ref_cmatrix(R, cl, nside, fwhm, nest):
@@ -112,6 +166,7 @@ def main():
             out["c_packed"] = c_fid
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
         print(name, "n", n, "m2lnl", out["m2lnl"][0], "chi2", rows[0, 0])
+    fiducial_cases(R)
 
 
 if __name__ == "__main__":

@@ -50,3 +50,27 @@ def test_reference_flow_through_cxx_dropin(exe, name, tmp_path):
     assert hmc[0] == "hmc"
     # a small step size leapfrog conserves the Hamiltonian to O(tau^2)
     assert abs(float(hmc[2])) < 0.05
+
+
+def test_low_l_flow_with_fiducial_matrix_through_cxx_dropin(exe, tmp_path):
+    """clToCMatrix + getFiducialMatrix + noise -> Likelihood -> calculate, as
+    source/test_like_low.cpp:181-193 runs it."""
+    g = load_golden("fid_nside4")
+    lmax = int(g["lmax"])
+    inp = tmp_path / "in.txt"
+    with open(inp, "w") as f:
+        f.write("%d %d %.17g %.17g %d\n" % (int(g["nside"]), lmax, float(g["fwhm_deg"]), float(g["sigma"]),
+                                            len(g["nest_good"])))
+        f.write(" ".join(str(int(v)) for v in g["nest_good"]) + "\n")
+        f.write(" ".join("%.17g" % v for v in g["cl_full"][:lmax + 1]) + "\n")
+        f.write(" ".join("%.17g" % v for v in g["d"]) + "\n")
+        f.write("%d\n" % int(g["lmax_max"]) + " ".join("%.17g" % v for v in g["cl_full"]) + "\n")
+    cbin, fbin = tmp_path / "c.bin", tmp_path / "fid.bin"
+    p = subprocess.run([exe, str(inp), str(cbin), str(fbin)], capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    assert hashlib.sha256(np.fromfile(cbin, dtype=np.float64).tobytes()).hexdigest() == str(g["c_sha256"])
+    assert np.array_equal(np.fromfile(fbin, dtype=np.float64), g["fid_packed"])
+    like, chi2, logdet = map(float, p.stdout.splitlines()[0].split())
+    assert abs(chi2 - float(g["chi2"])) <= 1e-6
+    assert abs(logdet - float(g["logdet_ref"])) <= 1e-6
+    assert abs(like - float(g["like_ref"])) <= 2e-6

@@ -37,6 +37,35 @@ def test_cmatrix_bit_identical_to_reference(name):
         assert np.array_equal(c, g["c_packed"])
 
 
+@pytest.mark.parametrize("name", ["fid_nside4", "fid_nside8"])
+def test_fiducial_matrix_bit_identical_and_low_l_flow(name):
+    """getFiducialMatrix on the GPU, bit for bit, then Likelihood(C, fiducial, N) as
+    source/test_like_low.cpp:181-193 uses it."""
+    g = load_golden(name)
+    lmax, lmax_max = int(g["lmax"]), int(g["lmax_max"])
+    with cg.Context(lmax=lmax, fwhm_deg=float(g["fwhm_deg"]), nside=int(g["nside"]), good_pixels=g["nest_good"],
+                    scheme="NEST", noise_sigma=float(g["sigma"]), precision="fp64") as ctx:
+        fid = ctx.fiducial_matrix(g["cl_full"], lmax_max)
+        c = ctx.build_cmatrix(g["cl_full"][:lmax + 1])
+        # an explicit beam table gives the same words as the context's Gaussian beam
+        beam = np.array([cg.beam(l, float(g["fwhm_deg"])) for l in range(lmax_max + 1)])
+        assert np.array_equal(ctx.fiducial_matrix(g["cl_full"], lmax_max, beam=beam), fid)
+        with pytest.raises(cg.CGError):
+            ctx.fiducial_matrix(g["cl_full"], lmax)  # lmax_max must exceed lmax
+    assert hashlib.sha256(fid.tobytes()).hexdigest() == str(g["fid_sha256"])
+    assert np.array_equal(fid[:len(g["fid_head"])], g["fid_head"])
+    if "fid_packed" in g:
+        assert np.array_equal(fid, g["fid_packed"])
+    assert hashlib.sha256(c.tobytes()).hexdigest() == str(g["c_sha256"])
+    n = len(g["nest_good"])
+    noise = np.zeros_like(c)
+    idx = np.arange(n)
+    noise[idx * (idx + 1) // 2 + idx] = float(g["sigma"]) ** 2
+    like, chi2, logdet = cg.Likelihood(c, fid, noise, good_pixels=g["nest_good"]).calculate(g["d"])
+    assert abs(chi2 - float(g["chi2"])) <= 1e-6
+    assert abs(like - float(g["like_ref"])) <= 2e-6
+
+
 def test_cmatrix_batched_matches_single(oracle_mod):
     g = load_golden("nside4")
     with _ctx(g) as ctx:

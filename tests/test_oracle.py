@@ -57,6 +57,27 @@ def test_oracle_cmatrix_matches_reference_bitwise(oracle_mod, name):
     assert np.array_equal(xyz, xyz_r)
 
 
+@pytest.mark.parametrize("name", ["fid_nside4", "fid_nside8"])
+def test_oracle_fiducial_matrix_matches_reference_bitwise(oracle_mod, name):
+    """getFiducialMatrix (source/c_matrix_generator.cpp:706-772) and the low-l flow that uses it."""
+    g = load_golden(name)
+    xyz = oracle_mod.unit_vectors(int(g["nside"]), g["nest_good"], "NEST")
+    fid = oracle_mod.fiducial_matrix(g["cl_full"], xyz, int(g["lmax"]), float(g["fwhm_deg"]))
+    assert hashlib.sha256(fid.tobytes()).hexdigest() == str(g["fid_sha256"])
+    if "fid_packed" in g:
+        assert np.array_equal(fid, g["fid_packed"])
+    n = len(g["nest_good"])
+    c = oracle_mod.cl_to_cmatrix(g["cl_full"][:int(g["lmax"]) + 1], xyz, float(g["fwhm_deg"]))
+    assert hashlib.sha256(c.tobytes()).hexdigest() == str(g["c_sha256"])
+    noise = np.zeros_like(c)
+    idx = np.arange(n)
+    noise[idx * (idx + 1) // 2 + idx] = float(g["sigma"]) ** 2
+    like, chi2, ld, _, st = oracle_mod.likelihood(c, noise, g["d"], fid_packed=fid)
+    assert st == 0
+    assert abs(chi2 - float(g["chi2"])) <= 1e-9 * abs(float(g["chi2"]))
+    assert abs((like + DET_OFFSET) - float(g["like_ref"])) <= 1e-8 * abs(float(g["like_ref"]))
+
+
 @pytest.mark.parametrize("name", ["nside1", "nside2", "nside4", "nside8_lmax24"])
 def test_oracle_likelihood_matches_reference(oracle_mod, name):
     g = load_golden(name)
