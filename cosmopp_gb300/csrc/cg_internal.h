@@ -79,6 +79,7 @@ struct MixedWork {
     double* Y = nullptr;         // [nharm_pad][N] real spherical harmonics x B_l at the pixels
     double* Z = nullptr;         // [nharm_pad][N] L_ref^-1 Y
     float* U = nullptr;          // [tiles][TS*TS][lpad] whitened Legendre table
+    float* Zf = nullptr;         // [nharm_pad][N] Z in FP32 (the x^T Ubar x term of the gradient)
     // per batch element
     float* A = nullptr;          // [cap][tiled] I + K_b (kept for the refinement residual)
     float* V = nullptr;          // [cap][tiled] V_b = (I + K_b)^-1
@@ -92,6 +93,7 @@ struct MixedWork {
     double* r = nullptr;         // [cap][N] refinement residual
     double* part = nullptr;      // [cap][tiles][2][TS] matvec partials
     float* gpart = nullptr;      // [tiles][cap][lpad] adjoint partials
+    float* proj = nullptr;       // [cap][nharm_pad] Z^T x_b
     double* ld = nullptr;        // [cap] ln det C_b
     int* st = nullptr;           // [cap]
     int* tcerr = nullptr;        // [1] set when a bounded tensor-core wait gave up

@@ -219,16 +219,19 @@ __global__ void __launch_bounds__(256) contract_fwd(int B, int lp, const float* 
                                                     size_t strideA)
 {
     extern __shared__ float fsm[];
-    float* sU = fsm;             // [lp][128]
-    float* sE = fsm + lp * 128;  // [lp][128]
+    constexpr int LD = 132;      // 128 + 4: 16-byte rows, staging stores spread over 8 banks
+    float* sU = fsm;             // [lp][LD]
+    float* sE = fsm + lp * LD;   // [lp][LD]
     const size_t e_begin = (size_t)blockIdx.x * 128;  // global entry index over all tiles
     const int b_begin = blockIdx.y * 128;
     const float* ublk = U + e_begin * lp;
+    // the 128 x lp block of the table and of eps are contiguous in global memory: read them in
+    // order (coalesced) and transpose into [l][entry] / [l][batch]
     for (int k = threadIdx.x; k < 128 * lp; k += 256) {
-        const int e = k % 128, l = k / 128;  // e fastest: conflict-free smem stores
-        sU[l * 128 + e] = ublk[(size_t)e * lp + l];
+        const int e = k / lp, l = k % lp;
+        sU[l * LD + e] = ublk[k];
         const int bb = b_begin + e;
-        sE[l * 128 + e] = (bb < B) ? eps[(size_t)bb * lp + l] : 0.f;
+        sE[l * LD + e] = (bb < B) ? eps[(size_t)b_begin * lp + k] : 0.f;
     }
     __syncthreads();
     const int te = threadIdx.x % 16, tb = threadIdx.x / 16;
@@ -239,10 +242,10 @@ __global__ void __launch_bounds__(256) contract_fwd(int B, int lp, const float* 
 #pragma unroll
         for (int q = 0; q < 8; ++q) acc[a][q] = 0.f;
     for (int l = 0; l < lp; ++l) {
-        const float4 u0 = *reinterpret_cast<const float4*>(&sU[l * 128 + e0]);
-        const float4 u1 = *reinterpret_cast<const float4*>(&sU[l * 128 + e0 + 4]);
-        const float4 w0 = *reinterpret_cast<const float4*>(&sE[l * 128 + b0]);
-        const float4 w1 = *reinterpret_cast<const float4*>(&sE[l * 128 + b0 + 4]);
+        const float4 u0 = *reinterpret_cast<const float4*>(&sU[l * LD + e0]);
+        const float4 u1 = *reinterpret_cast<const float4*>(&sU[l * LD + e0 + 4]);
+        const float4 w0 = *reinterpret_cast<const float4*>(&sE[l * LD + b0]);
+        const float4 w1 = *reinterpret_cast<const float4*>(&sE[l * LD + b0 + 4]);
         const float u[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
         const float w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
 #pragma unroll
@@ -326,82 +329,157 @@ __global__ void broadcast_vec(int B, int N, const double* __restrict__ y, double
     if (i < N && b < B) yb[(size_t)b * N + i] = y[i];
 }
 
-// Adjoint contraction partials: part[t][b][l] = sum_{e in tile t (lower)} w_e W_b[t][e] Ubar[t][e][l],
-// W_b = V_b - x_b x_b^T; grid (tiles, ceil(B / 64)); thread -> 4 batch x 3 l.
-__global__ void __launch_bounds__(256) contract_adj(int B, int N, int lp, const float* __restrict__ U,
-                                                    const float* __restrict__ V, size_t strideA,
-                                                    const double* __restrict__ x, float* __restrict__ part)
+// Adjoint gradient, d(-2lnL)/dC_l = tr((V - x x^T) Ubar_l) / cref_l, in two parts:
+//   tr(V Ubar_l)   = sum over stored entries e of w_e V[e] Ubar[e][l], w_e = 2 below the
+//                    diagonal, 1 on it, 0 above it (the tiles hold the lower triangle);
+//   x^T Ubar_l x   = cref_l |Z_l^T x|^2, Ubar_l = cref_l Z_l Z_l^T (Z_l: the 2l+1 rows of Z).
+
+// part[t][b][l] = sum_{e in tile t} w_e V_b[t][e] Ubar[t][e][l]: one CTA per tile and 256 batch
+// elements (the tile's table block is read once per 48 l); grid (tiles, ceil(B / 256),
+// ceil(lp / 48)).  Thread (bg = t % 32, lg = t / 32) holds batch elements bg + 32 a (a < 8) and
+// l = lbase + 6 lg .. + 5.  V chunks are staged [b][entry] with row
+// stride ADJ_LD (16-byte rows; the 8 lanes of each 128-bit phase hit different banks).
+constexpr int ADJ_KE = 64;       // entries per chunk
+constexpr int ADJ_LD = ADJ_KE + 4;
+__global__ void __launch_bounds__(256, 2) contract_adj(int B, int lp, const float* __restrict__ U,
+                                                       const float* __restrict__ V, size_t strideA,
+                                                       float* __restrict__ part)
 {
     extern __shared__ float asm_[];
-    float (*sU)[49] = reinterpret_cast<float (*)[49]>(asm_);              // [entry][l], 48 l per pass
-    float (*sW)[65] = reinterpret_cast<float (*)[65]>(asm_ + 64 * 49);    // [b][entry]
-    float (*sxi)[64] = reinterpret_cast<float (*)[64]>(asm_ + 64 * 49 + 64 * 65);
-    float (*sxj)[64] = reinterpret_cast<float (*)[64]>(asm_ + 64 * 49 + 64 * 65 + 64 * 64);  // x_b at rows / cols
-    const int t = blockIdx.x, b_begin = blockIdx.y * 64;
+    float* sV = asm_;                      // [256][ADJ_LD]
+    float* sU = asm_ + 256 * ADJ_LD;       // [ADJ_KE][48]
+    const int t = blockIdx.x, b_begin = blockIdx.y * 256, lbase = 48 * blockIdx.z;
     int I, J;
     tile_coords(t, I, J);
-    for (int k = threadIdx.x; k < 64 * 64; k += 256) {
-        const int bb = k / 64, r = k % 64, b = b_begin + bb;
-        sxi[bb][r] = (b < B) ? (float)x[(size_t)b * N + I * TS + r] : 0.f;
-        sxj[bb][r] = (b < B) ? (float)x[(size_t)b * N + J * TS + r] : 0.f;
-    }
-    const int tb = threadIdx.x / 16, tl = threadIdx.x % 16;  // b0 = 4 tb, l0 = 3 tl
-    for (int lbase = 0; lbase < lp; lbase += 48) {
-        float acc[4][3] = {};
-        for (int e0 = 0; e0 < TILE_ELEMS; e0 += 64) {
-            __syncthreads();
-            for (int k = threadIdx.x; k < 64 * 48; k += 256) {
-                const int e = k / 48, l = k % 48;
-                sU[e][l] = (lbase + l < lp) ? U[((size_t)t * TILE_ELEMS + e0 + e) * lp + lbase + l] : 0.f;
-            }
-            for (int k = threadIdx.x; k < 64 * 64; k += 256) {
-                const int bb = k / 64, e = k % 64, b = b_begin + bb;
-                const int ee = e0 + e, r = ee % TS, c = ee / TS;
-                float w = 0.f;
-                if (b < B && (I != J || r >= c)) {
-                    const float wt = (I == J && r == c) ? 1.f : 2.f;
-                    w = wt * (V[(size_t)b * strideA + (size_t)t * TILE_ELEMS + ee] - sxi[bb][r] * sxj[bb][c]);
+    const int bg = threadIdx.x % 32, lg = threadIdx.x / 32, l0 = 6 * lg;
+    float acc[8][6];
+#pragma unroll
+    for (int a = 0; a < 8; ++a)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) acc[a][q] = 0.f;
+    const float* Ut = U + (size_t)t * TILE_ELEMS * lp;
+    for (int e0 = 0; e0 < TILE_ELEMS; e0 += ADJ_KE) {
+        __syncthreads();
+        // V: 256 rows x 64 entries, 16 threads per row (coalesced), weights applied
+        for (int k = threadIdx.x; k < 256 * (ADJ_KE / 4); k += 256) {
+            const int bb = k / (ADJ_KE / 4), e4 = k % (ADJ_KE / 4), b = b_begin + bb;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (b < B) {
+                v = __ldg(reinterpret_cast<const float4*>(V + (size_t)b * strideA + (size_t)t * TILE_ELEMS + e0 + 4 * e4));
+                float w[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int ee = e0 + 4 * e4 + i, r = ee % TS, c = ee / TS;
+                    w[i] = (I != J || r > c) ? 2.f : (r == c ? 1.f : 0.f);
                 }
-                sW[bb][e] = w;
+                v = make_float4(w[0] * v.x, w[1] * v.y, w[2] * v.z, w[3] * v.w);
             }
-            __syncthreads();
-#pragma unroll 4
-            for (int e = 0; e < 64; ++e) {
-                float u[3], w[4];
+            *reinterpret_cast<float4*>(&sV[bb * ADJ_LD + 4 * e4]) = v;
+        }
+        // table: 64 entries x 48 l
+        for (int k = threadIdx.x; k < ADJ_KE * 12; k += 256) {
+            const int e = k / 12, q4 = k % 12;
+            float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (lbase + 4 * q4 < lp) u = __ldg(reinterpret_cast<const float4*>(Ut + (size_t)(e0 + e) * lp + lbase + 4 * q4));
+            *reinterpret_cast<float4*>(&sU[e * 48 + 4 * q4]) = u;
+        }
+        __syncthreads();
+#pragma unroll 2
+        for (int e4 = 0; e4 < ADJ_KE / 4; ++e4) {
+            float4 v[8];
 #pragma unroll
-                for (int q = 0; q < 3; ++q) u[q] = sU[e][tl * 3 + q];
+            for (int a = 0; a < 8; ++a) v[a] = *reinterpret_cast<const float4*>(&sV[(bg + 32 * a) * ADJ_LD + 4 * e4]);
 #pragma unroll
-                for (int a = 0; a < 4; ++a) w[a] = sW[tb * 4 + a][e];
+            for (int j = 0; j < 4; ++j) {
+                const float* ur = &sU[(4 * e4 + j) * 48 + l0];
+                const float2 u01 = *reinterpret_cast<const float2*>(ur);
+                const float2 u23 = *reinterpret_cast<const float2*>(ur + 2);
+                const float2 u45 = *reinterpret_cast<const float2*>(ur + 4);
+                const float u[6] = {u01.x, u01.y, u23.x, u23.y, u45.x, u45.y};
 #pragma unroll
-                for (int a = 0; a < 4; ++a)
+                for (int a = 0; a < 8; ++a) {
+                    const float va = (j == 0) ? v[a].x : (j == 1) ? v[a].y : (j == 2) ? v[a].z : v[a].w;
 #pragma unroll
-                    for (int q = 0; q < 3; ++q) acc[a][q] = fmaf(w[a], u[q], acc[a][q]);
+                    for (int q = 0; q < 6; ++q) acc[a][q] = fmaf(va, u[q], acc[a][q]);
+                }
             }
         }
+    }
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-            const int b = b_begin + tb * 4 + a;
-            if (b >= B) continue;
+    for (int a = 0; a < 8; ++a) {
+        const int b = b_begin + bg + 32 * a;
+        if (b >= B) continue;
 #pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                const int l = lbase + tl * 3 + q;
-                if (l < lp) part[((size_t)t * B + b) * lp + l] = acc[a][q];
-            }
-        }
+        for (int q = 0; q < 6; ++q)
+            if (lbase + l0 + q < lp) part[((size_t)t * B + b) * lp + lbase + l0 + q] = acc[a][q];
     }
 }
 
-// grad[b][l] = (sum_t part[t][b][l]) / cref_l, FP64 in tile order; grid B
-__global__ void adj_finish(int B, int ntile, int lmax, int lp, const float* __restrict__ part,
-                           const double* __restrict__ cref, double* __restrict__ grad)
+// proj[b][h] = sum_i Z[h][i] x_b[i] (FP32); 64 x 64 output per CTA, 4 x 4 per thread;
+// grid (nharm_pad / 64, ceil(B / 64))
+__global__ void __launch_bounds__(256) project_x(int B, int N, int nhp, const float* __restrict__ Zf,
+                                                 const double* __restrict__ x, float* __restrict__ proj)
+{
+    __shared__ float sx[64][33], sz[64][33];
+    const int h_begin = blockIdx.x * 64, b_begin = blockIdx.y * 64;
+    const int th = threadIdx.x % 16, tb = threadIdx.x / 16;
+    float acc[4][4] = {};
+    for (int k0 = 0; k0 < N; k0 += 32) {
+        __syncthreads();
+        for (int k = threadIdx.x; k < 64 * 32; k += 256) {
+            const int row = k / 32, kk = k % 32, b = b_begin + row;
+            sx[row][kk] = (b < B && k0 + kk < N) ? (float)x[(size_t)b * N + k0 + kk] : 0.f;
+            sz[row][kk] = (k0 + kk < N) ? Zf[(size_t)(h_begin + row) * N + k0 + kk] : 0.f;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int kk = 0; kk < 32; ++kk) {
+            float xv[4], zv[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) { xv[i] = sx[tb + 16 * i][kk]; zv[i] = sz[th + 16 * i][kk]; }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+                for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(xv[i], zv[j], acc[i][j]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const int b = b_begin + tb + 16 * i;
+        if (b >= B) continue;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) proj[(size_t)b * nhp + h_begin + th + 16 * j] = acc[i][j];
+    }
+}
+
+// grad[b][l] = (sum_t part[t][b][l]) / cref_l - sum_{h in l} proj[b][h]^2, FP64 sums in a fixed
+// order; rows of Z for l are h = l^2 - 4 .. l^2 + 2l - 4; grid B
+__global__ void adj_finish(int B, int ntile, int lmax, int lp, int nhp, const float* __restrict__ part,
+                           const float* __restrict__ proj, const double* __restrict__ cref,
+                           double* __restrict__ grad)
 {
     const int b = blockIdx.x;
     for (int l = threadIdx.x; l <= lmax; l += blockDim.x) {
-        double s = 0.0;
-        if (l >= 2)
+        double g = 0.0;
+        if (l >= 2) {
+            double s = 0.0;
             for (int t = 0; t < ntile; ++t) s += (double)part[((size_t)t * B + b) * lp + l];
-        grad[(size_t)b * (lmax + 1) + l] = (l >= 2) ? s / cref[l] : 0.0;
+            double xx = 0.0;
+            for (int h = l * l - 4; h < (l + 1) * (l + 1) - 4; ++h) {
+                const double p = (double)proj[(size_t)b * nhp + h];
+                xx += p * p;
+            }
+            g = s / cref[l] - xx;
+        }
+        grad[(size_t)b * (lmax + 1) + l] = g;
     }
+}
+
+// Z in FP32
+__global__ void to_f32(size_t n, const double* __restrict__ src, float* __restrict__ dst)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        dst[i] = (float)src[i];
 }
 
 template <typename T>
@@ -424,7 +502,7 @@ void mixed_free(cg_ctx* ctx)
     cudaFree(w.Lref); cudaFree(w.Mref); cudaFree(w.Dinv_ref); cudaFree(w.diag_ref); cudaFree(w.Y); cudaFree(w.Z);
     cudaFree(w.U); cudaFree(w.A); cudaFree(w.Ms); cudaFree(w.Linv); cudaFree(w.diag); cudaFree(w.eps); cudaFree(w.y);
     cudaFree(w.x); cudaFree(w.r); cudaFree(w.gpart); cudaFree(w.st); cudaFree(w.V); cudaFree(w.Ls); cudaFree(w.cref);
-    cudaFree(w.ldref); cudaFree(w.part); cudaFree(w.ld); cudaFree(w.tcerr);
+    cudaFree(w.ldref); cudaFree(w.part); cudaFree(w.ld); cudaFree(w.tcerr); cudaFree(w.Zf); cudaFree(w.proj);
     w = MixedWork();
 }
 
@@ -441,6 +519,7 @@ static int ensure_ref_bufs(cg_ctx* ctx)
     if (!rc) rc = dalloc(ctx, &w.Y, (size_t)nhp * N);
     if (!rc) rc = dalloc(ctx, &w.Z, (size_t)nhp * N);
     if (!rc) rc = dalloc(ctx, &w.U, tiled * lp);
+    if (!rc) rc = dalloc(ctx, &w.Zf, (size_t)nhp * N);
     if (!rc) rc = dalloc(ctx, &w.cref, (size_t)ctx->lmax + 1);
     if (!rc) rc = dalloc(ctx, &w.ldref, 1);
     if (!rc) rc = dalloc(ctx, &w.tcerr, 1);
@@ -456,7 +535,8 @@ static int ensure_batch_bufs(cg_ctx* ctx, int B)
     if (w.cap >= B) return CG_OK;
     cudaFree(w.A); cudaFree(w.V); cudaFree(w.Ls); cudaFree(w.Ms); cudaFree(w.Linv); cudaFree(w.diag); cudaFree(w.eps);
     cudaFree(w.y); cudaFree(w.x); cudaFree(w.r); cudaFree(w.part); cudaFree(w.gpart); cudaFree(w.st); cudaFree(w.ld);
-    w.A = w.V = w.Ls = w.Ms = w.Linv = w.diag = w.eps = w.gpart = nullptr;
+    cudaFree(w.proj);
+    w.A = w.V = w.Ls = w.Ms = w.Linv = w.diag = w.eps = w.gpart = w.proj = nullptr;
     w.y = w.x = w.r = w.part = w.ld = nullptr;
     w.st = nullptr;
     w.cap = 0;
@@ -474,6 +554,7 @@ static int ensure_batch_bufs(cg_ctx* ctx, int B)
     if (!rc) rc = dalloc(ctx, &w.r, (size_t)B * N);
     if (!rc) rc = dalloc(ctx, &w.part, (size_t)B * ntile * 2 * TS);
     if (!rc) rc = dalloc(ctx, &w.gpart, (size_t)ntile * B * lp);
+    if (!rc) rc = dalloc(ctx, &w.proj, (size_t)B * nharm_pad(ctx->lmax));
     if (!rc) rc = dalloc(ctx, &w.st, (size_t)B);
     if (!rc) rc = dalloc(ctx, &w.ld, (size_t)B);
     if (rc) return rc;
@@ -516,6 +597,7 @@ int mixed_prepare_reference(cg_ctx* ctx, const double* cl_ref_host)
         const size_t smz = 2 * (size_t)TS * SmemLd<double>::v * sizeof(double);
         cudaFuncSetAttribute(whiten_basis, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
         whiten_basis<<<dim3(nt, nhp / TS), 256, smz, s>>>(nt, N, w.Mref, w.Y, w.Z);
+        to_f32<<<1024, 256, 0, s>>>((size_t)nhp * N, w.Z, w.Zf);
         if (lp <= 48) {
             constexpr int CC = 8;
             const size_t smu = sizeof(double) * 32 * (TS + CC) + sizeof(float) * (size_t)CC * TS * lp;
@@ -604,7 +686,7 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
     }
     // A_b = I + sum_l eps_bl Ubar_l
     {
-        const size_t smem = sizeof(float) * 2 * 128 * lp;
+        const size_t smem = sizeof(float) * 2 * 132 * lp;
         cudaFuncSetAttribute(contract_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         contract_fwd<<<dim3((unsigned)(tiled / 128), (B + 127) / 128), 256, smem, s>>>(B, lp, w.U, w.eps, w.A,
                                                                                         tiled);
@@ -629,11 +711,13 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
     count_launch(ctx, 7);
     stage_mark(ctx, ST_ADJOINT, s);
     if (d_grad) {
-        const size_t sma = sizeof(float) * (64 * 49 + 64 * 65 + 2 * 64 * 64);
+        const size_t sma = sizeof(float) * (256 * ADJ_LD + ADJ_KE * 48);
         cudaFuncSetAttribute(contract_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma);
-        contract_adj<<<dim3(ntile, (B + 63) / 64), 256, sma, s>>>(B, N, lp, w.U, w.V, tiled, w.x, w.gpart);
-        adj_finish<<<B, 64, 0, s>>>(B, ntile, lmax, lp, w.gpart, w.cref, d_grad);
-        count_launch(ctx, 2);
+        contract_adj<<<dim3(ntile, (B + 255) / 256, (lp + 47) / 48), 256, sma, s>>>(B, lp, w.U, w.V, tiled, w.gpart);
+        const int nhp = nharm_pad(lmax);
+        project_x<<<dim3(nhp / 64, (B + 63) / 64), 256, 0, s>>>(B, N, nhp, w.Zf, w.x, w.proj);
+        adj_finish<<<B, 64, 0, s>>>(B, ntile, lmax, lp, nhp, w.gpart, w.proj, w.cref, d_grad);
+        count_launch(ctx, 3);
     }
     merge_tc_status<<<(B + 127) / 128, 128, 0, s>>>(B, w.tcerr, w.st);
     count_launch(ctx);

@@ -330,80 +330,110 @@ __device__ __forceinline__ void store_block(const float (&R)[64], float* base, i
 }
 
 // Cholesky of the 128x128 block in s (column-major, leading dimension 129, lower part used)
-// and the inverse of its factor into inv (same layout); all NTH threads.  Panels of 8 columns
-// factorised column by column, then one rank-8 update of the trailing block.  The inverse is
-// block-recursive: inv11 = L11^-1, inv22 = L22^-1 (in parallel), inv21 = -inv22 (L21 inv11),
-// with tmp a 64x65 scratch block.  Sets *bad on a non-positive pivot.
+// and the inverse of its factor into inv (same layout, zero above the diagonal); all NTH
+// threads take part (every __syncthreads is reached by all).  Sets *bad on a non-positive pivot.
+//
+// Factorisation: panels of 8 columns.  The updates from factorised columns are summed in
+// u (inv's storage) and subtracted from a column once, when it is reached: subtracting each
+// term from s directly drops the terms below half an ulp of the diagonal (about 1 after
+// whitening) and biases the log-determinant upwards.  Within a panel, thread t < 128 owns row
+// t; for column c every thread recomputes the pivot and the panel's column-c values from s and
+// u (same operands, same rounding as the owner's), so one barrier per column suffices, and the
+// finished column stays in registers until the panel ends.  Then one rank-8 update of the
+// trailing sums, register-blocked (4 rows x 1 column per thread and step).
+// Inverse: each thread t < 128 forward-substitutes column t of L^-1 in row blocks of 8, using
+// 1 / L_cc kept from the factorisation; columns are independent, so no barriers.
 __device__ void factor_block128(float* s, float* inv, float* tmp, int* bad)
 {
     constexpr int L = 129;
     const int t = threadIdx.x;
-    // Trailing updates are summed in u (inv's storage, free until the inverse) and subtracted
-    // once per column: subtracting each term from s directly drops the terms below half an
-    // ulp of the diagonal (about 1 after whitening) and biases the log-determinant upwards.
     float* u = inv;
+    float* rdg = tmp;  // 1 / L_cc, [128]
     for (int e = t; e < 128 * 128; e += NTH) u[(e / 128) * L + e % 128] = 0.f;
     __syncthreads();
     for (int kb = 0; kb < 128; kb += 8) {
-        for (int c = kb; c < kb + 8; ++c) {
+        float lreg[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            const int c = kb + j;
+            float v = s[c * L + c] - u[c * L + c];
+            const bool pos = v > 0.f;  // false also for NaN
+            if (!pos) v = 1.f;
+            const float piv = sqrtf(v);
+            const float rinv = 1.f / piv;
             if (t == 0) {
-                float v = s[c * L + c] - u[c * L + c];
-                if (!(v > 0.f)) { *bad = 1; v = 1.f; }
-                s[c * L + c] = sqrtf(v);
+                rdg[c] = rinv;
+                if (!pos) *bad = 1;
             }
-            __syncthreads();
-            const float piv = s[c * L + c];
-            if (t > c && t < 128) s[c * L + t] = (s[c * L + t] - u[c * L + t]) / piv;
-            __syncthreads();
-            const int nq = kb + 7 - c;  // remaining panel columns c+1 .. kb+7
-            for (int e = t; e < nq * 128; e += NTH) {
-                const int q = c + 1 + e / 128, rr = e % 128;
-                if (rr >= q) u[q * L + rr] += s[c * L + rr] * s[c * L + q];
+            lreg[j] = 0.f;
+            if (t < 128 && t >= c) {
+                const float l = (t == c) ? piv : (s[c * L + t] - u[c * L + t]) * rinv;
+                lreg[j] = l;
+#pragma unroll
+                for (int q2 = j + 1; q2 < 8; ++q2) {
+                    const int q = kb + q2;
+                    if (t >= q) {
+                        const float lq = (s[c * L + q] - u[c * L + q]) * rinv;
+                        u[q * L + t] = fmaf(l, lq, u[q * L + t]);
+                    }
+                }
             }
             __syncthreads();
         }
-        const int q0 = kb + 8;
-        for (int e = t; e < (128 - q0) * 128; e += NTH) {
-            const int q = q0 + e / 128, rr = e % 128;
-            if (rr < q) continue;
-            float acc = u[q * L + rr];
+        if (t < 128) {
 #pragma unroll
-            for (int c = 0; c < 8; ++c) acc += s[(kb + c) * L + rr] * s[(kb + c) * L + q];
-            u[q * L + rr] = acc;
+            for (int j = 0; j < 8; ++j)
+                if (t >= kb + j) s[(kb + j) * L + t] = lreg[j];
+        }
+        __syncthreads();
+        // u[q][r] += sum_j L[r][kb+j] L[q][kb+j] for kb + 8 <= q <= r < 128: warp w takes columns
+        // q = kb + 8 + w, + NTH/32, ...; lane takes rows lane + 32 i
+        const int warp = t / 32, lane = t % 32;
+        for (int q = kb + 8 + warp; q < 128; q += NTH / 32) {
+            float lq[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) lq[j] = s[(kb + j) * L + q];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int r = lane + 32 * i;
+                if (r >= q) {
+                    float acc = u[q * L + r];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) acc = fmaf(s[(kb + j) * L + r], lq[j], acc);
+                    u[q * L + r] = acc;
+                }
+            }
         }
         __syncthreads();
     }
-    // diagonal 64-blocks: thread t < 64 -> column t of L11^-1, 128 <= t < 192 -> column t-128 of L22^-1
-    if (t < 64 || (t >= 128 && t < 192)) {
-        const int off = (t < 64) ? 0 : 64;
-        const int col = off + (t % 64);
-        for (int r = off; r < off + 64; ++r) {
-            if (r < col) { inv[col * L + r] = 0.f; continue; }
-            float acc = (r == col) ? 1.f : 0.f;
-            for (int m = col; m < r; ++m) acc -= s[m * L + r] * inv[col * L + m];
-            inv[col * L + r] = acc / s[r * L + r];
+    // inverse: column c = t of X = L^-1; X[m][c] = 0 for m < c
+    if (t < 128) {
+        const int c = t;
+        for (int m = 0; m < c; ++m) inv[c * L + m] = 0.f;
+        for (int R = c / 8; R < 16; ++R) {
+            const int r0 = 8 * R;
+            float acc[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) acc[i] = (r0 + i == c) ? 1.f : 0.f;
+            for (int m = c; m < r0; ++m) {
+                const float x = inv[c * L + m];
+#pragma unroll
+                for (int i = 0; i < 8; ++i) acc[i] = fmaf(-s[m * L + r0 + i], x, acc[i]);
+            }
+            float y[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                float v = acc[i];
+#pragma unroll
+                for (int k = 0; k < i; ++k) v = fmaf(-s[(r0 + k) * L + r0 + i], y[k], v);
+                y[i] = (r0 + i < c) ? 0.f : v * rdg[r0 + i];
+            }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) inv[c * L + r0 + i] = y[i];
         }
     }
     __syncthreads();
-    // tmp = L21 inv11 (rows 64..127, cols 0..63 of L times inv11)
-    for (int e = t; e < 64 * 64; e += NTH) {
-        const int rr = e % 64, cc = e / 64;
-        float acc = 0.f;
-        for (int m = cc; m < 64; ++m) acc += s[m * L + 64 + rr] * inv[cc * L + m];
-        tmp[cc * 65 + rr] = acc;
-    }
-    __syncthreads();
-    // inv21 = -inv22 tmp; inv12 = 0
-    for (int e = t; e < 64 * 64; e += NTH) {
-        const int rr = e % 64, cc = e / 64;
-        float acc = 0.f;
-        for (int m = 0; m <= rr; ++m) acc += inv[(64 + m) * L + 64 + rr] * tmp[cc * 65 + m];
-        inv[cc * L + 64 + rr] = -acc;
-        inv[(64 + cc) * L + rr] = 0.f;
-    }
-    __syncthreads();
 }
-
 
 // Left-looking Cholesky, column block J2, row block I2 = J2 + blockIdx.x; grid (nt2 - J2, B).
 // Off-diagonal blocks: S_IJ = A_IJ - sum_{k < 2 J2} L_I,k L_J,k^T into the L storage (SC).
