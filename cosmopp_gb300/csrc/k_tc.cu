@@ -333,88 +333,98 @@ __device__ __forceinline__ void store_block(const float (&R)[64], float* base, i
 // and the inverse of its factor into inv (same layout, zero above the diagonal); all NTH
 // threads take part (every __syncthreads is reached by all).  Sets *bad on a non-positive pivot.
 //
-// Factorisation: panels of 8 columns.  The updates from factorised columns are summed in
-// u (inv's storage) and subtracted from a column once, when it is reached: subtracting each
-// term from s directly drops the terms below half an ulp of the diagonal (about 1 after
-// whitening) and biases the log-determinant upwards.  Within a panel, thread t < 128 owns row
-// t; for column c every thread recomputes the pivot and the panel's column-c values from s and
-// u (same operands, same rounding as the owner's), so one barrier per column suffices, and the
-// finished column stays in registers until the panel ends.  Then one rank-8 update of the
-// trailing sums, register-blocked (4 rows x 1 column per thread and step).
-// Inverse: each thread t < 128 forward-substitutes column t of L^-1 in row blocks of 8, using
-// 1 / L_cc kept from the factorisation; columns are independent, so no barriers.
+// Factorisation, panels of 8 columns.  The updates from factorised panels are summed in u
+// (inv's storage) and subtracted from a column once, when its panel is reached: subtracting
+// each term from s directly drops the terms below half an ulp of the diagonal (about 1 after
+// whitening) and biases the log-determinant upwards.  Per panel, every thread factors the
+// panel's 8x8 diagonal block itself (same operands and operation order in every thread, so the
+// same values) and then its own row's 8 values, so a panel needs no barrier until its
+// columns are written.  The trailing sums are then updated from those rows in registers,
+// two threads per row.
+// Inverse: L11^-1 and L22^-1 (64x64 halves) by per-column forward substitution, one thread
+// per column, both halves at once; then T = L21 L11^-1 and L21' = -L22^-1 T as register-
+// blocked 64x64 products (4x4 outputs per thread).
 __device__ void factor_block128(float* s, float* inv, float* tmp, int* bad)
 {
     constexpr int L = 129;
     const int t = threadIdx.x;
     float* u = inv;
-    float* rdg = tmp;  // 1 / L_cc, [128]
     for (int e = t; e < 128 * 128; e += NTH) u[(e / 128) * L + e % 128] = 0.f;
     __syncthreads();
+    const int r = t % 128, part = t / 128;  // threads t >= 256 only reach the barriers
     for (int kb = 0; kb < 128; kb += 8) {
-        float lreg[8];
+        float lb[8][8], rv[8], lr[8];
+        // the panel's 8x8 diagonal block, in every thread
 #pragma unroll
-        for (int j = 0; j < 8; ++j) {
-            const int c = kb + j;
-            float v = s[c * L + c] - u[c * L + c];
-            const bool pos = v > 0.f;  // false also for NaN
-            if (!pos) v = 1.f;
-            const float piv = sqrtf(v);
-            const float rinv = 1.f / piv;
-            if (t == 0) {
-                rdg[c] = rinv;
-                if (!pos) *bad = 1;
-            }
-            lreg[j] = 0.f;
-            if (t < 128 && t >= c) {
-                const float l = (t == c) ? piv : (s[c * L + t] - u[c * L + t]) * rinv;
-                lreg[j] = l;
+        for (int i = 0; i < 8; ++i) {
 #pragma unroll
-                for (int q2 = j + 1; q2 < 8; ++q2) {
-                    const int q = kb + q2;
-                    if (t >= q) {
-                        const float lq = (s[c * L + q] - u[c * L + q]) * rinv;
-                        u[q * L + t] = fmaf(l, lq, u[q * L + t]);
+            for (int j = 0; j <= i; ++j) {
+                const float a = s[(kb + j) * L + kb + i] - u[(kb + j) * L + kb + i];
+                float acc = 0.f;
+#pragma unroll
+                for (int k = 0; k < j; ++k) acc = fmaf(lb[i][k], lb[j][k], acc);
+                if (j < i) {
+                    lb[i][j] = (a - acc) * rv[j];
+                } else {
+                    float v = a - acc;
+                    if (!(v > 0.f)) {  // not positive definite (or NaN): flag, go on with a benign pivot
+                        if (t == 0) *bad = 1;
+                        v = 1.f;
                     }
+                    lb[i][i] = sqrtf(v);
+                    rv[i] = 1.f / lb[i][i];
                 }
             }
-            __syncthreads();
         }
+        // this thread's row r: below the block from its own column entries, inside it from lb
+#pragma unroll
+        for (int j = 0; j < 8; ++j) lr[j] = 0.f;
+        if (r >= kb + 8) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                float acc = 0.f;
+#pragma unroll
+                for (int k = 0; k < j; ++k) acc = fmaf(lr[k], lb[j][k], acc);
+                lr[j] = ((s[(kb + j) * L + r] - u[(kb + j) * L + r]) - acc) * rv[j];
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 8; ++i)
+                if (r == kb + i) {
+#pragma unroll
+                    for (int j = 0; j <= i; ++j) lr[j] = lb[i][j];
+                }
+        }
+        __syncthreads();  // every read of the panel's columns is done
         if (t < 128) {
 #pragma unroll
             for (int j = 0; j < 8; ++j)
-                if (t >= kb + j) s[(kb + j) * L + t] = lreg[j];
+                if (r >= kb + j) s[(kb + j) * L + r] = lr[j];
         }
         __syncthreads();
-        // u[q][r] += sum_j L[r][kb+j] L[q][kb+j] for kb + 8 <= q <= r < 128: warp w takes columns
-        // q = kb + 8 + w, + NTH/32, ...; lane takes rows lane + 32 i
-        const int warp = t / 32, lane = t % 32;
-        for (int q = kb + 8 + warp; q < 128; q += NTH / 32) {
-            float lq[8];
+        // u[q][r] += sum_j L[r][kb+j] L[q][kb+j] for kb + 8 <= q <= r; q of this thread's parity
+        if (t < 256 && r >= kb + 8) {
+            for (int q = kb + 8 + part; q <= r; q += 2) {
+                float acc = u[q * L + r];
 #pragma unroll
-            for (int j = 0; j < 8; ++j) lq[j] = s[(kb + j) * L + q];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const int r = lane + 32 * i;
-                if (r >= q) {
-                    float acc = u[q * L + r];
-#pragma unroll
-                    for (int j = 0; j < 8; ++j) acc = fmaf(s[(kb + j) * L + r], lq[j], acc);
-                    u[q * L + r] = acc;
-                }
+                for (int j = 0; j < 8; ++j) acc = fmaf(lr[j], s[(kb + j) * L + q], acc);
+                u[q * L + r] = acc;
             }
         }
         __syncthreads();
     }
-    // inverse: column c = t of X = L^-1; X[m][c] = 0 for m < c
+    // L11^-1 (t < 64) and L22^-1 (64 <= t < 128): column c of the half at offset o, by row blocks
+    // of 8; 1 / L_cc recomputed from the stored diagonal
     if (t < 128) {
-        const int c = t;
-        for (int m = 0; m < c; ++m) inv[c * L + m] = 0.f;
-        for (int R = c / 8; R < 16; ++R) {
-            const int r0 = 8 * R;
+        const int o = (t < 64) ? 0 : 64, c = o + t % 64;
+        for (int m = 0; m < 128; ++m)
+            if (m < c || m >= o + 64) inv[c * L + m] = 0.f;
+        for (int R = (c - o) / 8; R < 8; ++R) {
+            const int r0 = o + 8 * R;
             float acc[8];
 #pragma unroll
             for (int i = 0; i < 8; ++i) acc[i] = (r0 + i == c) ? 1.f : 0.f;
+#pragma unroll 2
             for (int m = c; m < r0; ++m) {
                 const float x = inv[c * L + m];
 #pragma unroll
@@ -426,27 +436,82 @@ __device__ void factor_block128(float* s, float* inv, float* tmp, int* bad)
                 float v = acc[i];
 #pragma unroll
                 for (int k = 0; k < i; ++k) v = fmaf(-s[(r0 + k) * L + r0 + i], y[k], v);
-                y[i] = (r0 + i < c) ? 0.f : v * rdg[r0 + i];
+                y[i] = (r0 + i < c) ? 0.f : v / s[(r0 + i) * L + r0 + i];
             }
 #pragma unroll
             for (int i = 0; i < 8; ++i) inv[c * L + r0 + i] = y[i];
         }
     }
     __syncthreads();
+    // T = L21 L11^-1 into tmp (tmp[j * 65 + i] = T[i][j]); thread: rows i0.., columns j0..
+    const int i0 = 4 * (t % 16), j0 = 4 * ((t / 16) % 16);
+    if (t < 256) {
+        float acc[4][4] = {};
+        for (int k = j0; k < 64; ++k) {  // L11^-1[k][j] = 0 for k < j
+            float a4[4], b4[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                a4[q] = s[k * L + 64 + i0 + q];
+                b4[q] = inv[(j0 + q) * L + k];
+            }
+#pragma unroll
+            for (int p = 0; p < 4; ++p)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[p][q] = fmaf(a4[p], b4[q], acc[p][q]);
+        }
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) tmp[(j0 + q) * 65 + i0 + p] = acc[p][q];
+    }
+    __syncthreads();
+    // L21' = -L22^-1 T into inv rows 64..127, columns 0..63; the upper-right block stays zero
+    if (t < 256) {
+        float acc[4][4] = {};
+        for (int k = 0; k <= i0 + 3; ++k) {  // L22^-1[i][k] = 0 for k > i
+            float a4[4], b4[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                a4[q] = inv[(64 + k) * L + 64 + i0 + q];
+                b4[q] = tmp[(j0 + q) * 65 + k];
+            }
+#pragma unroll
+            for (int p = 0; p < 4; ++p)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[p][q] = fmaf(a4[p], b4[q], acc[p][q]);
+        }
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) inv[(j0 + q) * L + 64 + i0 + p] = -acc[p][q];
+    }
+    __syncthreads();
 }
 
-// Left-looking Cholesky, column block J2, row block I2 = J2 + blockIdx.x; grid (nt2 - J2, B).
+// Left-looking Cholesky, column block J2; 1-D grid of B (nt2 - J2) CTAs.  The first B are the
+// diagonal blocks (one per batch element), which also factorise, so they start first and their
+// factorisation overlaps the off-diagonal CTAs; those follow batch-major (CTAs of one batch
+// element run together and share its L_J panel in L2).
 // Off-diagonal blocks: S_IJ = A_IJ - sum_{k < 2 J2} L_I,k L_J,k^T into the L storage (SC).
 // Diagonal block: S_JJ factorised, L_JJ into the L storage, its inverse into Linv and, transposed,
 // into the M storage, its diagonal into diag.
-__global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, const float* __restrict__ A,
+__global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, const float* __restrict__ A,
                                                       float* __restrict__ Ls, float* __restrict__ Linv,
                                                       float* __restrict__ Ms, float* __restrict__ diag,
                                                       int* __restrict__ status, int* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ TcCtl ctl;
-    const int I2 = J2 + blockIdx.x, b = blockIdx.y, nt2 = nt / 2;
+    const int nt2 = nt / 2, noff = nt2 - J2 - 1;
+    int I2, b;
+    if ((int)blockIdx.x < B) {
+        I2 = J2;
+        b = blockIdx.x;
+    } else {
+        const int k = blockIdx.x - B;
+        b = k / noff;
+        I2 = J2 + 1 + k % noff;
+    }
     const size_t ntile = (size_t)ntiles_lower(nt);
     const float* Ab = A + (size_t)b * ntile * TILE_ELEMS;
     float* Lb = Ls + (size_t)b * ntile * SC_TILE;
@@ -650,7 +715,7 @@ int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, flo
     if ((rc = set_smem(ctx, chol_tc_update)) || (rc = set_smem(ctx, chol_tc_panel))) return rc;
     const int nt2 = nt / 2;
     for (int J2 = 0; J2 < nt2; ++J2) {
-        chol_tc_update<<<dim3(nt2 - J2, B), NTH, tc_smem(), s>>>(J2, nt, A, Ls, Linv, Ms, diag, status, d_err);
+        chol_tc_update<<<B * (nt2 - J2), NTH, tc_smem(), s>>>(J2, nt, B, A, Ls, Linv, Ms, diag, status, d_err);
         count_launch(ctx);
         if (J2 + 1 < nt2) {
             chol_tc_panel<<<dim3(nt2 - J2 - 1, B), NTH, tc_smem(), s>>>(J2, nt, Ls, Linv, d_err);
