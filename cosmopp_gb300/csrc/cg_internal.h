@@ -85,6 +85,8 @@ struct MixedWork {
     float* V = nullptr;          // [cap][tiled] V_b = (I + K_b)^-1
     float* Ls = nullptr;         // [cap][tc_split_elems] L_b, split canonical storage
     float* Ms = nullptr;         // [cap][tc_split_elems] (L_b^-1)^T blocks, split canonical storage
+    float* Lc = nullptr;         // [cap][tc_c1_elems] L_b (and S before the panel solve), FP32 canonical
+    float* Mc = nullptr;         // [cap][tc_c1_elems] (L_b^-1)^T blocks, FP32 canonical
     float* Linv = nullptr;       // [cap][tc_linv_elems] inverses of the 128x128 diagonal blocks of L_b
     float* diag = nullptr;       // [cap][N]
     float* eps = nullptr;        // [cap][lpad] C_l / Cref_l - 1
@@ -174,12 +176,13 @@ template <typename T>
 int tiled_lauum(cg_ctx* ctx, int B, int nt, const T* M, T* V, size_t strideA, cudaStream_t s);
 // tensor-core FP32 (3xTF32) versions (k_tc.cu); d_err is set if a bounded wait gave up
 // tensor-core FP32 kernels (k_tc.cu): L, M^T and Linv in the split canonical storage
-size_t tc_split_elems(int nt);   // floats per matrix of the L / M^T storage
+size_t tc_split_elems(int nt);   // floats per matrix of the split (hi/lo) L / M^T storage
+size_t tc_c1_elems(int nt);      // floats per matrix of the FP32 canonical L / M^T copies
 size_t tc_linv_elems(int nt);    // floats per matrix of the Linv blocks
-int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, float* Linv, float* Ms, float* diag,
-                      int* status, int* d_err, cudaStream_t s);
-int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* Ls, const float* Linv, float* Ms, int* d_err,
-                   cudaStream_t s);
+int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, float* Lc, float* Linv, float* Ms,
+                      float* Mc, float* diag, int* status, int* d_err, cudaStream_t s);
+int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* Ls, const float* Linv, float* Ms, float* Mc,
+                   int* d_err, cudaStream_t s);
 int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, float* V, int* d_err, cudaStream_t s);
 // mixed path (k_mixed.cu)
 int mixed_prepare_reference(cg_ctx* ctx, const double* cl_ref_host);

@@ -503,6 +503,7 @@ void mixed_free(cg_ctx* ctx)
     cudaFree(w.U); cudaFree(w.A); cudaFree(w.Ms); cudaFree(w.Linv); cudaFree(w.diag); cudaFree(w.eps); cudaFree(w.y);
     cudaFree(w.x); cudaFree(w.r); cudaFree(w.gpart); cudaFree(w.st); cudaFree(w.V); cudaFree(w.Ls); cudaFree(w.cref);
     cudaFree(w.ldref); cudaFree(w.part); cudaFree(w.ld); cudaFree(w.tcerr); cudaFree(w.Zf); cudaFree(w.proj);
+    cudaFree(w.Lc); cudaFree(w.Mc);
     w = MixedWork();
 }
 
@@ -535,8 +536,8 @@ static int ensure_batch_bufs(cg_ctx* ctx, int B)
     if (w.cap >= B) return CG_OK;
     cudaFree(w.A); cudaFree(w.V); cudaFree(w.Ls); cudaFree(w.Ms); cudaFree(w.Linv); cudaFree(w.diag); cudaFree(w.eps);
     cudaFree(w.y); cudaFree(w.x); cudaFree(w.r); cudaFree(w.part); cudaFree(w.gpart); cudaFree(w.st); cudaFree(w.ld);
-    cudaFree(w.proj);
-    w.A = w.V = w.Ls = w.Ms = w.Linv = w.diag = w.eps = w.gpart = w.proj = nullptr;
+    cudaFree(w.proj); cudaFree(w.Lc); cudaFree(w.Mc);
+    w.A = w.V = w.Ls = w.Ms = w.Linv = w.diag = w.eps = w.gpart = w.proj = w.Lc = w.Mc = nullptr;
     w.y = w.x = w.r = w.part = w.ld = nullptr;
     w.st = nullptr;
     w.cap = 0;
@@ -547,6 +548,8 @@ static int ensure_batch_bufs(cg_ctx* ctx, int B)
     if (!rc) rc = dalloc(ctx, &w.Ls, tc_split_elems(nt) * B);
     if (!rc) rc = dalloc(ctx, &w.Ms, tc_split_elems(nt) * B);
     if (!rc) rc = dalloc(ctx, &w.Linv, tc_linv_elems(nt) * B);
+    if (!rc) rc = dalloc(ctx, &w.Lc, tc_c1_elems(nt) * B);
+    if (!rc) rc = dalloc(ctx, &w.Mc, tc_c1_elems(nt) * B);
     if (!rc) rc = dalloc(ctx, &w.diag, (size_t)B * N);
     if (!rc) rc = dalloc(ctx, &w.eps, (size_t)B * lp);
     if (!rc) rc = dalloc(ctx, &w.y, (size_t)B * N);
@@ -692,11 +695,11 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
                                                                                         tiled);
     }
     stage_mark(ctx, ST_CHOL, s);
-    if ((rc = tiled_cholesky_tc(ctx, B, nt, w.A, w.Ls, w.Linv, w.Ms, w.diag, w.st, w.tcerr, s))) return rc;
+    if ((rc = tiled_cholesky_tc(ctx, B, nt, w.A, w.Ls, w.Lc, w.Linv, w.Ms, w.Mc, w.diag, w.st, w.tcerr, s))) return rc;
     logdet_mixed<<<B, 256, 0, s>>>(n, N, w.diag, w.ldref, w.ld);
     count_launch(ctx);
     stage_mark(ctx, ST_TRTRI, s);
-    if ((rc = tiled_trtri_tc(ctx, B, nt, w.Ls, w.Linv, w.Ms, w.tcerr, s))) return rc;
+    if ((rc = tiled_trtri_tc(ctx, B, nt, w.Ls, w.Linv, w.Ms, w.Mc, w.tcerr, s))) return rc;
     stage_mark(ctx, ST_LAUUM, s);
     if ((rc = tiled_lauum_tc(ctx, B, nt, w.Ms, w.V, w.tcerr, s))) return rc;
     stage_mark(ctx, ST_SOLVE, s);

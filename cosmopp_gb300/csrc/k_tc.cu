@@ -41,10 +41,15 @@
 //   chol_tc_panel:  L_IJ = S_IJ Linv_J^T                       (I > J)
 //   trtri_tc_row:   (M_IJ)^T = -(sum_{k=J}^{I-1} M_kJ^T L_Ik^T) Linv_I^T    (M = L^-1, I > J)
 //   lauum_tc:       V_IJ = sum_{k >= I} M_kI^T M_kJ = (L L^T)^-1
+// A operands that are streamed from DRAM (each read by one CTA per launch: L's row
+// panels in the Cholesky, M^T's column panels in trtri) come instead from an FP32
+// copy in the same canonical layout (C1: one plane, 16 KB per tile) and are split
+// in registers, which halves their bytes; the producer warps have the time for it.
 // Layouts: A (input, I + K_b) and V (output) in FP32 64x64 column-major tiles;
-// L and S in SC tiles (rows = L's rows, K = L's columns); M in SC tiles of M^T
-// (SC tile (I, J) holds (M_IJ)^T: rows = M's columns in tile J, K = M's rows in
-// tile I); Linv_J as a 128x128 SC block [K chunk][plane][128 x 32].
+// L in SC and C1 tiles (rows = L's rows, K = L's columns), S (L before the panel
+// solve) in C1 only; M in SC and C1 tiles of M^T (tile (I, J) holds (M_IJ)^T:
+// rows = M's columns in tile J, K = M's rows in tile I); Linv_J as a 128x128 SC
+// block [K chunk][plane][128 x 32].
 #include "cg_internal.h"
 #include "cg_tc.cuh"
 
@@ -64,6 +69,7 @@ constexpr uint32_t STB_BYTES = 2u * 128 * KC * 4;  // one B stage: hi + lo, 128 
 constexpr int SC_PLANE = TS * TS;               // floats per plane of an SC tile
 constexpr int SC_CHUNK = TS * KC;               // floats per 64 x 32 block
 constexpr int SC_TILE = 2 * SC_PLANE;           // floats per SC tile (32 KB)
+constexpr int C1_TILE = SC_PLANE;               // floats per FP32 canonical tile (16 KB)
 constexpr int LI_CHUNK = 2 * 128 * KC;          // floats per K chunk of a Linv block (hi + lo)
 constexpr int LINV_SC = 4 * LI_CHUNK;           // floats per Linv block (128 KB)
 
@@ -154,25 +160,46 @@ __device__ __forceinline__ void tc_rearm(TcCtl& ctl)
 
 // ---- operand access --------------------------------------------------------
 
-// A operand: row rr of SC tile t, K chunk kc, K columns 16h .. 16h+15, hi and lo.  Across a
-// warp (32 consecutive rows) every load covers four whole 128-byte core-matrix rows.
-template <bool COHERENT>
+// A operand: row rr of SC tile t, K chunk kc, K columns 16h .. 16h+15, hi and lo.  Across a warp
+// (32 consecutive rows) every load covers four whole 128-byte core-matrix rows.
 __device__ __forceinline__ void ld_sc(const float* t, int rr, int kc, int h, float4 (&hi)[4], float4 (&lo)[4])
 {
     const float* p = t + kc * SC_CHUNK + (rr >> 3) * 256 + (rr & 7) * 4 + 4 * h * 32;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        const float4* ph = reinterpret_cast<const float4*>(p + i * 32);
-        const float4* pl = reinterpret_cast<const float4*>(p + SC_PLANE + i * 32);
-        hi[i] = COHERENT ? __ldcg(ph) : __ldg(ph);
-        lo[i] = COHERENT ? __ldcg(pl) : __ldg(pl);
+        hi[i] = __ldg(reinterpret_cast<const float4*>(p + i * 32));
+        lo[i] = __ldg(reinterpret_cast<const float4*>(p + SC_PLANE + i * 32));
     }
 }
 
-__device__ __forceinline__ void zero8(float4 (&hi)[4], float4 (&lo)[4])
+// A operand: row rr, K chunk kc, K columns 16h .. 16h+15 of an FP32 canonical tile (split into
+// hi and lo only when it is stored to tensor memory, so that the load's latency stays hidden)
+template <bool COHERENT>
+__device__ __forceinline__ void ld_c1(const float* t, int rr, int kc, int h, float4 (&x)[4])
+{
+    const float* p = t + kc * SC_CHUNK + (rr >> 3) * 256 + (rr & 7) * 4 + 4 * h * 32;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float4* px = reinterpret_cast<const float4*>(p + i * 32);
+        x[i] = COHERENT ? __ldcg(px) : __ldg(px);
+    }
+}
+
+__device__ __forceinline__ void zero4(float4 (&x)[4])
 {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) hi[i] = lo[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int i = 0; i < 4; ++i) x[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// x = hi + lo with hi = x rounded to nearest TF32 and lo = (x - hi) rounded to nearest TF32
+__device__ __forceinline__ void split4(const float4 (&x)[4], float4 (&hi)[4], float4 (&lo)[4])
+{
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        hi[i] = make_float4(tf32_rn(x[i].x), tf32_rn(x[i].y), tf32_rn(x[i].z), tf32_rn(x[i].w));
+        lo[i] = make_float4(tf32_rn(x[i].x - hi[i].x), tf32_rn(x[i].y - hi[i].y), tf32_rn(x[i].z - hi[i].z),
+                            tf32_rn(x[i].w - hi[i].w));
+    }
 }
 
 // B operand of one chunk from two stacked SC tiles (rows 0-63: top, 64-127: bot; nullptr = zero)
@@ -219,15 +246,30 @@ __device__ __forceinline__ void st_sc_row(float* tile, int rr, const float (&v)[
     st_split_row(tile, SC_CHUNK, SC_PLANE, rr, v, sgn);
 }
 
+// row rr (K values v[0..63] times sgn) of an FP32 canonical tile
+__device__ __forceinline__ void st_c1_row(float* tile, int rr, const float (&v)[64], float sgn)
+{
+#pragma unroll
+    for (int kc = 0; kc < 2; ++kc)
+#pragma unroll
+        for (int k4 = 0; k4 < 8; ++k4) {
+            const int k = 32 * kc + 4 * k4;
+            *reinterpret_cast<float4*>(tile + kc * SC_CHUNK + (rr >> 3) * 256 + k4 * 32 + (rr & 7) * 4) =
+                make_float4(sgn * v[k], sgn * v[k + 1], sgn * v[k + 2], sgn * v[k + 3]);
+        }
+}
+
 // ---- the K loop --------------------------------------------------------------
 
-// nchunks chunks; fa(c, r, h, hi, lo) loads the A chunk (row r, K half h); fb(c, dst, bar) issues
+// nchunks chunks; fa(c, r, h, x) loads the A chunk (row r, K half h): with SPLIT, x[4] holds FP32
+// values that are split into hi and lo when stored to tensor memory; without, x[8] holds hi
+// (x[0..3]) and lo (x[4..7]) as loaded; fb(c, dst, bar) issues
 // the B chunk's bulk copies into shared memory at dst.  Called by every thread of the CTA.  On
 // return the producer threads (t < NPROD) hold in R[j] the product for row t % 128, column
 // 64 (t / 128) + j (0 if nchunks == 0).  Returns false if an mbarrier wait gave up; waits give up
 // early once *err is set (by this or any other CTA), and a thread whose wait gave up skips its
 // later waits, so a failure ends the launch quickly.
-template <class FA, class FB>
+template <bool SPLIT, class FA, class FB>
 __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& ctl, uint32_t tm, float (&R)[64],
                          int* err)
 {
@@ -245,27 +287,40 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
     if (warp < NPROD / 32) {
         // ---- A producers: tensor-memory stage c & 1, then fold chunk c - 2's hi*hi sum
         const int r = threadIdx.x % 128, h = threadIdx.x / 128;
-        float4 a0h[4], a0l[4], a1h[4], a1l[4];
-        if (nchunks > 0) fa(0, r, h, a0h, a0l);
-        if (nchunks > 1) fa(1, r, h, a1h, a1l);
-        auto step = [&](int c, float4 (&qh)[4], float4 (&ql)[4]) {
+        constexpr int NX = SPLIT ? 4 : 8;
+        float4 a0[NX], a1[NX];
+        if (nchunks > 0) fa(0, r, h, a0);
+        if (nchunks > 1) fa(1, r, h, a1);
+        auto step = [&](int c, float4 (&qx)[NX]) {
             const int st = c & 1;
             if (c >= 2) {  // chunk c-2's MMAs done: its A stage is free, its hi*hi sum goes to R
                 wait(&ctl.mma_bar[st], ((c - 2) >> 1) & 1);
                 fence_after();
                 drain(tm, col_main(st), R);
             }
-            tmem_st16(tm + lane_base() + col_a_hi(st) + 16 * h, qh);
-            tmem_st16(tm + lane_base() + col_a_lo(st) + 16 * h, ql);
-            if (c + 2 < nchunks) fa(c + 2, r, h, qh, ql);
+            {
+                float4 qh[4], ql[4];
+                if constexpr (SPLIT) {
+                    split4(qx, qh, ql);
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        qh[i] = qx[i];
+                        ql[i] = qx[4 + i];
+                    }
+                }
+                tmem_st16(tm + lane_base() + col_a_hi(st) + 16 * h, qh);
+                tmem_st16(tm + lane_base() + col_a_lo(st) + 16 * h, ql);
+            }
+            if (c + 2 < nchunks) fa(c + 2, r, h, qx);
             tmem_wait_st();
             fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&ctl.a_full[st]);
         };
         for (int c = 0; c < nchunks; c += 2) {
-            step(c, a0h, a0l);
-            if (c + 1 < nchunks) step(c + 1, a1h, a1l);
+            step(c, a0);
+            if (c + 1 < nchunks) step(c + 1, a1);
         }
         if (nchunks > 0) {
             // every MMA is issued whatever happened, so the last commit always arrives: wait for it
@@ -496,9 +551,10 @@ __device__ void factor_block128(float* s, float* inv, float* tmp, int* bad)
 // Diagonal block: S_JJ factorised, L_JJ into the L storage, its inverse into Linv and, transposed,
 // into the M storage, its diagonal into diag.
 __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, const float* __restrict__ A,
-                                                      float* __restrict__ Ls, float* __restrict__ Linv,
-                                                      float* __restrict__ Ms, float* __restrict__ diag,
-                                                      int* __restrict__ status, int* __restrict__ err)
+                                                         float* __restrict__ Ls, float* __restrict__ Lc,
+                                                         float* __restrict__ Linv, float* __restrict__ Ms,
+                                                         float* __restrict__ Mc, float* __restrict__ diag,
+                                                         int* __restrict__ status, int* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ TcCtl ctl;
@@ -515,17 +571,18 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
     const size_t ntile = (size_t)ntiles_lower(nt);
     const float* Ab = A + (size_t)b * ntile * TILE_ELEMS;
     float* Lb = Ls + (size_t)b * ntile * SC_TILE;
+    float* Lcb = Lc + (size_t)b * ntile * C1_TILE;
     const uint32_t tm = tc_begin(ctl);
     const int nchunks = 2 * J2 * (TS / KC);
-    auto fa = [&](int c, int r, int h, float4 (&hi)[4], float4 (&lo)[4]) {
-        ld_sc<false>(Lb + (size_t)tile_index(2 * I2 + r / 64, c / 2) * SC_TILE, r % 64, c % 2, h, hi, lo);
+    auto fa = [&](int c, int r, int h, float4 (&x)[4]) {
+        ld_c1<false>(Lcb + (size_t)tile_index(2 * I2 + r / 64, c / 2) * C1_TILE, r % 64, c % 2, h, x);
     };
     auto fb = [&](int c, uint32_t dst, uint64_t* bar) {
         bulk_tiles(Lb + (size_t)tile_index(2 * J2, c / 2) * SC_TILE, Lb + (size_t)tile_index(2 * J2 + 1, c / 2) * SC_TILE,
                    c % 2, dst, bar);
     };
     float R[64];
-    tc_kloop(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
+    tc_kloop<true>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
     const int row = threadIdx.x % 128, h = threadIdx.x / 128;
     const bool prod = threadIdx.x < NPROD;
     if (I2 > J2) {
@@ -534,7 +591,7 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
             const float* a = Ab + (size_t)tile_index(ti, tj) * TILE_ELEMS + row % 64;
 #pragma unroll
             for (int j = 0; j < 64; ++j) R[j] = a[TS * j] - R[j];
-            st_sc_row(Lb + (size_t)tile_index(ti, tj) * SC_TILE, row % 64, R, 1.f);
+            st_c1_row(Lcb + (size_t)tile_index(ti, tj) * C1_TILE, row % 64, R, 1.f);
         }
         tc_end(tm);
         return;
@@ -561,6 +618,7 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
 #pragma unroll
             for (int j = 0; j < 64; ++j) v[j] = (row >= 64 * h + j) ? s[(64 * h + j) * 129 + row] : 0.f;
             st_sc_row(Lb + (size_t)tile_index(ti, tj) * SC_TILE, row % 64, v, 1.f);
+            st_c1_row(Lcb + (size_t)tile_index(ti, tj) * C1_TILE, row % 64, v, 1.f);
         }
     }
     if (threadIdx.x < 128) diag[(size_t)b * nt * TS + J2 * 128 + row] = s[row * 129 + row];
@@ -575,9 +633,11 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
         const int ti = 2 * J2 + h, tj = 2 * J2 + cc / 64;
         if (tj <= ti) {
             float* Mb = Ms + (size_t)b * ntile * SC_TILE;
+            float* Mcb = Mc + (size_t)b * ntile * C1_TILE;
 #pragma unroll
             for (int j = 0; j < 64; ++j) v[j] = inv[cc * 129 + 64 * h + j];
             st_sc_row(Mb + (size_t)tile_index(ti, tj) * SC_TILE, cc % 64, v, 1.f);
+            st_c1_row(Mcb + (size_t)tile_index(ti, tj) * C1_TILE, cc % 64, v, 1.f);
         }
     }
     if (threadIdx.x == 0 && ctl.bad && status && status[b] == CG_OK) status[b] = CG_ERR_NOT_PD;
@@ -586,33 +646,38 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
 
 // L_IJ = S_IJ Linv_J^T for I2 = J2 + 1 + blockIdx.x; grid (nt2 - J2 - 1, B)
 __global__ void __launch_bounds__(NTH, 1) chol_tc_panel(int J2, int nt, float* __restrict__ Ls,
-                                                     const float* __restrict__ Linv, int* __restrict__ err)
+                                                        float* __restrict__ Lc, const float* __restrict__ Linv,
+                                                        int* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ TcCtl ctl;
     const int I2 = J2 + 1 + blockIdx.x, b = blockIdx.y, nt2 = nt / 2;
     float* Lb = Ls + (size_t)b * ntiles_lower(nt) * SC_TILE;
+    float* Lcb = Lc + (size_t)b * ntiles_lower(nt) * C1_TILE;
     const float* li = Linv + ((size_t)b * nt2 + J2) * LINV_SC;
     const uint32_t tm = tc_begin(ctl);
-    // A(r, m) = S_IJ(r, m), SC tiles (2 I2 + r/64, 2 J2 + m/64); B(c, m) = Linv_J(c, m)
-    auto fa = [&](int c, int r, int h, float4 (&hi)[4], float4 (&lo)[4]) {
-        ld_sc<false>(Lb + (size_t)tile_index(2 * I2 + r / 64, 2 * J2 + c / 2) * SC_TILE, r % 64, c % 2, h, hi, lo);
+    // A(r, m) = S_IJ(r, m), C1 tiles (2 I2 + r/64, 2 J2 + m/64); B(c, m) = Linv_J(c, m)
+    auto fa = [&](int c, int r, int h, float4 (&x)[4]) {
+        ld_c1<false>(Lcb + (size_t)tile_index(2 * I2 + r / 64, 2 * J2 + c / 2) * C1_TILE, r % 64, c % 2, h, x);
     };
     auto fb = [&](int c, uint32_t dst, uint64_t* bar) { bulk_linv(li, c, dst, bar); };
     float R[64];
-    tc_kloop(128 / KC, fa, fb, smem_raw, ctl, tm, R, err);
+    tc_kloop<true>(128 / KC, fa, fb, smem_raw, ctl, tm, R, err);
     __syncthreads();  // every S read is done before the tiles are overwritten
     const int row = threadIdx.x % 128, h = threadIdx.x / 128;
-    if (threadIdx.x < NPROD)
-        st_sc_row(Lb + (size_t)tile_index(2 * I2 + row / 64, 2 * J2 + h) * SC_TILE, row % 64, R, 1.f);
+    if (threadIdx.x < NPROD) {
+        const size_t tix = tile_index(2 * I2 + row / 64, 2 * J2 + h);
+        st_sc_row(Lb + tix * SC_TILE, row % 64, R, 1.f);
+        st_c1_row(Lcb + tix * C1_TILE, row % 64, R, 1.f);
+    }
     tc_end(tm);
 }
 
 // Row block I2 of M = L^-1, off-diagonal blocks J2 = blockIdx.x < I2; grid (I2, B).  Computes
 // the transposes: S^T = sum_{k=2 J2}^{2 I2 - 1} M_kJ^T L_Ik^T, then (M_IJ)^T = -S^T Linv_I^T.
 __global__ void __launch_bounds__(NTH, 1) trtri_tc_row(int I2, int nt, const float* __restrict__ Ls,
-                                                    const float* __restrict__ Linv, float* __restrict__ Ms,
-                                                    int* __restrict__ err)
+                                                       const float* __restrict__ Linv, float* __restrict__ Ms,
+                                                       float* __restrict__ Mc, int* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ TcCtl ctl;
@@ -620,17 +685,18 @@ __global__ void __launch_bounds__(NTH, 1) trtri_tc_row(int I2, int nt, const flo
     const size_t ntile = (size_t)ntiles_lower(nt);
     const float* Lb = Ls + (size_t)b * ntile * SC_TILE;
     float* Mb = Ms + (size_t)b * ntile * SC_TILE;
+    float* Mcb = Mc + (size_t)b * ntile * C1_TILE;
     const float* li = Linv + ((size_t)b * nt2 + I2) * LINV_SC;
     const int row = threadIdx.x % 128, h = threadIdx.x / 128;
     const uint32_t tm = tc_begin(ctl);
-    // A(c, m) = M_kJ(m, c): SC tile (k, 2 J2 + c/64) of M^T (zero above the diagonal);
+    // A(c, m) = M_kJ(m, c): C1 tile (k, 2 J2 + c/64) of M^T (zero above the diagonal);
     // B(r, m) = L_Ik(r, m): SC tiles (2 I2, k), (2 I2 + 1, k)
     const int k0 = 2 * J2;
     const int nchunks = (2 * I2 - k0) * (TS / KC);
-    auto fa = [&](int c, int r, int hh, float4 (&hi)[4], float4 (&lo)[4]) {
+    auto fa = [&](int c, int r, int hh, float4 (&x)[4]) {
         const int k = k0 + c / 2, col = 2 * J2 + r / 64;
-        if (k < col) zero8(hi, lo);
-        else ld_sc<false>(Mb + (size_t)tile_index(k, col) * SC_TILE, r % 64, c % 2, hh, hi, lo);
+        if (k < col) zero4(x);
+        else ld_c1<false>(Mcb + (size_t)tile_index(k, col) * C1_TILE, r % 64, c % 2, hh, x);
     };
     auto fb = [&](int c, uint32_t dst, uint64_t* bar) {
         const int k = k0 + c / 2;
@@ -638,27 +704,30 @@ __global__ void __launch_bounds__(NTH, 1) trtri_tc_row(int I2, int nt, const flo
                    c % 2, dst, bar);
     };
     float R[64];
-    tc_kloop(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
+    tc_kloop<true>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
     // S^T into the M storage of block (I2, J2): row = M's column, K = M's rows 64h .. 64h+63
     if (threadIdx.x < NPROD)
-        st_sc_row(Mb + (size_t)tile_index(2 * I2 + h, 2 * J2 + row / 64) * SC_TILE, row % 64, R, 1.f);
+        st_c1_row(Mcb + (size_t)tile_index(2 * I2 + h, 2 * J2 + row / 64) * C1_TILE, row % 64, R, 1.f);
     tc_rearm(ctl);  // its __syncthreads also makes the S^T stores visible to the whole CTA
     // A(c, m) = S^T(c, m): written above by this CTA (coherent loads); B(r, m) = Linv_I(r, m)
-    auto fa2 = [&](int c, int r, int hh, float4 (&hi)[4], float4 (&lo)[4]) {
-        ld_sc<true>(Mb + (size_t)tile_index(2 * I2 + c / 2, 2 * J2 + r / 64) * SC_TILE, r % 64, c % 2, hh, hi, lo);
+    auto fa2 = [&](int c, int r, int hh, float4 (&x)[4]) {
+        ld_c1<true>(Mcb + (size_t)tile_index(2 * I2 + c / 2, 2 * J2 + r / 64) * C1_TILE, r % 64, c % 2, hh, x);
     };
     auto fb2 = [&](int c, uint32_t dst, uint64_t* bar) { bulk_linv(li, c, dst, bar); };
-    tc_kloop(128 / KC, fa2, fb2, smem_raw, ctl, tm, R, err);
+    tc_kloop<true>(128 / KC, fa2, fb2, smem_raw, ctl, tm, R, err);
     __syncthreads();  // every S^T read is done before the tiles are overwritten
-    if (threadIdx.x < NPROD)
-        st_sc_row(Mb + (size_t)tile_index(2 * I2 + h, 2 * J2 + row / 64) * SC_TILE, row % 64, R, -1.f);
+    if (threadIdx.x < NPROD) {
+        const size_t tix = tile_index(2 * I2 + h, 2 * J2 + row / 64);
+        st_sc_row(Mb + tix * SC_TILE, row % 64, R, -1.f);
+        st_c1_row(Mcb + tix * C1_TILE, row % 64, R, -1.f);
+    }
     tc_end(tm);
 }
 
 // V_IJ (128x128 supertile, lower) = sum over k of M_k,I^T M_k,J from the M^T storage; V in FP32
 // column-major tiles.  grid (supertiles of the lower triangle, B).
 __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restrict__ Ms, float* __restrict__ V,
-                                                int* __restrict__ err)
+                                                   int* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ TcCtl ctl;
@@ -671,10 +740,22 @@ __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restri
     const int k0 = 2 * I2;  // first tile row with a non-zero M_k,I
     const int nchunks = (nt - k0) * (TS / KC);
     // A(r, m) = M_{k, 2I2 + r/64}(m, r%64); B(c, m) = M_{k, 2J2 + c/64}(m, c%64); zero above the diagonal
-    auto fa = [&](int c, int r, int h, float4 (&hi)[4], float4 (&lo)[4]) {
+    // (A from the split copy: lauum's operands are shared by many CTAs and stay in L2, so the
+    // extra bytes cost less than splitting in the producers)
+    auto fa = [&](int c, int r, int h, float4 (&x)[8]) {
         const int k = k0 + c / 2, col = 2 * I2 + r / 64;
-        if (k < col) zero8(hi, lo);
-        else ld_sc<false>(Mb + (size_t)tile_index(k, col) * SC_TILE, r % 64, c % 2, h, hi, lo);
+        if (k < col) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) x[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+            float4 hi[4], lo[4];
+            ld_sc(Mb + (size_t)tile_index(k, col) * SC_TILE, r % 64, c % 2, h, hi, lo);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                x[i] = hi[i];
+                x[4 + i] = lo[i];
+            }
+        }
     };
     auto fb = [&](int c, uint32_t dst, uint64_t* bar) {
         const int k = k0 + c / 2;
@@ -683,7 +764,7 @@ __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restri
         bulk_tiles(top, bot, c % 2, dst, bar);
     };
     float R[64];
-    tc_kloop(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
+    tc_kloop<false>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
     store_block(R, V + (size_t)b * ntile * TILE_ELEMS, I2, J2, 1.f);
     tc_end(tm);
 }
@@ -705,20 +786,21 @@ static int set_smem(cg_ctx* ctx, K kern)
 }
 
 size_t tc_split_elems(int nt) { return (size_t)ntiles_lower(nt) * SC_TILE; }
+size_t tc_c1_elems(int nt) { return (size_t)ntiles_lower(nt) * C1_TILE; }
 size_t tc_linv_elems(int nt) { return (size_t)(nt / 2) * LINV_SC; }
 
-int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, float* Linv, float* Ms, float* diag,
-                      int* status, int* d_err, cudaStream_t s)
+int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, float* Lc, float* Linv, float* Ms,
+                      float* Mc, float* diag, int* status, int* d_err, cudaStream_t s)
 {
     if (nt % 2) { ctx->err = "tensor-core Cholesky needs an even tile count"; return CG_ERR_BAD_ARG; }
     int rc;
     if ((rc = set_smem(ctx, chol_tc_update)) || (rc = set_smem(ctx, chol_tc_panel))) return rc;
     const int nt2 = nt / 2;
     for (int J2 = 0; J2 < nt2; ++J2) {
-        chol_tc_update<<<B * (nt2 - J2), NTH, tc_smem(), s>>>(J2, nt, B, A, Ls, Linv, Ms, diag, status, d_err);
+        chol_tc_update<<<B * (nt2 - J2), NTH, tc_smem(), s>>>(J2, nt, B, A, Ls, Lc, Linv, Ms, Mc, diag, status, d_err);
         count_launch(ctx);
         if (J2 + 1 < nt2) {
-            chol_tc_panel<<<dim3(nt2 - J2 - 1, B), NTH, tc_smem(), s>>>(J2, nt, Ls, Linv, d_err);
+            chol_tc_panel<<<dim3(nt2 - J2 - 1, B), NTH, tc_smem(), s>>>(J2, nt, Ls, Lc, Linv, d_err);
             count_launch(ctx);
         }
     }
@@ -726,15 +808,15 @@ int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, flo
     return CG_OK;
 }
 
-int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* Ls, const float* Linv, float* Ms, int* d_err,
-                   cudaStream_t s)
+int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* Ls, const float* Linv, float* Ms, float* Mc,
+                   int* d_err, cudaStream_t s)
 {
     if (nt % 2) { ctx->err = "tensor-core trtri needs an even tile count"; return CG_ERR_BAD_ARG; }
     int rc;
     if ((rc = set_smem(ctx, trtri_tc_row))) return rc;
     const int nt2 = nt / 2;
     for (int I2 = 1; I2 < nt2; ++I2) {  // the diagonal blocks M_II come from the Cholesky
-        trtri_tc_row<<<dim3(I2, B), NTH, tc_smem(), s>>>(I2, nt, Ls, Linv, Ms, d_err);
+        trtri_tc_row<<<dim3(I2, B), NTH, tc_smem(), s>>>(I2, nt, Ls, Linv, Ms, Mc, d_err);
         count_launch(ctx);
     }
     CG_CUDA_TRY(ctx, cudaGetLastError());
