@@ -87,6 +87,7 @@ def library():
     L.cg_reference_count.argtypes = [ctypes.c_void_p]
     L.cg_hmc_run.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, _dp, _dp, ctypes.c_int, ctypes.c_int,
                              ctypes.c_double, _dp, ctypes.c_int, ctypes.c_ulonglong, _dp, _dp]
+    L.cg_selftest_wait_timeout.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
     L.cg_launch_count.restype = ctypes.c_longlong
     L.cg_launch_count.argtypes = [ctypes.c_void_p]
     L.cg_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int]
@@ -310,6 +311,12 @@ class Context:
                                        int(nleap), float(tau), _p(m), int(bool(jitter)), int(seed), _p(chain),
                                        _p(acc)))
         return chain, acc
+
+    def selftest_wait_timeout(self):
+        """Status a bounded device wait reports when it gives up (CG_ERR_TIMEOUT expected)."""
+        st = ctypes.c_int(-1)
+        self._check(self._L.cg_selftest_wait_timeout(self._h, ctypes.byref(st)))
+        return st.value
 
     def launch_count(self):
         """Kernels this context has launched so far."""

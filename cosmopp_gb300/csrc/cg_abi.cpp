@@ -505,3 +505,10 @@ extern "C" int cg_likelihood_calculate(cg_lik* lik, const double* t, double* chi
     }
     return CG_OK;
 }
+
+extern "C" int cg_selftest_wait_timeout(cg_ctx* ctx, int* status)
+{
+    if (!ctx || !status) return CG_ERR_BAD_ARG;
+    CG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    return cg::selftest_wait_timeout(ctx, status);
+}

@@ -184,6 +184,7 @@ int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, flo
 int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* Ls, const float* Linv, float* Ms, float* Mc,
                    int* d_err, cudaStream_t s);
 int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, float* V, int* d_err, cudaStream_t s);
+int selftest_wait_timeout(cg_ctx* ctx, int* host_status);
 // mixed path (k_mixed.cu)
 int mixed_prepare_reference(cg_ctx* ctx, const double* cl_ref_host);
 int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, const double* d_d, int d_stride,

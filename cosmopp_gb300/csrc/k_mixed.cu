@@ -29,6 +29,7 @@
 #include <vector>
 
 #include "cg_internal.h"
+#include "cg_tc.cuh"
 #include "cg_tile.cuh"
 
 namespace cg {
@@ -126,7 +127,7 @@ __global__ void __launch_bounds__(256) build_ubar(int N, int lmax, int lp, const
     constexpr int HB = 32;                                   // harmonics per sub-batch
     double* zi = reinterpret_cast<double*>(smem_raw);        // [HB][TS]
     double* zj = zi + HB * TS;                               // [HB][CC]
-    float* out = reinterpret_cast<float*>(zj + HB * CC);     // [CC*TS][lp]
+    float* out = reinterpret_cast<float*>(zj + HB * CC);     // [lp][CC*TS]
     int I, J;
     tile_coords(blockIdx.x, I, J);
     const int c_begin = blockIdx.y * CC;
@@ -157,11 +158,12 @@ __global__ void __launch_bounds__(256) build_ubar(int N, int lmax, int lp, const
             __syncthreads();
         }
 #pragma unroll
-        for (int p = 0; p < PER; ++p) out[(threadIdx.x + 256 * p) * lp + l] = (float)(cref[l] * acc[p]);
+        for (int p = 0; p < PER; ++p) out[l * NE + threadIdx.x + 256 * p] = (float)(cref[l] * acc[p]);
     }
     __syncthreads();
-    float* dst = U + ((size_t)blockIdx.x * TILE_ELEMS + (size_t)c_begin * TS) * lp;
-    for (int k = threadIdx.x; k < NE * lp; k += blockDim.x) dst[k] = out[k];
+    // table layout [tile][l][entry]: each l row of this block's entries is contiguous
+    float* dst = U + (size_t)blockIdx.x * TILE_ELEMS * lp + (size_t)c_begin * TS;
+    for (int k = threadIdx.x; k < NE * lp; k += blockDim.x) dst[(size_t)(k / NE) * TILE_ELEMS + k % NE] = out[k];
 }
 
 // y[b][I-block] = sum_{J <= I} Mref_IJ d_b[J-block]; grid (nt, maps), 256 threads
@@ -186,7 +188,7 @@ __global__ void __launch_bounds__(256) trmv_lower(int nt, int n, int N, const do
     if (q == 0) y[(size_t)b * N + I * TS + r] = ((part[0][r] + part[1][r]) + part[2][r]) + part[3][r];
 }
 
-// eps[b][l] = C_bl / cref_l - 1 (0 for l < 2 and padding)
+// eps[l][b] = C_bl / cref_l - 1 (0 for l < 2 and padding)
 __global__ void make_eps(int B, int lmax, int lp, const double* __restrict__ cl, const double* __restrict__ cref,
                          float* __restrict__ eps)
 {
@@ -197,7 +199,7 @@ __global__ void make_eps(int B, int lmax, int lp, const double* __restrict__ cl,
             const double c = cl[(size_t)b * (lmax + 1) + l];
             v = (float)(c / cref[l] - 1.0);
         }
-        eps[(size_t)b * lp + l] = v;
+        eps[(size_t)l * B + b] = v;  // [l][b]: the contraction stages a row of batch elements per l
     }
 }
 
@@ -211,67 +213,96 @@ __global__ void init_status(int B, const double* __restrict__ cl, int lmax, int*
     status[b] = st;
 }
 
-// Forward contraction: A_b[t][e] = [e on the diagonal] + sum_l Ubar[t][e][l] eps[b][l],
-// written to A.
-// grid (tiles * TILE_ELEMS / 128, ceil(B / 128)); 256 threads, 8 entries x 8 batch each.
+// Forward contraction: A_b[t][e] = [e on the diagonal] + sum_l Ubar[t][l][e] eps[l][b], written
+// to A.  A CTA covers BB batch elements and FWD_NBLK consecutive blocks of EB = 16384 / BB entries
+// (blocks never straddle a tile); thread (te, tb) computes 8 entries x 8 batch elements.  The
+// next block's table rows (lp rows of EB floats, 4096 floats apart) arrive by bulk copies into a
+// double buffer while the current block is computed; eps is staged once.  A bounded wait that
+// gives up sets *err (reported as CG_ERR_TIMEOUT).
+// grid (tiles * TILE_ELEMS / (EB * FWD_NBLK), ceil(B / BB)).
+constexpr int FWD_NBLK = 8;
+template <int BB>
 __global__ void __launch_bounds__(256) contract_fwd(int B, int lp, const float* __restrict__ U,
                                                     const float* __restrict__ eps, float* __restrict__ A,
-                                                    size_t strideA)
+                                                    size_t strideA, int* __restrict__ err)
 {
-    extern __shared__ float fsm[];
-    constexpr int LD = 132;      // 128 + 4: 16-byte rows, staging stores spread over 8 banks
-    float* sU = fsm;             // [lp][LD]
-    float* sE = fsm + lp * LD;   // [lp][LD]
-    const size_t e_begin = (size_t)blockIdx.x * 128;  // global entry index over all tiles
-    const int b_begin = blockIdx.y * 128;
-    const float* ublk = U + e_begin * lp;
-    // the 128 x lp block of the table and of eps are contiguous in global memory: read them in
-    // order (coalesced) and transpose into [l][entry] / [l][batch]
-    for (int k = threadIdx.x; k < 128 * lp; k += 256) {
-        const int e = k / lp, l = k % lp;
-        sU[l * LD + e] = ublk[k];
-        const int bb = b_begin + e;
-        sE[l * LD + e] = (bb < B) ? eps[(size_t)b_begin * lp + k] : 0.f;
+    constexpr int EB = 128 * 128 / BB, TE = EB / 8;  // entries per block, threads along entries
+    extern __shared__ __align__(128) float fsm[];
+    float* sE = fsm;                       // [lp][BB]
+    float* sU = fsm + lp * BB;             // [2][lp][EB]
+    __shared__ uint64_t full[2];
+    const int b_begin = blockIdx.y * BB;
+    const size_t blk0 = (size_t)blockIdx.x * FWD_NBLK;  // first entry block of this CTA
+    const uint32_t bytes = (uint32_t)(lp * EB * sizeof(float));
+    auto issue = [&](int i) {  // table rows of block blk0 + i into buffer i & 1 (thread 0)
+        const size_t e_begin = (blk0 + i) * EB;
+        const float* src = U + (e_begin / TILE_ELEMS) * TILE_ELEMS * lp + e_begin % TILE_ELEMS;
+        float* dst = sU + (i & 1) * lp * EB;
+        tc::mbar_arrive_expect_tx(&full[i & 1], bytes);
+        for (int l = 0; l < lp; ++l)
+            tc::bulk_g2s(tc::smem_u32(dst + l * EB), src + (size_t)l * TILE_ELEMS, EB * sizeof(float), &full[i & 1]);
+    };
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&full[0], 1);
+        tc::mbar_init(&full[1], 1);
+        tc::fence_mbar_init();
+        issue(0);
+        issue(1);
+    }
+    for (int k = threadIdx.x; k < lp * BB; k += 256) {
+        const int l = k / BB, bb = k % BB, b = b_begin + bb;
+        sE[l * BB + bb] = (b < B) ? eps[(size_t)l * B + b] : 0.f;
     }
     __syncthreads();
-    const int te = threadIdx.x % 16, tb = threadIdx.x / 16;
+    const int te = threadIdx.x % TE, tb = threadIdx.x / TE;
     const int e0 = te * 8, b0 = tb * 8;
-    float acc[8][8];
-#pragma unroll
-    for (int a = 0; a < 8; ++a)
-#pragma unroll
-        for (int q = 0; q < 8; ++q) acc[a][q] = 0.f;
-    for (int l = 0; l < lp; ++l) {
-        const float4 u0 = *reinterpret_cast<const float4*>(&sU[l * LD + e0]);
-        const float4 u1 = *reinterpret_cast<const float4*>(&sU[l * LD + e0 + 4]);
-        const float4 w0 = *reinterpret_cast<const float4*>(&sE[l * LD + b0]);
-        const float4 w1 = *reinterpret_cast<const float4*>(&sE[l * LD + b0 + 4]);
-        const float u[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
-        const float w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+    bool ok = true;
+    for (int i = 0; i < FWD_NBLK; ++i) {
+        if (ok && !tc::mbar_wait(&full[i & 1], (i >> 1) & 1, 1u << 22, err)) {
+            ok = false;
+            atomicExch(err, 1);
+        }
+        const float* bu = sU + (i & 1) * lp * EB;
+        float acc[8][8];
 #pragma unroll
         for (int a = 0; a < 8; ++a)
 #pragma unroll
-            for (int q = 0; q < 8; ++q) acc[a][q] = fmaf(u[a], w[q], acc[a][q]);
-    }
-    const size_t tile_id = e_begin / TILE_ELEMS;
-    int I, J;
-    tile_coords((int)tile_id, I, J);
-    const int ein = (int)(e_begin % TILE_ELEMS) + e0;  // entry offset within the tile
+            for (int q = 0; q < 8; ++q) acc[a][q] = 0.f;
+        if (b_begin + b0 < B) {
+            for (int l = 0; l < lp; ++l) {
+                const float4 u0 = *reinterpret_cast<const float4*>(&bu[l * EB + e0]);
+                const float4 u1 = *reinterpret_cast<const float4*>(&bu[l * EB + e0 + 4]);
+                const float4 w0 = *reinterpret_cast<const float4*>(&sE[l * BB + b0]);
+                const float4 w1 = *reinterpret_cast<const float4*>(&sE[l * BB + b0 + 4]);
+                const float u[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+                const float w[8] = {w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-        const int bb = b_begin + b0 + q;
-        if (bb >= B) continue;
-        float v[8];
+                for (int a = 0; a < 8; ++a)
 #pragma unroll
-        for (int a = 0; a < 8; ++a) {
-            const int e = ein + a;
-            const bool dg = (I == J) && (e % TS == e / TS);
-            v[a] = acc[a][q] + (dg ? 1.f : 0.f);
+                    for (int q = 0; q < 8; ++q) acc[a][q] = fmaf(u[a], w[q], acc[a][q]);
+            }
         }
-        const size_t off = (size_t)bb * strideA + e_begin + e0;
-        float4* pa = reinterpret_cast<float4*>(A + off);
-        pa[0] = make_float4(v[0], v[1], v[2], v[3]);
-        pa[1] = make_float4(v[4], v[5], v[6], v[7]);
+        __syncthreads();  // buffer i & 1 is read: refill it with block i + 2
+        if (threadIdx.x == 0 && i + 2 < FWD_NBLK) issue(i + 2);
+        const size_t e_begin = (blk0 + i) * EB;
+        int I, J;
+        tile_coords((int)(e_begin / TILE_ELEMS), I, J);
+        const int ein = (int)(e_begin % TILE_ELEMS) + e0;  // entry offset within the tile
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const int bb = b_begin + b0 + q;
+            if (bb >= B) continue;
+            float v[8];
+#pragma unroll
+            for (int a = 0; a < 8; ++a) {
+                const int e = ein + a;
+                const bool dg = (I == J) && (e % TS == e / TS);
+                v[a] = acc[a][q] + (dg ? 1.f : 0.f);
+            }
+            float4* pa = reinterpret_cast<float4*>(A + (size_t)bb * strideA + e_begin + e0);
+            pa[0] = make_float4(v[0], v[1], v[2], v[3]);
+            pa[1] = make_float4(v[4], v[5], v[6], v[7]);
+        }
     }
 }
 
@@ -334,7 +365,7 @@ __global__ void broadcast_vec(int B, int N, const double* __restrict__ y, double
 //                    diagonal, 1 on it, 0 above it (the tiles hold the lower triangle);
 //   x^T Ubar_l x   = cref_l |Z_l^T x|^2, Ubar_l = cref_l Z_l Z_l^T (Z_l: the 2l+1 rows of Z).
 
-// part[t][b][l] = sum_{e in tile t} w_e V_b[t][e] Ubar[t][e][l]: one CTA per tile and 256 batch
+// part[t][b][l] = sum_{e in tile t} w_e V_b[t][e] Ubar[t][l][e]: one CTA per tile and 256 batch
 // elements (the tile's table block is read once per 48 l); grid (tiles, ceil(B / 256),
 // ceil(lp / 48)).  Thread (bg = t % 32, lg = t / 32) holds batch elements bg + 32 a (a < 8) and
 // l = lbase + 6 lg .. + 5.  V chunks are staged [b][entry] with row
@@ -347,7 +378,7 @@ __global__ void __launch_bounds__(256, 2) contract_adj(int B, int lp, const floa
 {
     extern __shared__ float asm_[];
     float* sV = asm_;                      // [256][ADJ_LD]
-    float* sU = asm_ + 256 * ADJ_LD;       // [ADJ_KE][48]
+    float* sU = asm_ + 256 * ADJ_LD;       // [48][ADJ_KE]
     const int t = blockIdx.x, b_begin = blockIdx.y * 256, lbase = 48 * blockIdx.z;
     int I, J;
     tile_coords(t, I, J);
@@ -358,10 +389,12 @@ __global__ void __launch_bounds__(256, 2) contract_adj(int B, int lp, const floa
 #pragma unroll
         for (int q = 0; q < 6; ++q) acc[a][q] = 0.f;
     const float* Ut = U + (size_t)t * TILE_ELEMS * lp;
+    // batch rows present; staging skips the 32-row groups beyond them (their sums are never stored)
+    const int nrow = min(256, B - b_begin), na = (nrow + 31) / 32;
     for (int e0 = 0; e0 < TILE_ELEMS; e0 += ADJ_KE) {
         __syncthreads();
-        // V: 256 rows x 64 entries, 16 threads per row (coalesced), weights applied
-        for (int k = threadIdx.x; k < 256 * (ADJ_KE / 4); k += 256) {
+        // V: up to 256 rows x 64 entries, 16 threads per row (coalesced), weights applied
+        for (int k = threadIdx.x; k < 32 * na * (ADJ_KE / 4); k += 256) {
             const int bb = k / (ADJ_KE / 4), e4 = k % (ADJ_KE / 4), b = b_begin + bb;
             float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
             if (b < B) {
@@ -376,31 +409,32 @@ __global__ void __launch_bounds__(256, 2) contract_adj(int B, int lp, const floa
             }
             *reinterpret_cast<float4*>(&sV[bb * ADJ_LD + 4 * e4]) = v;
         }
-        // table: 64 entries x 48 l
-        for (int k = threadIdx.x; k < ADJ_KE * 12; k += 256) {
-            const int e = k / 12, q4 = k % 12;
+        // table: 48 l rows x 64 entries (rows contiguous in the [tile][l][entry] layout)
+        for (int k = threadIdx.x; k < 48 * (ADJ_KE / 4); k += 256) {
+            const int l = k / (ADJ_KE / 4), e4 = k % (ADJ_KE / 4);
             float4 u = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (lbase + 4 * q4 < lp) u = __ldg(reinterpret_cast<const float4*>(Ut + (size_t)(e0 + e) * lp + lbase + 4 * q4));
-            *reinterpret_cast<float4*>(&sU[e * 48 + 4 * q4]) = u;
+            if (lbase + l < lp)
+                u = __ldg(reinterpret_cast<const float4*>(Ut + (size_t)(lbase + l) * TILE_ELEMS + e0 + 4 * e4));
+            *reinterpret_cast<float4*>(&sU[l * ADJ_KE + 4 * e4]) = u;
         }
         __syncthreads();
 #pragma unroll 2
         for (int e4 = 0; e4 < ADJ_KE / 4; ++e4) {
-            float4 v[8];
+            float4 v[8], u4[6];
 #pragma unroll
             for (int a = 0; a < 8; ++a) v[a] = *reinterpret_cast<const float4*>(&sV[(bg + 32 * a) * ADJ_LD + 4 * e4]);
 #pragma unroll
+            for (int q = 0; q < 6; ++q) u4[q] = *reinterpret_cast<const float4*>(&sU[(l0 + q) * ADJ_KE + 4 * e4]);
+#pragma unroll
             for (int j = 0; j < 4; ++j) {
-                const float* ur = &sU[(4 * e4 + j) * 48 + l0];
-                const float2 u01 = *reinterpret_cast<const float2*>(ur);
-                const float2 u23 = *reinterpret_cast<const float2*>(ur + 2);
-                const float2 u45 = *reinterpret_cast<const float2*>(ur + 4);
-                const float u[6] = {u01.x, u01.y, u23.x, u23.y, u45.x, u45.y};
 #pragma unroll
                 for (int a = 0; a < 8; ++a) {
                     const float va = (j == 0) ? v[a].x : (j == 1) ? v[a].y : (j == 2) ? v[a].z : v[a].w;
 #pragma unroll
-                    for (int q = 0; q < 6; ++q) acc[a][q] = fmaf(va, u[q], acc[a][q]);
+                    for (int q = 0; q < 6; ++q) {
+                        const float uq = (j == 0) ? u4[q].x : (j == 1) ? u4[q].y : (j == 2) ? u4[q].z : u4[q].w;
+                        acc[a][q] = fmaf(va, uq, acc[a][q]);
+                    }
                 }
             }
         }
@@ -598,18 +632,18 @@ int mixed_prepare_reference(cg_ctx* ctx, const double* cl_ref_host)
         CG_CUDA_TRY(ctx, cudaMemsetAsync(w.Y, 0, sizeof(double) * (size_t)nhp * N, s));
         ylm_basis<<<dim3((N + 127) / 128, lmax + 1), 128, 0, s>>>(n, N, lmax, ctx->d_xyz, ctx->d_beam, w.Y);
         const size_t smz = 2 * (size_t)TS * SmemLd<double>::v * sizeof(double);
-        cudaFuncSetAttribute(whiten_basis, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
+        CG_CUDA_TRY(ctx, cudaFuncSetAttribute(whiten_basis, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz));
         whiten_basis<<<dim3(nt, nhp / TS), 256, smz, s>>>(nt, N, w.Mref, w.Y, w.Z);
         to_f32<<<1024, 256, 0, s>>>((size_t)nhp * N, w.Z, w.Zf);
         if (lp <= 48) {
             constexpr int CC = 8;
             const size_t smu = sizeof(double) * 32 * (TS + CC) + sizeof(float) * (size_t)CC * TS * lp;
-            cudaFuncSetAttribute(build_ubar<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smu);
+            CG_CUDA_TRY(ctx, cudaFuncSetAttribute(build_ubar<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smu));
             build_ubar<CC><<<dim3(ntiles_lower(nt), TS / CC), 256, smu, s>>>(N, lmax, lp, w.Z, w.cref, w.U);
         } else {
             constexpr int CC = 4;
             const size_t smu = sizeof(double) * 32 * (TS + CC) + sizeof(float) * (size_t)CC * TS * lp;
-            cudaFuncSetAttribute(build_ubar<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smu);
+            CG_CUDA_TRY(ctx, cudaFuncSetAttribute(build_ubar<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smu));
             build_ubar<CC><<<dim3(ntiles_lower(nt), TS / CC), 256, smu, s>>>(N, lmax, lp, w.Z, w.cref, w.U);
         }
         CG_CUDA_TRY(ctx, cudaGetLastError());
@@ -677,6 +711,7 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
     const int lp = w.lpad, ntile = ntiles_lower(nt);
     const size_t tiled = tiled_elems(nt);
     stage_mark(ctx, ST_BUILD, s);
+    CG_CUDA_TRY(ctx, cudaMemsetAsync(w.tcerr, 0, sizeof(int), s));  // a timeout reports on its own call only
     init_status<<<(B + 127) / 128, 128, 0, s>>>(B, d_cl, lmax, w.st);
     make_eps<<<B, 64, 0, s>>>(B, lmax, lp, d_cl, w.cref, w.eps);
     count_launch(ctx, d_stride == 0 ? 5 : 4);
@@ -687,12 +722,17 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
     } else {
         trmv_lower<<<dim3(nt, B), 256, 0, s>>>(nt, n, N, w.Mref, d_d, d_stride, w.y);
     }
-    // A_b = I + sum_l eps_bl Ubar_l
-    {
-        const size_t smem = sizeof(float) * 2 * 132 * lp;
-        cudaFuncSetAttribute(contract_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        contract_fwd<<<dim3((unsigned)(tiled / 128), (B + 127) / 128), 256, smem, s>>>(B, lp, w.U, w.eps, w.A,
-                                                                                        tiled);
+    // A_b = I + sum_l eps_bl Ubar_l; small batches use 32-element CTA tiles (more entries per block)
+    // when the double-buffered table rows fit in shared memory
+    const size_t smem32 = sizeof(float) * lp * (32 + 2 * 512), smem128 = sizeof(float) * lp * (128 + 2 * 128);
+    if (B <= 48 && smem32 <= 200 * 1024) {
+        CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_fwd<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32));
+        contract_fwd<32><<<dim3((unsigned)(tiled / (512 * FWD_NBLK)), (B + 31) / 32), 256, smem32, s>>>(
+            B, lp, w.U, w.eps, w.A, tiled, w.tcerr);
+    } else {
+        CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_fwd<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem128));
+        contract_fwd<128><<<dim3((unsigned)(tiled / (128 * FWD_NBLK)), (B + 127) / 128), 256, smem128, s>>>(
+            B, lp, w.U, w.eps, w.A, tiled, w.tcerr);
     }
     stage_mark(ctx, ST_CHOL, s);
     if ((rc = tiled_cholesky_tc(ctx, B, nt, w.A, w.Ls, w.Lc, w.Linv, w.Ms, w.Mc, w.diag, w.st, w.tcerr, s))) return rc;
@@ -714,8 +754,8 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
     count_launch(ctx, 7);
     stage_mark(ctx, ST_ADJOINT, s);
     if (d_grad) {
-        const size_t sma = sizeof(float) * (256 * ADJ_LD + ADJ_KE * 48);
-        cudaFuncSetAttribute(contract_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma);
+        const size_t sma = sizeof(float) * (256 * ADJ_LD + 48 * ADJ_KE);
+        CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma));
         contract_adj<<<dim3(ntile, (B + 255) / 256, (lp + 47) / 48), 256, sma, s>>>(B, lp, w.U, w.V, tiled, w.gpart);
         const int nhp = nharm_pad(lmax);
         project_x<<<dim3(nhp / 64, (B + 63) / 64), 256, 0, s>>>(B, N, nhp, w.Zf, w.x, w.proj);

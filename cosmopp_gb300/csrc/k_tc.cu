@@ -769,6 +769,18 @@ __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restri
     tc_end(tm);
 }
 
+// Self-test of the bounded-wait path: one thread waits, with a short limit, on an mbarrier
+// that nothing arrives on; the wait must give up and report CG_ERR_TIMEOUT.
+__global__ void wait_timeout_probe(int* status)
+{
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+        *status = mbar_wait(&bar, 0, 1u << 12) ? CG_OK : CG_ERR_TIMEOUT;
+    }
+}
+
 }  // namespace
 
 static int tc_smem()
@@ -832,6 +844,23 @@ int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, float* V, int* d
     lauum_tc<<<dim3(nt2 * (nt2 + 1) / 2, B), NTH, tc_smem(), s>>>(nt, Ms, V, d_err);
     count_launch(ctx);
     CG_CUDA_TRY(ctx, cudaGetLastError());
+    return CG_OK;
+}
+
+int selftest_wait_timeout(cg_ctx* ctx, int* host_status)
+{
+    int* d = nullptr;
+    CG_CUDA_TRY(ctx, cudaMalloc((void**)&d, sizeof(int)));
+    wait_timeout_probe<<<1, 32, 0, ctx->stream>>>(d);
+    count_launch(ctx);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(host_status, d, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(d);
+    if (e != cudaSuccess) {
+        ctx->err = cudaGetErrorString(e);
+        return CG_ERR_CUDA;
+    }
     return CG_OK;
 }
 

@@ -102,7 +102,8 @@ int cg_fiducial_matrix(cg_ctx* ctx, const double* cl, int lmax, int lmax_max, co
    hard-coded detOffset: logdet is the raw ln det C).
    d: one map (d_stride = 0) or B maps at stride d_stride (>= n).
    grad (nullable): [B][lmax+1] d(-2lnL)/dC_l (l < 2 are 0) -- new, no reference counterpart.
-   chi2 / logdet / status nullable; status[b] = CG_OK or CG_ERR_NOT_PD / CG_ERR_NONFINITE.
+   chi2 / logdet / status nullable; status[b] = CG_OK or CG_ERR_NOT_PD / CG_ERR_NONFINITE, or
+   (mixed path) CG_ERR_TIMEOUT when a bounded tensor-core wait gave up during the call.
    Returns CG_OK when the call ran, even if some elements carry a bad status. */
 int cg_loglike(cg_ctx* ctx, int B, const double* cl, const double* d, int d_stride,
                double* m2lnl, double* chi2, double* logdet, double* grad, int* status);
@@ -130,6 +131,10 @@ int cg_hmc_run(cg_ctx* ctx, const double* map, int nchains, const double* x0, co
                double* chain, double* accept_rate);
 
 /* ---- instrumentation ------------------------------------------------------ */
+/* self-test of the failure path of the device's bounded waits: one thread waits, with a short
+   limit, on a barrier that nothing completes; *status receives CG_ERR_TIMEOUT when the wait
+   gave up and reported as it should.  Nothing faults or hangs; the context stays usable. */
+int cg_selftest_wait_timeout(cg_ctx* ctx, int* status);
 /* kernels this context has launched so far */
 long long cg_launch_count(const cg_ctx* ctx);
 /* record CUDA events between the stages of each cg_loglike* call */

@@ -101,6 +101,22 @@ def test_mixed_nonfinite_status():
     assert r["status"][1] == cg.CG_ERR_NONFINITE
 
 
+def test_bounded_wait_reports_timeout_and_context_survives():
+    """A device wait on a barrier that nothing completes gives up within its limit and reports
+    CG_ERR_TIMEOUT (no fault, no hang); the same context then evaluates normally, and a
+    timeout is reported on its own call only."""
+    g = load_golden("nside4")
+    B = len(g["cls"])
+    with _ctx(g, "mixed", B) as ctx:
+        assert ctx.selftest_wait_timeout() == cg.CG_ERR_TIMEOUT
+        r = ctx.loglike(g["cls"], g["d"])
+        assert ctx.selftest_wait_timeout() == cg.CG_ERR_TIMEOUT
+        r2 = ctx.loglike(g["cls"], g["d"])
+    for res in (r, r2):
+        assert np.all(res["status"] == 0)
+        assert np.abs(res["m2lnl"] - g["m2lnl"]).max() <= TOL_M2LNL
+
+
 def test_mixed_against_oracle_nside16(oracle_mod):
     """Two elements of an nside-16 batch straight against the CPU oracle (FP64)."""
     g = load_golden("nside16_lmax47")
