@@ -306,8 +306,12 @@ def run_ours(args):
         chol_flops = B * n ** 3 / 3.0
         roof = {"kernel": "tensor-core Cholesky (chol_tc_update + chol_tc_panel, 3xTF32 tcgen05)",
                 "bound": "tensor", "achieved": chol_flops / (stages["cholesky"] * 1e-3) / 1e12, "peak": peak3,
-                "unit": "TFLOP/s", "traffic": None, "algorithmic_flops": chol_flops,
-                "peak_note": "measured bf16 sustained / 6 (TF32 = bf16 / 2, three MMAs per product)"}
+                "unit": "TFLOP/s", "algorithmic_flops": chol_flops,
+                "peak_note": "measured bf16 sustained / 6 (TF32 = bf16 / 2, three MMAs per product)",
+                # ncu dram__bytes_read + dram__bytes_write of all 39 Cholesky launches of one batch-32
+                # step, x B / 32 (traffic grows with the batch): profiles/tc_kernels_nside16_b32.md
+                "traffic": 5.198e9 * B / 32.0 if args.workload == WORKLOAD else None,
+                "traffic_unit": "bytes per step (whole Cholesky stage)"}
         roof["frac"] = roof["achieved"] / roof["peak"]
         # the forward contraction A_b = I + sum_l eps_bl Ubar_l: reads the FP32 table once
         # (tiles x 4096 x lpad x 4 B) and writes A (B x tiles x 4096 x 4 B)

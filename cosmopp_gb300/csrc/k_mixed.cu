@@ -365,32 +365,33 @@ __global__ void broadcast_vec(int B, int N, const double* __restrict__ y, double
 //                    diagonal, 1 on it, 0 above it (the tiles hold the lower triangle);
 //   x^T Ubar_l x   = cref_l |Z_l^T x|^2, Ubar_l = cref_l Z_l Z_l^T (Z_l: the 2l+1 rows of Z).
 
-// part[t][b][l] = sum_{e in tile t} w_e V_b[t][e] Ubar[t][l][e]: one CTA per tile and 256 batch
-// elements (the tile's table block is read once per 48 l); grid (tiles, ceil(B / 256),
-// ceil(lp / 48)).  Thread (bg = t % 32, lg = t / 32) holds batch elements bg + 32 a (a < 8) and
-// l = lbase + 6 lg .. + 5.  V chunks are staged [b][entry] with row
+// part[t][b][l] = sum_{e in tile t} w_e V_b[t][e] Ubar[t][l][e]: one CTA per tile and 32 NA batch
+// elements (the tile's table block is read once per 48 l); grid (tiles, ceil(B / (32 NA)),
+// ceil(lp / 48)).  Thread (bg = t % 32, lg = t / 32) holds batch elements bg + 32 a (a < NA) and
+// l = lbase + 6 lg .. + 5.  NA = 8 for large batches, 2 when B <= 64.  V chunks are staged [b][entry] with row
 // stride ADJ_LD (16-byte rows; the 8 lanes of each 128-bit phase hit different banks).
 constexpr int ADJ_KE = 64;       // entries per chunk
 constexpr int ADJ_LD = ADJ_KE + 4;
+template <int NA>
 __global__ void __launch_bounds__(256, 2) contract_adj(int B, int lp, const float* __restrict__ U,
                                                        const float* __restrict__ V, size_t strideA,
                                                        float* __restrict__ part)
 {
     extern __shared__ float asm_[];
-    float* sV = asm_;                      // [256][ADJ_LD]
-    float* sU = asm_ + 256 * ADJ_LD;       // [48][ADJ_KE]
-    const int t = blockIdx.x, b_begin = blockIdx.y * 256, lbase = 48 * blockIdx.z;
+    float* sV = asm_;                      // [32 NA][ADJ_LD]
+    float* sU = asm_ + 32 * NA * ADJ_LD;   // [48][ADJ_KE]
+    const int t = blockIdx.x, b_begin = blockIdx.y * 32 * NA, lbase = 48 * blockIdx.z;
     int I, J;
     tile_coords(t, I, J);
     const int bg = threadIdx.x % 32, lg = threadIdx.x / 32, l0 = 6 * lg;
-    float acc[8][6];
+    float acc[NA][6];
 #pragma unroll
-    for (int a = 0; a < 8; ++a)
+    for (int a = 0; a < NA; ++a)
 #pragma unroll
         for (int q = 0; q < 6; ++q) acc[a][q] = 0.f;
     const float* Ut = U + (size_t)t * TILE_ELEMS * lp;
     // batch rows present; staging skips the 32-row groups beyond them (their sums are never stored)
-    const int nrow = min(256, B - b_begin), na = (nrow + 31) / 32;
+    const int nrow = min(32 * NA, B - b_begin), na = (nrow + 31) / 32;
     for (int e0 = 0; e0 < TILE_ELEMS; e0 += ADJ_KE) {
         __syncthreads();
         // V: up to 256 rows x 64 entries, 16 threads per row (coalesced), weights applied
@@ -420,15 +421,15 @@ __global__ void __launch_bounds__(256, 2) contract_adj(int B, int lp, const floa
         __syncthreads();
 #pragma unroll 2
         for (int e4 = 0; e4 < ADJ_KE / 4; ++e4) {
-            float4 v[8], u4[6];
+            float4 v[NA], u4[6];
 #pragma unroll
-            for (int a = 0; a < 8; ++a) v[a] = *reinterpret_cast<const float4*>(&sV[(bg + 32 * a) * ADJ_LD + 4 * e4]);
+            for (int a = 0; a < NA; ++a) v[a] = *reinterpret_cast<const float4*>(&sV[(bg + 32 * a) * ADJ_LD + 4 * e4]);
 #pragma unroll
             for (int q = 0; q < 6; ++q) u4[q] = *reinterpret_cast<const float4*>(&sU[(l0 + q) * ADJ_KE + 4 * e4]);
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
 #pragma unroll
-                for (int a = 0; a < 8; ++a) {
+                for (int a = 0; a < NA; ++a) {
                     const float va = (j == 0) ? v[a].x : (j == 1) ? v[a].y : (j == 2) ? v[a].z : v[a].w;
 #pragma unroll
                     for (int q = 0; q < 6; ++q) {
@@ -440,7 +441,7 @@ __global__ void __launch_bounds__(256, 2) contract_adj(int B, int lp, const floa
         }
     }
 #pragma unroll
-    for (int a = 0; a < 8; ++a) {
+    for (int a = 0; a < NA; ++a) {
         const int b = b_begin + bg + 32 * a;
         if (b >= B) continue;
 #pragma unroll
@@ -754,9 +755,15 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
     count_launch(ctx, 7);
     stage_mark(ctx, ST_ADJOINT, s);
     if (d_grad) {
-        const size_t sma = sizeof(float) * (256 * ADJ_LD + 48 * ADJ_KE);
-        CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma));
-        contract_adj<<<dim3(ntile, (B + 255) / 256, (lp + 47) / 48), 256, sma, s>>>(B, lp, w.U, w.V, tiled, w.gpart);
+        if (B <= 64) {
+            const size_t sma = sizeof(float) * (64 * ADJ_LD + 48 * ADJ_KE);
+            CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_adj<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma));
+            contract_adj<2><<<dim3(ntile, (B + 63) / 64, (lp + 47) / 48), 256, sma, s>>>(B, lp, w.U, w.V, tiled, w.gpart);
+        } else {
+            const size_t sma = sizeof(float) * (256 * ADJ_LD + 48 * ADJ_KE);
+            CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_adj<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma));
+            contract_adj<8><<<dim3(ntile, (B + 255) / 256, (lp + 47) / 48), 256, sma, s>>>(B, lp, w.U, w.V, tiled, w.gpart);
+        }
         const int nhp = nharm_pad(lmax);
         project_x<<<dim3(nhp / 64, (B + 63) / 64), 256, 0, s>>>(B, N, nhp, w.Zf, w.x, w.proj);
         adj_finish<<<B, 64, 0, s>>>(B, ntile, lmax, lp, nhp, w.gpart, w.proj, w.cref, d_grad);
