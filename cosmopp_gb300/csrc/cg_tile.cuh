@@ -87,6 +87,9 @@ __device__ __forceinline__ void df_add(float& hi, float& lo, float v)
     hi = t;
 }
 
+// One CTA walks SYMV_TPB consecutive tiles of one batch element: 128-bit loads, the next tile
+// prefetched into registers while the current one is reduced.  grid (ceil(tiles / SYMV_TPB), B).
+constexpr int SYMV_TPB = 8;
 template <bool DF>
 __global__ void __launch_bounds__(256) symv_partials(int nt, const float* __restrict__ V, size_t strideA,
                                                      const double* __restrict__ v, int vstride,
@@ -95,46 +98,68 @@ __global__ void __launch_bounds__(256) symv_partials(int nt, const float* __rest
     __shared__ float s[TS][TS + 1];
     __shared__ float svh[2][TS], svl[2][TS];
     __shared__ double red[4][2][TS];
-    int I, J;
-    tile_coords(blockIdx.x, I, J);
     const int b = blockIdx.y, ntile = ntiles_lower(nt);
-    const float* tile = V + (size_t)b * strideA + (size_t)blockIdx.x * TILE_ELEMS;
-    for (int e = threadIdx.x; e < TILE_ELEMS; e += blockDim.x) s[e / TS][e % TS] = tile[e];  // s[c][r]
-    if (threadIdx.x < 2 * TS) {
-        const int w = threadIdx.x / TS, k = threadIdx.x % TS;
-        const double x = v[(size_t)b * vstride + (w == 0 ? J : I) * TS + k];
-        const float h = (float)x;
-        svh[w][k] = h;
-        svl[w][k] = (float)(x - (double)h);
-    }
-    __syncthreads();
+    const int t0 = blockIdx.x * SYMV_TPB;
+    const int tn = min(SYMV_TPB, ntile - t0);
+    const float* base = V + (size_t)b * strideA;
+    // thread's share of a tile: float4 k at element 4 (threadIdx.x + 256 k), k < 4
+    auto load = [&](int t, float4 (&d)[4]) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            d[k] = __ldg(reinterpret_cast<const float4*>(base + (size_t)t * TILE_ELEMS + 4 * (threadIdx.x + 256 * k)));
+    };
+    float4 cur[4], nxt[4];
+    load(t0, cur);
     const int r = threadIdx.x % TS, q = threadIdx.x / TS;
-    float ah = 0.f, al = 0.f, th = 0.f, tl = 0.f;
-    for (int c = q; c < TS; c += 4) {
-        const float va = s[c][r], vt = s[r][c];
-        if (DF) {
-            const float p = va * svh[0][c];
-            df_add(ah, al, p);
-            al += fmaf(va, svh[0][c], -p) + va * svl[0][c];
-            const float pt = vt * svh[1][c];
-            df_add(th, tl, pt);
-            tl += fmaf(vt, svh[1][c], -pt) + vt * svl[1][c];
-        } else {
-            ah = fmaf(va, svh[0][c], ah);
-            th = fmaf(vt, svh[1][c], th);
+    for (int i = 0; i < tn; ++i) {
+        const int t = t0 + i;
+        int I, J;
+        tile_coords(t, I, J);
+        if (i + 1 < tn) load(t + 1, nxt);
+        __syncthreads();  // the previous tile's shared-memory reads are done
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int e = 4 * (threadIdx.x + 256 * k);  // s[c][r] = tile(r, c), e = r + TS c
+            const float w[4] = {cur[k].x, cur[k].y, cur[k].z, cur[k].w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) s[(e + j) / TS][(e + j) % TS] = w[j];
         }
-    }
-    red[q][0][r] = (double)ah + (double)al;
-    red[q][1][r] = (double)th + (double)tl;
-    __syncthreads();
-    if (q == 0) {
-        double* p = part + ((size_t)b * ntile + blockIdx.x) * 2 * TS;
-        p[r] = ((red[0][0][r] + red[1][0][r]) + red[2][0][r]) + red[3][0][r];
-        p[TS + r] = (I != J) ? ((red[0][1][r] + red[1][1][r]) + red[2][1][r]) + red[3][1][r] : 0.0;
+        if (threadIdx.x < 2 * TS) {
+            const int w = threadIdx.x / TS, k = threadIdx.x % TS;
+            const double x = v[(size_t)b * vstride + (w == 0 ? J : I) * TS + k];
+            const float h = (float)x;
+            svh[w][k] = h;
+            svl[w][k] = (float)(x - (double)h);
+        }
+        __syncthreads();
+        float ah = 0.f, al = 0.f, th = 0.f, tl = 0.f;
+        for (int c = q; c < TS; c += 4) {
+            const float va = s[c][r], vt = s[r][c];
+            if (DF) {
+                const float p = va * svh[0][c];
+                df_add(ah, al, p);
+                al += fmaf(va, svh[0][c], -p) + va * svl[0][c];
+                const float pt = vt * svh[1][c];
+                df_add(th, tl, pt);
+                tl += fmaf(vt, svh[1][c], -pt) + vt * svl[1][c];
+            } else {
+                ah = fmaf(va, svh[0][c], ah);
+                th = fmaf(vt, svh[1][c], th);
+            }
+        }
+        red[q][0][r] = (double)ah + (double)al;
+        red[q][1][r] = (double)th + (double)tl;
+        __syncthreads();
+        if (q == 0) {
+            double* p = part + ((size_t)b * ntile + t) * 2 * TS;
+            p[r] = ((red[0][0][r] + red[1][0][r]) + red[2][0][r]) + red[3][0][r];
+            p[TS + r] = (I != J) ? ((red[0][1][r] + red[1][1][r]) + red[2][1][r]) + red[3][1][r] : 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) cur[k] = nxt[k];
     }
 }
 
-// out[b][I*TS + r] = scale_out * sum + add[b][..] (add nullable)
 static __global__ void __launch_bounds__(64) symv_reduce(int nt, const double* __restrict__ part, double* __restrict__ out,
                                                   int ostride, const double* __restrict__ add, double sign)
 {

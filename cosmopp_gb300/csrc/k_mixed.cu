@@ -745,11 +745,11 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
     if ((rc = tiled_lauum_tc(ctx, B, nt, w.Ms, w.V, w.tcerr, s))) return rc;
     stage_mark(ctx, ST_SOLVE, s);
     // x = V y; r = y - A x; x += V r
-    symv_partials<false><<<dim3(ntile, B), 256, 0, s>>>(nt, w.V, tiled, w.y, N, w.part);
+    symv_partials<false><<<dim3((ntile + SYMV_TPB - 1) / SYMV_TPB, B), 256, 0, s>>>(nt, w.V, tiled, w.y, N, w.part);
     symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, w.part, w.x, N, nullptr, 1.0);
-    symv_partials<true><<<dim3(ntile, B), 256, 0, s>>>(nt, w.A, tiled, w.x, N, w.part);
+    symv_partials<true><<<dim3((ntile + SYMV_TPB - 1) / SYMV_TPB, B), 256, 0, s>>>(nt, w.A, tiled, w.x, N, w.part);
     symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, w.part, w.r, N, w.y, -1.0);
-    symv_partials<false><<<dim3(ntile, B), 256, 0, s>>>(nt, w.V, tiled, w.r, N, w.part);
+    symv_partials<false><<<dim3((ntile + SYMV_TPB - 1) / SYMV_TPB, B), 256, 0, s>>>(nt, w.V, tiled, w.r, N, w.part);
     symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, w.part, w.x, N, w.x, 1.0);
     chi2_mixed<<<B, 256, 0, s>>>(n, N, N, w.y, w.x, w.ld, d_m2lnl, d_chi2, d_logdet);
     count_launch(ctx, 7);

@@ -64,8 +64,10 @@ constexpr uint32_t LBO = 128, SBO = KC / 4 * 128;
 constexpr uint32_t IDESC = idesc_tf32(128, 128);
 constexpr int NPROD = 256;                      // A producers (warps 0-7)
 constexpr int NTH = NPROD + 64;                 // + the MMA warp and the copy warp
-constexpr int NSTB = 5;                         // B stages (bulk copies run NSTB - 2 chunks ahead)
+constexpr int NSTB = 4;                         // B stages in shared memory
 constexpr uint32_t STB_BYTES = 2u * 128 * KC * 4;  // one B stage: hi + lo, 128 rows x 32 K (32 KB)
+constexpr int NSTA = 4;                         // A stages in shared memory (FP32 canonical chunks)
+constexpr uint32_t STA_BYTES = 128u * KC * 4;   // one A stage: 128 rows x 32 K FP32 (16 KB)
 constexpr int SC_PLANE = TS * TS;               // floats per plane of an SC tile
 constexpr int SC_CHUNK = TS * KC;               // floats per 64 x 32 block
 constexpr int SC_TILE = 2 * SC_PLANE;           // floats per SC tile (32 KB)
@@ -82,7 +84,9 @@ __device__ __align__(128) float g_zero_block[SC_CHUNK];
 __device__ __forceinline__ int canon_off(int r, int k) { return (r >> 3) * 256 + (k >> 2) * 32 + (r & 7) * 4 + (k & 3); }
 
 // Tensor-memory columns (512): hi*hi accumulators for the two chunk parities, the correction
-// accumulator, and the A operand (hi, lo) of the two stages.
+// accumulator, and the A operand (hi, lo) of the two stages.  Keeping the corrections in their
+// own accumulator also gives the tensor pipe two independent accumulation chains to interleave
+// (one accumulator for all 12 MMAs of a chunk measured 8% slower).
 constexpr uint32_t TMEM_COLS = 512;
 constexpr uint32_t COL_CORR = 256;
 __device__ __forceinline__ uint32_t col_main(int set) { return 128u * set; }
@@ -109,6 +113,8 @@ struct TcCtl {
     uint64_t a_full[2];       // chunk parity: the chunk's A is in tensor memory (one arrival per producer warp)
     uint64_t b_full[NSTB];    // B stage landed
     uint64_t b_empty[NSTB];   // B stage's MMAs completed
+    uint64_t as_full[NSTA];   // A shared-memory stage landed
+    uint64_t as_empty[NSTA];  // A shared-memory stage read by every producer warp
     uint32_t tbase;
     int bad;
 };
@@ -122,6 +128,10 @@ __device__ __forceinline__ void init_bars(TcCtl& ctl)
     for (int i = 0; i < NSTB; ++i) {
         mbar_init(&ctl.b_full[i], 1);
         mbar_init(&ctl.b_empty[i], 1);
+    }
+    for (int i = 0; i < NSTA; ++i) {
+        mbar_init(&ctl.as_full[i], 1);
+        mbar_init(&ctl.as_empty[i], NPROD / 32);
     }
     fence_mbar_init();
 }
@@ -151,8 +161,9 @@ __device__ __forceinline__ void tc_rearm(TcCtl& ctl)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
-        uint64_t* all = &ctl.mma_bar[0];  // mma_bar, a_full, b_full, b_empty are contiguous
-        for (int i = 0; i < 4 + 2 * NSTB; ++i) asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(all + i)));
+        uint64_t* all = &ctl.mma_bar[0];  // mma_bar, a_full, b_full, b_empty, as_full, as_empty are contiguous
+        for (int i = 0; i < 4 + 2 * NSTB + 2 * NSTA; ++i)
+            asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(all + i)));
         init_bars(ctl);
     }
     __syncthreads();
@@ -222,6 +233,17 @@ __device__ __forceinline__ void bulk_linv(const float* li, int kc, uint32_t dst,
     bulk_g2s(dst + STB_BYTES / 2, li + kc * LI_CHUNK + LI_CHUNK / 2, STB_BYTES / 2, bar);
 }
 
+// A operand of one chunk from two stacked FP32 canonical tiles (rows 0-63: top, 64-127: bot;
+// nullptr = zero) into an A stage
+__device__ __forceinline__ void bulk_a_c1(const float* top, const float* bot, int kc, uint32_t dst, uint64_t* bar)
+{
+    mbar_arrive_expect_tx(bar, STA_BYTES);
+    const float* z = g_zero_block;
+    const uint32_t blk = SC_CHUNK * 4;
+    bulk_g2s(dst, top ? top + kc * SC_CHUNK : z, blk, bar);
+    bulk_g2s(dst + blk, bot ? bot + kc * SC_CHUNK : z, blk, bar);
+}
+
 // split row rr (K values v[0..63] times sgn) into a split canonical store: element (rr, k) at
 // base + (k / 32) * chunk_stride + plane * plane_stride + canon_off(rr, k % 32)
 __device__ __forceinline__ void st_split_row(float* base, int chunk_stride, int plane_stride, int rr,
@@ -261,15 +283,20 @@ __device__ __forceinline__ void st_c1_row(float* tile, int rr, const float (&v)[
 
 // ---- the K loop --------------------------------------------------------------
 
-// nchunks chunks; fa(c, r, h, x) loads the A chunk (row r, K half h): with SPLIT, x[4] holds FP32
-// values that are split into hi and lo when stored to tensor memory; without, x[8] holds hi
-// (x[0..3]) and lo (x[4..7]) as loaded; fb(c, dst, bar) issues
-// the B chunk's bulk copies into shared memory at dst.  Called by every thread of the CTA.  On
-// return the producer threads (t < NPROD) hold in R[j] the product for row t % 128, column
-// 64 (t / 128) + j (0 if nchunks == 0).  Returns false if an mbarrier wait gave up; waits give up
-// early once *err is set (by this or any other CTA), and a thread whose wait gave up skips its
-// later waits, so a failure ends the launch quickly.
-template <bool SPLIT, class FA, class FB>
+// How the A operand reaches the producers:
+//   A_REG_SC  fa(c, r, h, x[8]) loads row r, K half h of chunk c as hi (x[0..3]) and lo (x[4..7]);
+//   A_REG_C1  fa(c, r, h, x[4]) loads it as FP32, split when stored to tensor memory;
+//   A_SMEM_C1 fa(c, top, bot, kc) names the two FP32 canonical tiles (rows 0-63, 64-127; nullptr =
+//             zero) and the K chunk within them; the copy warp brings them into a ring of NSTA
+//             shared-memory stages by bulk copies, ahead of the producers.
+enum { A_REG_SC = 0, A_REG_C1 = 1, A_SMEM_C1 = 2 };
+
+// nchunks chunks; fb(c, dst, bar) issues the B chunk's bulk copies into shared memory at dst.
+// Called by every thread of the CTA.  On return the producer threads (t < NPROD) hold in R[j] the
+// product for row t % 128, column 64 (t / 128) + j (0 if nchunks == 0).  Returns false if an
+// mbarrier wait gave up; waits give up early once *err is set (by this or any other CTA), and a
+// thread whose wait gave up skips its later waits, so a failure ends the launch quickly.
+template <int AMODE, class FA, class FB>
 __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& ctl, uint32_t tm, float (&R)[64],
                          int* err)
 {
@@ -281,18 +308,32 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
         if (!ok) atomicExch(err, 1);
     };
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const uint32_t sb = smem_u32(sbuf);
+    const uint32_t sb = smem_u32(sbuf);                      // B ring
+    const uint32_t sa = sb + NSTB * STB_BYTES;               // A ring (A_SMEM_C1)
+    const float* sa_f = reinterpret_cast<const float*>(sbuf + NSTB * STB_BYTES);
 #pragma unroll
     for (int j = 0; j < 64; ++j) R[j] = 0.f;
     if (warp < NPROD / 32) {
         // ---- A producers: tensor-memory stage c & 1, then fold chunk c - 2's hi*hi sum
         const int r = threadIdx.x % 128, h = threadIdx.x / 128;
-        constexpr int NX = SPLIT ? 4 : 8;
+        constexpr int NX = (AMODE == A_REG_SC) ? 8 : 4;
         float4 a0[NX], a1[NX];
-        if (nchunks > 0) fa(0, r, h, a0);
-        if (nchunks > 1) fa(1, r, h, a1);
+        if constexpr (AMODE != A_SMEM_C1) {
+            if (nchunks > 0) fa(0, r, h, a0);
+            if (nchunks > 1) fa(1, r, h, a1);
+        }
         auto step = [&](int c, float4 (&qx)[NX]) {
             const int st = c & 1;
+            if constexpr (AMODE == A_SMEM_C1) {
+                // this thread's 16 values of the staged chunk (row r, K columns 16h .. 16h+15)
+                const int si = c % NSTA;
+                wait(&ctl.as_full[si], (c / NSTA) & 1);
+                const float* p = sa_f + si * (STA_BYTES / 4) + (r >> 3) * 256 + (r & 7) * 4 + 4 * h * 32;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) qx[i] = *reinterpret_cast<const float4*>(p + i * 32);
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&ctl.as_empty[si]);
+            }
             if (c >= 2) {  // chunk c-2's MMAs done: its A stage is free, its hi*hi sum goes to R
                 wait(&ctl.mma_bar[st], ((c - 2) >> 1) & 1);
                 fence_after();
@@ -300,19 +341,21 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
             }
             {
                 float4 qh[4], ql[4];
-                if constexpr (SPLIT) {
-                    split4(qx, qh, ql);
-                } else {
+                if constexpr (AMODE == A_REG_SC) {
 #pragma unroll
                     for (int i = 0; i < 4; ++i) {
                         qh[i] = qx[i];
                         ql[i] = qx[4 + i];
                     }
+                } else {
+                    split4(reinterpret_cast<const float4(&)[4]>(qx), qh, ql);
                 }
                 tmem_st16(tm + lane_base() + col_a_hi(st) + 16 * h, qh);
                 tmem_st16(tm + lane_base() + col_a_lo(st) + 16 * h, ql);
             }
-            if (c + 2 < nchunks) fa(c + 2, r, h, qx);
+            if constexpr (AMODE != A_SMEM_C1) {
+                if (c + 2 < nchunks) fa(c + 2, r, h, qx);
+            }
             tmem_wait_st();
             fence_before();
             __syncwarp();
@@ -348,9 +391,11 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
 #pragma unroll
                 for (int kk = 0; kk < KC / 8; ++kk) {
                     const uint32_t off = kk * 2 * LBO;
+                    // corrections and hi*hi alternate, so consecutive MMAs mostly update different
+                    // accumulators and can overlap in the tensor pipe
                     mma_tf32_ta(tm + COL_CORR, al + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, (c | kk) ? 1u : 0u);
-                    mma_tf32_ta(tm + COL_CORR, ah + 8 * kk, smem_desc(bl + off, LBO, SBO), IDESC, 1u);
                     mma_tf32_ta(tm + col_main(st), ah + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, kk ? 1u : 0u);
+                    mma_tf32_ta(tm + COL_CORR, ah + 8 * kk, smem_desc(bl + off, LBO, SBO), IDESC, 1u);
                 }
                 mma_commit(&ctl.mma_bar[st]);
                 mma_commit(&ctl.b_empty[sbi]);
@@ -358,9 +403,17 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
         }
         __syncwarp();
     } else {
-        // ---- B copies: one thread keeps the ring of NSTB stages full
+        // ---- copies: one thread keeps the B ring (and, for A_SMEM_C1, the A ring) full
         if (lane == 0) {
             for (int c = 0; c < nchunks; ++c) {
+                if constexpr (AMODE == A_SMEM_C1) {
+                    const int si = c % NSTA;
+                    if (c >= NSTA) wait(&ctl.as_empty[si], ((c / NSTA) - 1) & 1);
+                    const float *top, *bot;
+                    int kc;
+                    fa(c, top, bot, kc);
+                    bulk_a_c1(top, bot, kc, sa + si * STA_BYTES, &ctl.as_full[si]);
+                }
                 const int sbi = c % NSTB;
                 if (c >= NSTB) wait(&ctl.b_empty[sbi], ((c / NSTB) - 1) & 1);
                 fb(c, sb + sbi * STB_BYTES, &ctl.b_full[sbi]);
@@ -574,15 +627,17 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
     float* Lcb = Lc + (size_t)b * ntile * C1_TILE;
     const uint32_t tm = tc_begin(ctl);
     const int nchunks = 2 * J2 * (TS / KC);
-    auto fa = [&](int c, int r, int h, float4 (&x)[4]) {
-        ld_c1<false>(Lcb + (size_t)tile_index(2 * I2 + r / 64, c / 2) * C1_TILE, r % 64, c % 2, h, x);
+    auto fa = [&](int c, const float*& top, const float*& bot, int& kc) {
+        top = Lcb + (size_t)tile_index(2 * I2, c / 2) * C1_TILE;
+        bot = Lcb + (size_t)tile_index(2 * I2 + 1, c / 2) * C1_TILE;
+        kc = c % 2;
     };
     auto fb = [&](int c, uint32_t dst, uint64_t* bar) {
         bulk_tiles(Lb + (size_t)tile_index(2 * J2, c / 2) * SC_TILE, Lb + (size_t)tile_index(2 * J2 + 1, c / 2) * SC_TILE,
                    c % 2, dst, bar);
     };
     float R[64];
-    tc_kloop<true>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
+    tc_kloop<A_SMEM_C1>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
     const int row = threadIdx.x % 128, h = threadIdx.x / 128;
     const bool prod = threadIdx.x < NPROD;
     if (I2 > J2) {
@@ -657,12 +712,14 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_panel(int J2, int nt, float* _
     const float* li = Linv + ((size_t)b * nt2 + J2) * LINV_SC;
     const uint32_t tm = tc_begin(ctl);
     // A(r, m) = S_IJ(r, m), C1 tiles (2 I2 + r/64, 2 J2 + m/64); B(c, m) = Linv_J(c, m)
-    auto fa = [&](int c, int r, int h, float4 (&x)[4]) {
-        ld_c1<false>(Lcb + (size_t)tile_index(2 * I2 + r / 64, 2 * J2 + c / 2) * C1_TILE, r % 64, c % 2, h, x);
+    auto fa = [&](int c, const float*& top, const float*& bot, int& kc) {
+        top = Lcb + (size_t)tile_index(2 * I2, 2 * J2 + c / 2) * C1_TILE;
+        bot = Lcb + (size_t)tile_index(2 * I2 + 1, 2 * J2 + c / 2) * C1_TILE;
+        kc = c % 2;
     };
     auto fb = [&](int c, uint32_t dst, uint64_t* bar) { bulk_linv(li, c, dst, bar); };
     float R[64];
-    tc_kloop<true>(128 / KC, fa, fb, smem_raw, ctl, tm, R, err);
+    tc_kloop<A_SMEM_C1>(128 / KC, fa, fb, smem_raw, ctl, tm, R, err);
     __syncthreads();  // every S read is done before the tiles are overwritten
     const int row = threadIdx.x % 128, h = threadIdx.x / 128;
     if (threadIdx.x < NPROD) {
@@ -693,10 +750,11 @@ __global__ void __launch_bounds__(NTH, 1) trtri_tc_row(int I2, int nt, const flo
     // B(r, m) = L_Ik(r, m): SC tiles (2 I2, k), (2 I2 + 1, k)
     const int k0 = 2 * J2;
     const int nchunks = (2 * I2 - k0) * (TS / KC);
-    auto fa = [&](int c, int r, int hh, float4 (&x)[4]) {
-        const int k = k0 + c / 2, col = 2 * J2 + r / 64;
-        if (k < col) zero4(x);
-        else ld_c1<false>(Mcb + (size_t)tile_index(k, col) * C1_TILE, r % 64, c % 2, hh, x);
+    auto fa = [&](int c, const float*& top, const float*& bot, int& kc) {
+        const int k = k0 + c / 2;
+        top = (k >= 2 * J2) ? Mcb + (size_t)tile_index(k, 2 * J2) * C1_TILE : nullptr;
+        bot = (k >= 2 * J2 + 1) ? Mcb + (size_t)tile_index(k, 2 * J2 + 1) * C1_TILE : nullptr;
+        kc = c % 2;
     };
     auto fb = [&](int c, uint32_t dst, uint64_t* bar) {
         const int k = k0 + c / 2;
@@ -704,7 +762,7 @@ __global__ void __launch_bounds__(NTH, 1) trtri_tc_row(int I2, int nt, const flo
                    c % 2, dst, bar);
     };
     float R[64];
-    tc_kloop<true>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
+    tc_kloop<A_SMEM_C1>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
     // S^T into the M storage of block (I2, J2): row = M's column, K = M's rows 64h .. 64h+63
     if (threadIdx.x < NPROD)
         st_c1_row(Mcb + (size_t)tile_index(2 * I2 + h, 2 * J2 + row / 64) * C1_TILE, row % 64, R, 1.f);
@@ -714,7 +772,7 @@ __global__ void __launch_bounds__(NTH, 1) trtri_tc_row(int I2, int nt, const flo
         ld_c1<true>(Mcb + (size_t)tile_index(2 * I2 + c / 2, 2 * J2 + r / 64) * C1_TILE, r % 64, c % 2, hh, x);
     };
     auto fb2 = [&](int c, uint32_t dst, uint64_t* bar) { bulk_linv(li, c, dst, bar); };
-    tc_kloop<true>(128 / KC, fa2, fb2, smem_raw, ctl, tm, R, err);
+    tc_kloop<A_REG_C1>(128 / KC, fa2, fb2, smem_raw, ctl, tm, R, err);
     __syncthreads();  // every S^T read is done before the tiles are overwritten
     if (threadIdx.x < NPROD) {
         const size_t tix = tile_index(2 * I2 + h, 2 * J2 + row / 64);
@@ -764,7 +822,7 @@ __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restri
         bulk_tiles(top, bot, c % 2, dst, bar);
     };
     float R[64];
-    tc_kloop<false>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
+    tc_kloop<A_REG_SC>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
     store_block(R, V + (size_t)b * ntile * TILE_ELEMS, I2, J2, 1.f);
     tc_end(tm);
 }
@@ -786,7 +844,7 @@ __global__ void wait_timeout_probe(int* status)
 static int tc_smem()
 {
     const int fac = (2 * 128 * 129 + 64 * 65) * (int)sizeof(float);  // block, its inverse, scratch
-    const int ring = NSTB * (int)STB_BYTES;
+    const int ring = NSTB * (int)STB_BYTES + NSTA * (int)STA_BYTES;
     return (ring > fac ? ring : fac) + 1024;
 }
 
