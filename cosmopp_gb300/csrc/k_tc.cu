@@ -4,11 +4,9 @@
 // and a_lo = a - a_hi rounded to nearest TF32 (unbiased; truncating instead
 // biases sums of squares).  The tensor core's FP32 accumulation is not
 // round-to-nearest and drifts by ~0.4 ulp per instruction, always the same
-// way, so each chunk's hi*hi products (4 MMAs) go to a fresh tensor-memory
+// way, so each chunk's 12 MMAs (K = 32) go to a fresh tensor-memory
 // accumulator that is folded into a per-thread FP32 register sum
-// (round-to-nearest) one chunk later.  The correction products (8 MMAs per
-// chunk) are ~2^-11 of the sum, so their drift is negligible and they
-// accumulate in one tensor-memory accumulator over the whole K loop.
+// (round-to-nearest) two chunks later: the drift stays bounded by one chunk's.
 //
 // Operand storage ("split canonical", SC): every factor these kernels consume
 // is stored already split, hi and lo planes, each 64-row x 32-K block in the
@@ -24,16 +22,19 @@
 // One CTA owns a 128x128 output supertile (2x2 storage tiles) and runs a
 // warp-specialised K loop over 32-wide chunks, the roles handing off through
 // mbarriers only:
-//   warps 0-7  (A producers): thread t loads row t % 128, K half t / 128 of the A
-//              chunk two chunks ahead into registers, stores it into one of two
-//              tensor-memory stages once the MMAs that last read that stage are
-//              done, and folds the finished hi*hi accumulator into its registers;
-//   warp 8     (MMA issue): one thread issues the 12 MMAs (M128 N128 K8, A from
-//              tensor memory, B from shared memory) of each chunk as soon as its A
-//              and B are in place, and commits them to the chunk's mbarriers; the
-//              tensor pipe throttles this thread, so it does nothing else;
-//   warp 9     (B copies): one thread keeps a ring of NSTB shared-memory stages
-//              filled with bulk copies, refilling a stage when its MMAs are done.
+//   warps 0-7  (producers): when chunk c's MMAs are done, fold its accumulator
+//              into registers and release it, then store the A operand of chunk
+//              c + 4 into the tensor-memory stage chunk c used (four stages);
+//              thread t handles row t % 128, K half t / 128;
+//   warps 8,10 (MMA issue): one thread each, for the even and the odd chunks,
+//              issues the chunk's 12 MMAs (M128 N128 K8, A from tensor memory, B
+//              from shared memory) once its A, its B and its accumulator are ready,
+//              and commits them to the chunk's mbarriers.  Issue blocks while the
+//              tensor pipe is busy, so with one issuer the pipe idled during every
+//              barrier wait; with two, one issuer waits while the other's MMAs run;
+//   warp 9     (copies): one thread keeps a ring of NSTB shared-memory B stages
+//              (and NSTA A stages, for A streamed through shared memory) filled
+//              with bulk copies, refilling a stage when its readers are done.
 //
 //   chol_tc_update: left-looking Cholesky, column block J: S_IJ = A_IJ - sum_{k<J} L_Ik L_Jk^T;
 //                   the diagonal CTA factors S_JJ = L_JJ L_JJ^T, inverts L_JJ in shared memory and
@@ -62,8 +63,9 @@ namespace {
 constexpr int KC = 32;                          // K columns per chunk
 constexpr uint32_t LBO = 128, SBO = KC / 4 * 128;
 constexpr uint32_t IDESC = idesc_tf32(128, 128);
-constexpr int NPROD = 256;                      // A producers (warps 0-7)
-constexpr int NTH = NPROD + 64;                 // + the MMA warp and the copy warp
+constexpr int NPROD = 256;                      // producers (warps 0-7)
+constexpr int NTH = NPROD + 96;                 // + the MMA issuers (warps 8, 10) and the copy warp (9)
+constexpr int NAST = 4;                         // A stages in tensor memory
 constexpr int NSTB = 4;                         // B stages in shared memory
 constexpr uint32_t STB_BYTES = 2u * 128 * KC * 4;  // one B stage: hi + lo, 128 rows x 32 K (32 KB)
 constexpr int NSTA = 4;                         // A stages in shared memory (FP32 canonical chunks)
@@ -83,15 +85,12 @@ __device__ __align__(128) float g_zero_block[SC_CHUNK];
 // float offset of element (r, k) inside one canonical block (r < 128, k < 32)
 __device__ __forceinline__ int canon_off(int r, int k) { return (r >> 3) * 256 + (k >> 2) * 32 + (r & 7) * 4 + (k & 3); }
 
-// Tensor-memory columns (512): hi*hi accumulators for the two chunk parities, the correction
-// accumulator, and the A operand (hi, lo) of the two stages.  Keeping the corrections in their
-// own accumulator also gives the tensor pipe two independent accumulation chains to interleave
-// (one accumulator for all 12 MMAs of a chunk measured 8% slower).
+// Tensor-memory columns (512): the accumulators of the two chunk parities and the A operand
+// (hi, lo) of the four stages
 constexpr uint32_t TMEM_COLS = 512;
-constexpr uint32_t COL_CORR = 256;
 __device__ __forceinline__ uint32_t col_main(int set) { return 128u * set; }
-__device__ __forceinline__ uint32_t col_a_hi(int st) { return 384u + 64u * st; }
-__device__ __forceinline__ uint32_t col_a_lo(int st) { return 384u + 64u * st + 32u; }
+__device__ __forceinline__ uint32_t col_a_hi(int st) { return 256u + 64u * st; }
+__device__ __forceinline__ uint32_t col_a_lo(int st) { return 256u + 64u * st + 32u; }
 
 // the accumulator row this thread holds in TMEM (warp w: lanes 32 (w % 4) .. + 31)
 __device__ __forceinline__ uint32_t lane_base() { return (uint32_t)(32 * ((threadIdx.x / 32) % 4)) << 16; }
@@ -109,8 +108,9 @@ __device__ __forceinline__ void drain(uint32_t tm, uint32_t col, float (&R)[64])
 }
 
 struct TcCtl {
-    uint64_t mma_bar[2];      // chunk parity: the chunk's MMAs completed (A stage free, hi*hi sum ready)
-    uint64_t a_full[2];       // chunk parity: the chunk's A is in tensor memory (one arrival per producer warp)
+    uint64_t mma_bar[2];      // chunk parity: the chunk's MMAs completed (A stage free, sum ready)
+    uint64_t acc_free[2];     // chunk parity: the accumulator was drained (one arrival per producer warp)
+    uint64_t a_full[NAST];    // A stage: the chunk's A is in tensor memory (one arrival per producer warp)
     uint64_t b_full[NSTB];    // B stage landed
     uint64_t b_empty[NSTB];   // B stage's MMAs completed
     uint64_t as_full[NSTA];   // A shared-memory stage landed
@@ -123,8 +123,9 @@ __device__ __forceinline__ void init_bars(TcCtl& ctl)
 {
     for (int i = 0; i < 2; ++i) {
         mbar_init(&ctl.mma_bar[i], 1);
-        mbar_init(&ctl.a_full[i], NPROD / 32);
+        mbar_init(&ctl.acc_free[i], NPROD / 32);
     }
+    for (int i = 0; i < NAST; ++i) mbar_init(&ctl.a_full[i], NPROD / 32);
     for (int i = 0; i < NSTB; ++i) {
         mbar_init(&ctl.b_full[i], 1);
         mbar_init(&ctl.b_empty[i], 1);
@@ -161,8 +162,8 @@ __device__ __forceinline__ void tc_rearm(TcCtl& ctl)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
-        uint64_t* all = &ctl.mma_bar[0];  // mma_bar, a_full, b_full, b_empty, as_full, as_empty are contiguous
-        for (int i = 0; i < 4 + 2 * NSTB + 2 * NSTA; ++i)
+        uint64_t* all = &ctl.mma_bar[0];  // every barrier of TcCtl, contiguous
+        for (int i = 0; i < 4 + NAST + 2 * NSTB + 2 * NSTA; ++i)
             asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(all + i)));
         init_bars(ctl);
     }
@@ -314,16 +315,13 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
 #pragma unroll
     for (int j = 0; j < 64; ++j) R[j] = 0.f;
     if (warp < NPROD / 32) {
-        // ---- A producers: tensor-memory stage c & 1, then fold chunk c - 2's hi*hi sum
+        // ---- producers
         const int r = threadIdx.x % 128, h = threadIdx.x / 128;
         constexpr int NX = (AMODE == A_REG_SC) ? 8 : 4;
-        float4 a0[NX], a1[NX];
-        if constexpr (AMODE != A_SMEM_C1) {
-            if (nchunks > 0) fa(0, r, h, a0);
-            if (nchunks > 1) fa(1, r, h, a1);
-        }
-        auto step = [&](int c, float4 (&qx)[NX]) {
-            const int st = c & 1;
+        float4 a0[NX], a1[NX];  // register modes: the loaded A of two chunks (slot = chunk & 1)
+        // chunk c's A (from qx, or for A_SMEM_C1 from the shared-memory ring) into tensor-memory stage c % NAST
+        auto put = [&](int c, float4 (&qx)[NX]) {
+            const int st = c % NAST;
             if constexpr (AMODE == A_SMEM_C1) {
                 // this thread's 16 values of the staged chunk (row r, K columns 16h .. 16h+15)
                 const int si = c % NSTA;
@@ -334,70 +332,87 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&ctl.as_empty[si]);
             }
-            if (c >= 2) {  // chunk c-2's MMAs done: its A stage is free, its hi*hi sum goes to R
-                wait(&ctl.mma_bar[st], ((c - 2) >> 1) & 1);
-                fence_after();
-                drain(tm, col_main(st), R);
-            }
-            {
-                float4 qh[4], ql[4];
-                if constexpr (AMODE == A_REG_SC) {
+            float4 qh[4], ql[4];
+            if constexpr (AMODE == A_REG_SC) {
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        qh[i] = qx[i];
-                        ql[i] = qx[4 + i];
-                    }
-                } else {
-                    split4(reinterpret_cast<const float4(&)[4]>(qx), qh, ql);
+                for (int i = 0; i < 4; ++i) {
+                    qh[i] = qx[i];
+                    ql[i] = qx[4 + i];
                 }
-                tmem_st16(tm + lane_base() + col_a_hi(st) + 16 * h, qh);
-                tmem_st16(tm + lane_base() + col_a_lo(st) + 16 * h, ql);
+            } else {
+                split4(reinterpret_cast<const float4(&)[4]>(qx), qh, ql);
             }
-            if constexpr (AMODE != A_SMEM_C1) {
-                if (c + 2 < nchunks) fa(c + 2, r, h, qx);
-            }
+            tmem_st16(tm + lane_base() + col_a_hi(st) + 16 * h, qh);
+            tmem_st16(tm + lane_base() + col_a_lo(st) + 16 * h, ql);
             tmem_wait_st();
             fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&ctl.a_full[st]);
         };
+        // chunks 0 and 1 into the empty stages 0 and 1; register modes load two chunks ahead of the store
+        if constexpr (AMODE != A_SMEM_C1) {
+            if (nchunks > 0) fa(0, r, h, a0);
+            if (nchunks > 1) fa(1, r, h, a1);
+        }
+        if (nchunks > 0) {
+            put(0, a0);
+            if constexpr (AMODE != A_SMEM_C1) { if (nchunks > 2) fa(2, r, h, a0); }
+        }
+        if (nchunks > 1) {
+            put(1, a1);
+            if constexpr (AMODE != A_SMEM_C1) { if (nchunks > 3) fa(3, r, h, a1); }
+        }
+        // step c: chunk c - 2's MMAs are done, so its accumulator is drained and released, and its
+        // A stage takes chunk c + 2 (held in slot qx = c & 1)
+        auto step = [&](int c, float4 (&qx)[NX]) {
+            if (c >= 2) {
+                wait(&ctl.mma_bar[c & 1], ((c - 2) >> 1) & 1);
+                fence_after();
+                drain(tm, col_main(c & 1), R);
+                fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&ctl.acc_free[c & 1]);
+            }
+            if (c + 2 < nchunks) {
+                put(c + 2, qx);
+                if constexpr (AMODE != A_SMEM_C1) { if (c + 4 < nchunks) fa(c + 4, r, h, qx); }
+            }
+        };
         for (int c = 0; c < nchunks; c += 2) {
             step(c, a0);
             if (c + 1 < nchunks) step(c + 1, a1);
         }
-        if (nchunks > 0) {
-            // every MMA is issued whatever happened, so the last commit always arrives: wait for it
-            // (bounded) even after a failure, so that no MMA still runs when tensor memory is freed
-            if (!mbar_wait(&ctl.mma_bar[(nchunks - 1) & 1], ((nchunks - 1) >> 1) & 1, kMaxIter)) {
+        // the last two chunks: every MMA is issued whatever happened, so their commits always arrive;
+        // wait for them (bounded) even after a failure, so that no MMA still runs when tensor memory
+        // is freed
+        for (int c = (nchunks >= 2 ? nchunks - 2 : 0); c < nchunks; ++c) {
+            if (!mbar_wait(&ctl.mma_bar[c & 1], (c >> 1) & 1, kMaxIter)) {
                 ok = false;
                 atomicExch(err, 1);
             }
             fence_after();
-            if (nchunks >= 2) drain(tm, col_main((nchunks - 2) & 1), R);
-            drain(tm, col_main((nchunks - 1) & 1), R);
-            drain(tm, COL_CORR, R);
-            fence_before();
+            drain(tm, col_main(c & 1), R);
         }
-    } else if (warp == NPROD / 32) {
-        // ---- MMA issue: one thread; the tensor pipe throttles it
+        fence_before();
+    } else if (warp == NPROD / 32 || warp == NPROD / 32 + 2) {
+        // ---- MMA issue: the even chunks from warp 8, the odd ones from warp 10
         if (lane == 0) {
-            for (int c = 0; c < nchunks; ++c) {
-                const int st = c & 1, sbi = c % NSTB;
-                wait(&ctl.a_full[st], (c >> 1) & 1);
+            for (int c = (warp == NPROD / 32) ? 0 : 1; c < nchunks; c += 2) {
+                const int st = c % NAST, sbi = c % NSTB;
+                wait(&ctl.a_full[st], (c / NAST) & 1);
                 wait(&ctl.b_full[sbi], (c / NSTB) & 1);
+                if (c >= 2) wait(&ctl.acc_free[c & 1], ((c - 2) >> 1) & 1);
                 fence_after();
                 const uint32_t bh = sb + sbi * STB_BYTES, bl = bh + STB_BYTES / 2;
-                const uint32_t ah = tm + col_a_hi(st), al = tm + col_a_lo(st);
+                const uint32_t ah = tm + col_a_hi(st), al = tm + col_a_lo(st), d = tm + col_main(c & 1);
 #pragma unroll
                 for (int kk = 0; kk < KC / 8; ++kk) {
                     const uint32_t off = kk * 2 * LBO;
-                    // corrections and hi*hi alternate, so consecutive MMAs mostly update different
-                    // accumulators and can overlap in the tensor pipe
-                    mma_tf32_ta(tm + COL_CORR, al + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, (c | kk) ? 1u : 0u);
-                    mma_tf32_ta(tm + col_main(st), ah + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, kk ? 1u : 0u);
-                    mma_tf32_ta(tm + COL_CORR, ah + 8 * kk, smem_desc(bl + off, LBO, SBO), IDESC, 1u);
+                    mma_tf32_ta(d, al + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, kk ? 1u : 0u);
+                    mma_tf32_ta(d, ah + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, 1u);
+                    mma_tf32_ta(d, ah + 8 * kk, smem_desc(bl + off, LBO, SBO), IDESC, 1u);
                 }
-                mma_commit(&ctl.mma_bar[st]);
+                mma_commit(&ctl.mma_bar[c & 1]);
                 mma_commit(&ctl.b_empty[sbi]);
             }
         }
