@@ -98,7 +98,7 @@ struct MixedWork {
     float* proj = nullptr;       // [cap][nharm_pad] Z^T x_b
     double* ld = nullptr;        // [cap] ln det C_b
     int* st = nullptr;           // [cap]
-    int* tcerr = nullptr;        // [1] set when a bounded tensor-core wait gave up
+    int* tcerr = nullptr;        // [1 + tc_queue_slots] tensor-core error flag and work-queue counters
 };
 
 }  // namespace cg
@@ -179,11 +179,15 @@ int tiled_lauum(cg_ctx* ctx, int B, int nt, const T* M, T* V, size_t strideA, cu
 size_t tc_split_elems(int nt);   // floats per matrix of the split (hi/lo) L / M^T storage
 size_t tc_c1_elems(int nt);      // floats per matrix of the FP32 canonical L / M^T copies
 size_t tc_linv_elems(int nt);    // floats per matrix of the Linv blocks
+// The tensor-core entry points take d_err = [0] the error flag (set when a bounded wait gave up),
+// then tc_queue_slots(nt) work-queue counters, all zero before the call.
+int tc_queue_slots(int nt);
 int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, float* Lc, float* Linv, float* Ms,
                       float* Mc, float* diag, int* status, int* d_err, cudaStream_t s);
 int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* Ls, const float* Linv, float* Ms, float* Mc,
                    int* d_err, cudaStream_t s);
-int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, float* V, int* d_err, cudaStream_t s);
+int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, const float* Mc, float* V, int* d_err,
+                   cudaStream_t s);
 int selftest_wait_timeout(cg_ctx* ctx, int* host_status);
 // mixed path (k_mixed.cu)
 int mixed_prepare_reference(cg_ctx* ctx, const double* cl_ref_host);

@@ -558,8 +558,8 @@ static int ensure_ref_bufs(cg_ctx* ctx)
     if (!rc) rc = dalloc(ctx, &w.Zf, (size_t)nhp * N);
     if (!rc) rc = dalloc(ctx, &w.cref, (size_t)ctx->lmax + 1);
     if (!rc) rc = dalloc(ctx, &w.ldref, 1);
-    if (!rc) rc = dalloc(ctx, &w.tcerr, 1);
-    if (!rc) CG_CUDA_TRY(ctx, cudaMemset(w.tcerr, 0, sizeof(int)));
+    if (!rc) rc = dalloc(ctx, &w.tcerr, 1 + (size_t)tc_queue_slots(nt));
+    if (!rc) CG_CUDA_TRY(ctx, cudaMemset(w.tcerr, 0, sizeof(int) * (1 + tc_queue_slots(nt))));
     if (rc) { mixed_free(ctx); return rc; }
     w.lpad = lp;
     return CG_OK;
@@ -712,7 +712,8 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
     const int lp = w.lpad, ntile = ntiles_lower(nt);
     const size_t tiled = tiled_elems(nt);
     stage_mark(ctx, ST_BUILD, s);
-    CG_CUDA_TRY(ctx, cudaMemsetAsync(w.tcerr, 0, sizeof(int), s));  // a timeout reports on its own call only
+    // a timeout reports on its own call only; the work queues start empty
+    CG_CUDA_TRY(ctx, cudaMemsetAsync(w.tcerr, 0, sizeof(int) * (1 + tc_queue_slots(nt)), s));
     init_status<<<(B + 127) / 128, 128, 0, s>>>(B, d_cl, lmax, w.st);
     make_eps<<<B, 64, 0, s>>>(B, lmax, lp, d_cl, w.cref, w.eps);
     count_launch(ctx, d_stride == 0 ? 5 : 4);
@@ -742,7 +743,7 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
     stage_mark(ctx, ST_TRTRI, s);
     if ((rc = tiled_trtri_tc(ctx, B, nt, w.Ls, w.Linv, w.Ms, w.Mc, w.tcerr, s))) return rc;
     stage_mark(ctx, ST_LAUUM, s);
-    if ((rc = tiled_lauum_tc(ctx, B, nt, w.Ms, w.V, w.tcerr, s))) return rc;
+    if ((rc = tiled_lauum_tc(ctx, B, nt, w.Ms, w.Mc, w.V, w.tcerr, s))) return rc;
     stage_mark(ctx, ST_SOLVE, s);
     // x = V y; r = y - A x; x += V r
     symv_partials<false><<<dim3((ntile + SYMV_TPB - 1) / SYMV_TPB, B), 256, 0, s>>>(nt, w.V, tiled, w.y, N, w.part);

@@ -66,6 +66,7 @@ constexpr uint32_t IDESC = idesc_tf32(128, 128);
 constexpr int NPROD = 256;                      // producers (warps 0-7)
 constexpr int NTH = NPROD + 96;                 // + the MMA issuers (warps 8, 10) and the copy warp (9)
 constexpr int NAST = 4;                         // A stages in tensor memory
+constexpr int NIQ = 8;                          // item ids in flight in a CTA's stream
 constexpr int NSTB = 4;                         // B stages in shared memory
 constexpr uint32_t STB_BYTES = 2u * 128 * KC * 4;  // one B stage: hi + lo, 128 rows x 32 K (32 KB)
 constexpr int NSTA = 4;                         // A stages in shared memory (FP32 canonical chunks)
@@ -78,12 +79,15 @@ constexpr int LI_CHUNK = 2 * 128 * KC;          // floats per K chunk of a Linv 
 constexpr int LINV_SC = 4 * LI_CHUNK;           // floats per Linv block (128 KB)
 
 static_assert(SC_CHUNK * 4 == 8192 && LI_CHUNK * 4 == (int)STB_BYTES, "layout sizes");
+// Chunk c goes to B stage c % NSTB and tensor-memory A stage c % NAST, and is issued by the issuer
+// of parity c % 2.  Even stage counts give every stage to one issuer, which then waits on the
+// stage's barriers phase by phase in order.  With an odd count the issuer that is ahead could
+// wait for a phase two ahead of the barrier, which a parity wait reports as complete: it would
+// read a stage whose copy is still in flight.
+static_assert(NSTB % 2 == 0 && NAST % 2 == 0, "stage counts must be even (one issuer per stage)");
 
 // zero 64 x 32 block: the source of bulk copies for operand tiles above the diagonal
 __device__ __align__(128) float g_zero_block[SC_CHUNK];
-
-// float offset of element (r, k) inside one canonical block (r < 128, k < 32)
-__device__ __forceinline__ int canon_off(int r, int k) { return (r >> 3) * 256 + (k >> 2) * 32 + (r & 7) * 4 + (k & 3); }
 
 // Tensor-memory columns (512): the accumulators of the two chunk parities and the A operand
 // (hi, lo) of the four stages
@@ -115,6 +119,9 @@ struct TcCtl {
     uint64_t b_empty[NSTB];   // B stage's MMAs completed
     uint64_t as_full[NSTA];   // A shared-memory stage landed
     uint64_t as_empty[NSTA];  // A shared-memory stage read by every producer warp
+    uint64_t iq_full[NIQ];    // item slot written by the copy thread
+    uint64_t iq_empty[NIQ];   // item slot released by every producer warp and both issuers
+    int iq[NIQ];              // item ids of the stream, -1 = end
     uint32_t tbase;
     int bad;
 };
@@ -133,6 +140,11 @@ __device__ __forceinline__ void init_bars(TcCtl& ctl)
     for (int i = 0; i < NSTA; ++i) {
         mbar_init(&ctl.as_full[i], 1);
         mbar_init(&ctl.as_empty[i], NPROD / 32);
+    }
+    for (int i = 0; i < NIQ; ++i) {
+        mbar_init(&ctl.iq_full[i], 1);
+        mbar_init(&ctl.iq_empty[i], NPROD / 32 + 2);
+        ctl.iq[i] = -1;
     }
     fence_mbar_init();
 }
@@ -163,7 +175,7 @@ __device__ __forceinline__ void tc_rearm(TcCtl& ctl)
     __syncthreads();
     if (threadIdx.x == 0) {
         uint64_t* all = &ctl.mma_bar[0];  // every barrier of TcCtl, contiguous
-        for (int i = 0; i < 4 + NAST + 2 * NSTB + 2 * NSTA; ++i)
+        for (int i = 0; i < 4 + NAST + 2 * NSTB + 2 * NSTA + 2 * NIQ; ++i)
             asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(all + i)));
         init_bars(ctl);
     }
@@ -195,12 +207,6 @@ __device__ __forceinline__ void ld_c1(const float* t, int rr, int kc, int h, flo
         const float4* px = reinterpret_cast<const float4*>(p + i * 32);
         x[i] = COHERENT ? __ldcg(px) : __ldg(px);
     }
-}
-
-__device__ __forceinline__ void zero4(float4 (&x)[4])
-{
-#pragma unroll
-    for (int i = 0; i < 4; ++i) x[i] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 // x = hi + lo with hi = x rounded to nearest TF32 and lo = (x - hi) rounded to nearest TF32
@@ -284,13 +290,116 @@ __device__ __forceinline__ void st_c1_row(float* tile, int rr, const float (&v)[
 
 // ---- the K loop --------------------------------------------------------------
 
-// How the A operand reaches the producers:
-//   A_REG_SC  fa(c, r, h, x[8]) loads row r, K half h of chunk c as hi (x[0..3]) and lo (x[4..7]);
+// How the A operand of chunk c reaches the producers (the item stream passes the item's geometry
+// first: fa(gm, c, ...)):
+//   A_REG_SC  fa(c, r, h, x[8]) loads row r, K half h of the chunk as hi (x[0..3]) and lo (x[4..7]);
 //   A_REG_C1  fa(c, r, h, x[4]) loads it as FP32, split when stored to tensor memory;
 //   A_SMEM_C1 fa(c, top, bot, kc) names the two FP32 canonical tiles (rows 0-63, 64-127; nullptr =
 //             zero) and the K chunk within them; the copy warp brings them into a ring of NSTA
 //             shared-memory stages by bulk copies, ahead of the producers.
 enum { A_REG_SC = 0, A_REG_C1 = 1, A_SMEM_C1 = 2 };
+
+// ---- pieces shared by the single-item K loop and the item stream -----------------------------
+
+constexpr uint32_t kMaxIter = 1u << 22;  // try_wait attempts before a wait gives up
+
+// chunk g's A (row r, K half h: from qx, or for A_SMEM_C1 from the shared-memory ring) into
+// tensor-memory stage g % NAST, then one arrival per warp on the stage's a_full barrier
+template <int AMODE, int NX, class W>
+__device__ __forceinline__ void put_a(int g, float4 (&qx)[NX], W& wait, const float* sa_f, TcCtl& ctl, uint32_t tm)
+{
+    const int r = threadIdx.x % 128, h = threadIdx.x / 128, lane = threadIdx.x % 32, st = g % NAST;
+    if constexpr (AMODE == A_SMEM_C1) {
+        // this thread's 16 values of the staged chunk (row r, K columns 16h .. 16h+15)
+        const int si = g % NSTA;
+        wait(&ctl.as_full[si], (g / NSTA) & 1);
+        const float* p = sa_f + si * (STA_BYTES / 4) + (r >> 3) * 256 + (r & 7) * 4 + 4 * h * 32;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) qx[i] = *reinterpret_cast<const float4*>(p + i * 32);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&ctl.as_empty[si]);
+    }
+    float4 qh[4], ql[4];
+    if constexpr (AMODE == A_REG_SC) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            qh[i] = qx[i];
+            ql[i] = qx[4 + i];
+        }
+    } else {
+        split4(reinterpret_cast<const float4(&)[4]>(qx), qh, ql);
+    }
+    tmem_st16(tm + lane_base() + col_a_hi(st) + 16 * h, qh);
+    tmem_st16(tm + lane_base() + col_a_lo(st) + 16 * h, ql);
+    tmem_wait_st();
+    fence_before();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&ctl.a_full[st]);
+}
+
+// chunk g's MMAs are done: fold its accumulator into R and release it (one arrival per warp).  With
+// `last` the wait ignores the abort flag: every MMA that was issued completes, and none may still
+// run when tensor memory is freed.
+template <class W>
+__device__ __forceinline__ void retire_acc(int g, bool last, W& wait, bool& ok, int* err, TcCtl& ctl, uint32_t tm,
+                                           float (&R)[64])
+{
+    if (!last) {
+        wait(&ctl.mma_bar[g & 1], (g >> 1) & 1);
+    } else if (!mbar_wait(&ctl.mma_bar[g & 1], (g >> 1) & 1, kMaxIter)) {
+        ok = false;
+        atomicExch(err, 1);
+    }
+    fence_after();
+    drain(tm, col_main(g & 1), R);
+    fence_before();
+    __syncwarp();
+    if (threadIdx.x % 32 == 0) mbar_arrive(&ctl.acc_free[g & 1]);
+}
+
+// one issuer thread: chunk g's 12 MMAs (M128 N128 K8, A from tensor-memory stage g % NAST, B from
+// shared-memory stage g % NSTB) into the accumulator of parity g & 1, once its A, its B and its
+// accumulator are ready, committed to the chunk's mbarriers
+template <class W>
+__device__ __forceinline__ void issue_chunk(int g, W& wait, TcCtl& ctl, uint32_t tm, uint32_t sb)
+{
+    const int st = g % NAST, sbi = g % NSTB;
+    wait(&ctl.a_full[st], (g / NAST) & 1);
+    wait(&ctl.b_full[sbi], (g / NSTB) & 1);
+    if (g >= 2) wait(&ctl.acc_free[g & 1], ((g - 2) >> 1) & 1);
+    fence_after();
+    const uint32_t bh = sb + sbi * STB_BYTES, bl = bh + STB_BYTES / 2;
+    const uint32_t ah = tm + col_a_hi(st), al = tm + col_a_lo(st), d = tm + col_main(g & 1);
+#pragma unroll
+    for (int kk = 0; kk < KC / 8; ++kk) {
+        const uint32_t off = kk * 2 * LBO;
+        mma_tf32_ta(d, al + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, kk ? 1u : 0u);
+        mma_tf32_ta(d, ah + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, 1u);
+        mma_tf32_ta(d, ah + 8 * kk, smem_desc(bl + off, LBO, SBO), IDESC, 1u);
+    }
+    mma_commit(&ctl.mma_bar[g & 1]);
+    mma_commit(&ctl.b_empty[sbi]);
+}
+
+// the copy thread's share of chunk g: its A (A_SMEM_C1: fa(..., top, bot, kc) names the tiles) into
+// the A ring and its B (fb(..., dst, bar)) into the B ring, once their stages are free
+template <int AMODE, class W, class FA, class FB>
+__device__ __forceinline__ void copy_chunk(int g, W& wait, TcCtl& ctl, uint32_t sb, FA&& fa, FB&& fb)
+{
+    if constexpr (AMODE == A_SMEM_C1) {
+        const int si = g % NSTA;
+        if (g >= NSTA) wait(&ctl.as_empty[si], ((g / NSTA) - 1) & 1);
+        const float *top, *bot;
+        int kc;
+        fa(top, bot, kc);
+        bulk_a_c1(top, bot, kc, sb + NSTB * STB_BYTES + si * STA_BYTES, &ctl.as_full[si]);
+    }
+    const int sbi = g % NSTB;
+    if (g >= NSTB) wait(&ctl.b_empty[sbi], ((g / NSTB) - 1) & 1);
+    fb(sb + sbi * STB_BYTES, &ctl.b_full[sbi]);
+}
+
+// ---- the K loop of one item ------------------------------------------------------------------
 
 // nchunks chunks; fb(c, dst, bar) issues the B chunk's bulk copies into shared memory at dst.
 // Called by every thread of the CTA.  On return the producer threads (t < NPROD) hold in R[j] the
@@ -301,7 +410,6 @@ template <int AMODE, class FA, class FB>
 __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& ctl, uint32_t tm, float (&R)[64],
                          int* err)
 {
-    constexpr uint32_t kMaxIter = 1u << 22;
     bool ok = true;
     auto wait = [&](uint64_t* bar, uint32_t parity) {
         if (!ok) return;
@@ -309,8 +417,7 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
         if (!ok) atomicExch(err, 1);
     };
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
-    const uint32_t sb = smem_u32(sbuf);                      // B ring
-    const uint32_t sa = sb + NSTB * STB_BYTES;               // A ring (A_SMEM_C1)
+    const uint32_t sb = smem_u32(sbuf);
     const float* sa_f = reinterpret_cast<const float*>(sbuf + NSTB * STB_BYTES);
 #pragma unroll
     for (int j = 0; j < 64; ++j) R[j] = 0.f;
@@ -319,62 +426,24 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
         const int r = threadIdx.x % 128, h = threadIdx.x / 128;
         constexpr int NX = (AMODE == A_REG_SC) ? 8 : 4;
         float4 a0[NX], a1[NX];  // register modes: the loaded A of two chunks (slot = chunk & 1)
-        // chunk c's A (from qx, or for A_SMEM_C1 from the shared-memory ring) into tensor-memory stage c % NAST
-        auto put = [&](int c, float4 (&qx)[NX]) {
-            const int st = c % NAST;
-            if constexpr (AMODE == A_SMEM_C1) {
-                // this thread's 16 values of the staged chunk (row r, K columns 16h .. 16h+15)
-                const int si = c % NSTA;
-                wait(&ctl.as_full[si], (c / NSTA) & 1);
-                const float* p = sa_f + si * (STA_BYTES / 4) + (r >> 3) * 256 + (r & 7) * 4 + 4 * h * 32;
-#pragma unroll
-                for (int i = 0; i < 4; ++i) qx[i] = *reinterpret_cast<const float4*>(p + i * 32);
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&ctl.as_empty[si]);
-            }
-            float4 qh[4], ql[4];
-            if constexpr (AMODE == A_REG_SC) {
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    qh[i] = qx[i];
-                    ql[i] = qx[4 + i];
-                }
-            } else {
-                split4(reinterpret_cast<const float4(&)[4]>(qx), qh, ql);
-            }
-            tmem_st16(tm + lane_base() + col_a_hi(st) + 16 * h, qh);
-            tmem_st16(tm + lane_base() + col_a_lo(st) + 16 * h, ql);
-            tmem_wait_st();
-            fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&ctl.a_full[st]);
-        };
         // chunks 0 and 1 into the empty stages 0 and 1; register modes load two chunks ahead of the store
         if constexpr (AMODE != A_SMEM_C1) {
             if (nchunks > 0) fa(0, r, h, a0);
             if (nchunks > 1) fa(1, r, h, a1);
         }
         if (nchunks > 0) {
-            put(0, a0);
+            put_a<AMODE>(0, a0, wait, sa_f, ctl, tm);
             if constexpr (AMODE != A_SMEM_C1) { if (nchunks > 2) fa(2, r, h, a0); }
         }
         if (nchunks > 1) {
-            put(1, a1);
+            put_a<AMODE>(1, a1, wait, sa_f, ctl, tm);
             if constexpr (AMODE != A_SMEM_C1) { if (nchunks > 3) fa(3, r, h, a1); }
         }
-        // step c: chunk c - 2's MMAs are done, so its accumulator is drained and released, and its
-        // A stage takes chunk c + 2 (held in slot qx = c & 1)
+        // step c: chunk c - 2 is retired and its A stage takes chunk c + 2 (held in slot qx = c & 1)
         auto step = [&](int c, float4 (&qx)[NX]) {
-            if (c >= 2) {
-                wait(&ctl.mma_bar[c & 1], ((c - 2) >> 1) & 1);
-                fence_after();
-                drain(tm, col_main(c & 1), R);
-                fence_before();
-                __syncwarp();
-                if (lane == 0) mbar_arrive(&ctl.acc_free[c & 1]);
-            }
+            if (c >= 2) retire_acc(c - 2, false, wait, ok, err, ctl, tm, R);
             if (c + 2 < nchunks) {
-                put(c + 2, qx);
+                put_a<AMODE>(c + 2, qx, wait, sa_f, ctl, tm);
                 if constexpr (AMODE != A_SMEM_C1) { if (c + 4 < nchunks) fa(c + 4, r, h, qx); }
             }
         };
@@ -382,56 +451,170 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
             step(c, a0);
             if (c + 1 < nchunks) step(c + 1, a1);
         }
-        // the last two chunks: every MMA is issued whatever happened, so their commits always arrive;
-        // wait for them (bounded) even after a failure, so that no MMA still runs when tensor memory
-        // is freed
-        for (int c = (nchunks >= 2 ? nchunks - 2 : 0); c < nchunks; ++c) {
-            if (!mbar_wait(&ctl.mma_bar[c & 1], (c >> 1) & 1, kMaxIter)) {
-                ok = false;
-                atomicExch(err, 1);
-            }
-            fence_after();
-            drain(tm, col_main(c & 1), R);
-        }
-        fence_before();
+        for (int c = (nchunks >= 2 ? nchunks - 2 : 0); c < nchunks; ++c) retire_acc(c, true, wait, ok, err, ctl, tm, R);
     } else if (warp == NPROD / 32 || warp == NPROD / 32 + 2) {
         // ---- MMA issue: the even chunks from warp 8, the odd ones from warp 10
-        if (lane == 0) {
-            for (int c = (warp == NPROD / 32) ? 0 : 1; c < nchunks; c += 2) {
-                const int st = c % NAST, sbi = c % NSTB;
-                wait(&ctl.a_full[st], (c / NAST) & 1);
-                wait(&ctl.b_full[sbi], (c / NSTB) & 1);
-                if (c >= 2) wait(&ctl.acc_free[c & 1], ((c - 2) >> 1) & 1);
-                fence_after();
-                const uint32_t bh = sb + sbi * STB_BYTES, bl = bh + STB_BYTES / 2;
-                const uint32_t ah = tm + col_a_hi(st), al = tm + col_a_lo(st), d = tm + col_main(c & 1);
+        if (lane == 0)
+            for (int c = (warp == NPROD / 32) ? 0 : 1; c < nchunks; c += 2) issue_chunk(c, wait, ctl, tm, sb);
+        __syncwarp();
+    } else {
+        // ---- copies: one thread keeps the B ring (and, for A_SMEM_C1, the A ring) full
+        if (lane == 0)
+            for (int c = 0; c < nchunks; ++c)
+                copy_chunk<AMODE>(
+                    c, wait, ctl, sb, [&](auto& top, auto& bot, auto& kc) { fa(c, top, bot, kc); },
+                    [&](uint32_t dst, uint64_t* bar) { fb(c, dst, bar); });
+        __syncwarp();
+    }
+    return ok;
+}
+
+// ---- the K loop over a stream of items -------------------------------------------------------
+
+// Items taken in order from a counter shared by the CTAs of a launch (zero before the launch): the
+// copy thread takes them and publishes the ids, in order, through a ring of NIQ shared-memory slots
+// (-1 = no more items); every role walks the same sequence of (item, chunk) pairs, and the chunks
+// of all the items pass through the stages as one sequence, so an item's copies and A stores start
+// while the previous item is still in the tensor pipe and a CTA pays its set-up and its first
+// loads' latency once, not per item.  Taking items in order keeps the CTAs running together on
+// neighbouring items (a static share per CTA lets them drift apart).
+// geo(it) gives item it's geometry (a struct whose member n >= 1 is its chunk count), worked out
+// once per item by each role; fa(gm, c, ...) (as for tc_kloop) and fb(gm, c, dst, bar) receive it.
+// Once the last chunk of an item is folded in, the producer threads (t < NPROD) call epi(gm, R)
+// with R[j] its product at row t % 128, column 64 (t / 128) + j, then clear R.  Called by every
+// thread of the CTA.  Failure handling as tc_kloop; a thread whose wait gave up also takes no new
+// items, and item ids outside [0, nitems) end the stream.
+template <int AMODE, class GEO, class FA, class FB, class FE>
+__device__ bool tc_stream(int nitems, int* queue, GEO geo, FA fa, FB fb, FE epi, unsigned char* sbuf, TcCtl& ctl,
+                          uint32_t tm, float (&R)[64], int* err)
+{
+    bool ok = true;
+    auto wait = [&](uint64_t* bar, uint32_t parity) {
+        if (!ok) return;
+        ok = mbar_wait(bar, parity, kMaxIter, err);
+        if (!ok) atomicExch(err, 1);
+    };
+    // a reader's position in the stream: chunk c of the item in queue slot k % NIQ, of geometry gm;
+    // gm.n = 0 at the end
+    using Geo = decltype(geo(0));
+    struct Cur {
+        int k, c;
+        Geo gm;
+    };
+    auto enter = [&](Cur& q) {
+        wait(&ctl.iq_full[q.k % NIQ], (q.k / NIQ) & 1);
+        const int it = ctl.iq[q.k % NIQ];
+        q.c = 0;
+        if (ok && it >= 0 && it < nitems) {
+            q.gm = geo(it);
+        } else {
+            q.gm.n = 0;
+        }
+    };
+    // to the next chunk; on leaving an item a releasing reader frees its slot: REL_WARP for a whole
+    // warp (one arrival after every lane is done), REL_ONE for a single thread (the issuers)
+    enum { REL_NONE, REL_WARP, REL_ONE };
+    auto next = [&](Cur& q, int release) {
+        if (++q.c < q.gm.n) return;
+        if (release == REL_WARP) {
+            __syncwarp();
+            if ((threadIdx.x % 32) == 0) mbar_arrive(&ctl.iq_empty[q.k % NIQ]);
+        } else if (release == REL_ONE) {
+            mbar_arrive(&ctl.iq_empty[q.k % NIQ]);
+        }
+        ++q.k;
+        enter(q);
+    };
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const uint32_t sb = smem_u32(sbuf);
+    const float* sa_f = reinterpret_cast<const float*>(sbuf + NSTB * STB_BYTES);
 #pragma unroll
-                for (int kk = 0; kk < KC / 8; ++kk) {
-                    const uint32_t off = kk * 2 * LBO;
-                    mma_tf32_ta(d, al + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, kk ? 1u : 0u);
-                    mma_tf32_ta(d, ah + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, 1u);
-                    mma_tf32_ta(d, ah + 8 * kk, smem_desc(bl + off, LBO, SBO), IDESC, 1u);
+    for (int j = 0; j < 64; ++j) R[j] = 0.f;
+    if (warp < NPROD / 32) {
+        // ---- producers
+        const int r = threadIdx.x % 128, h = threadIdx.x / 128;
+        constexpr int NX = (AMODE == A_REG_SC) ? 8 : 4;
+        float4 a0[NX], a1[NX];  // register modes: the loaded A of two chunks (slot = chunk & 1)
+        // the next chunk to load (register modes), to put into tensor memory, to retire
+        Cur lq{}, pq{}, dq{};
+        if constexpr (AMODE != A_SMEM_C1) enter(lq);
+        enter(pq);
+        enter(dq);
+        auto load = [&](float4 (&x)[NX]) {
+            if constexpr (AMODE != A_SMEM_C1) {
+                if (lq.gm.n) {
+                    fa(lq.gm, lq.c, r, h, x);
+                    next(lq, REL_NONE);
                 }
-                mma_commit(&ctl.mma_bar[c & 1]);
-                mma_commit(&ctl.b_empty[sbi]);
+            }
+        };
+        auto put = [&](int g, float4 (&qx)[NX]) {
+            put_a<AMODE>(g, qx, wait, sa_f, ctl, tm);
+            next(pq, REL_NONE);
+        };
+        auto retire = [&](int g, bool last) {
+            retire_acc(g, last, wait, ok, err, ctl, tm, R);
+            if (dq.c == dq.gm.n - 1) {
+                epi(dq.gm, R);
+#pragma unroll
+                for (int j = 0; j < 64; ++j) R[j] = 0.f;
+            }
+            next(dq, REL_WARP);
+        };
+        // chunks 0 and 1 into the empty stages 0 and 1; register modes load two chunks ahead of the store
+        int nput = 0;  // chunks put so far; while any remain, chunk g + 2 is put at step g
+        load(a0);
+        load(a1);
+        if (pq.gm.n) {
+            put(nput++, a0);
+            load(a0);
+        }
+        if (pq.gm.n) {
+            put(nput++, a1);
+            load(a1);
+        }
+        // step g: chunk g - 2 is retired and its A stage takes chunk g + 2 (held in slot qx = g & 1)
+        auto step = [&](int g, float4 (&qx)[NX]) {
+            if (g >= 2) retire(g - 2, false);
+            if (pq.gm.n) {
+                put(nput++, qx);
+                load(qx);
+            }
+        };
+        for (int g = 0; g < nput; g += 2) {
+            step(g, a0);
+            if (g + 1 < nput) step(g + 1, a1);
+        }
+        for (int g = (nput >= 2 ? nput - 2 : 0); g < nput; ++g) retire(g, true);
+    } else if (warp == NPROD / 32 || warp == NPROD / 32 + 2) {
+        // ---- MMA issue: the even chunks of the stream from warp 8, the odd ones from warp 10
+        const int par = (warp == NPROD / 32) ? 0 : 1;
+        if (lane == 0) {
+            Cur q{};
+            enter(q);
+            for (int g = 0; q.gm.n; ++g) {
+                if ((g & 1) == par) issue_chunk(g, wait, ctl, tm, sb);
+                next(q, REL_ONE);
             }
         }
         __syncwarp();
     } else {
-        // ---- copies: one thread keeps the B ring (and, for A_SMEM_C1, the A ring) full
+        // ---- copies: one thread takes the items, publishes them and keeps the rings full
         if (lane == 0) {
-            for (int c = 0; c < nchunks; ++c) {
-                if constexpr (AMODE == A_SMEM_C1) {
-                    const int si = c % NSTA;
-                    if (c >= NSTA) wait(&ctl.as_empty[si], ((c / NSTA) - 1) & 1);
-                    const float *top, *bot;
-                    int kc;
-                    fa(c, top, bot, kc);
-                    bulk_a_c1(top, bot, kc, sa + si * STA_BYTES, &ctl.as_full[si]);
-                }
-                const int sbi = c % NSTB;
-                if (c >= NSTB) wait(&ctl.b_empty[sbi], ((c / NSTB) - 1) & 1);
-                fb(c, sb + sbi * STB_BYTES, &ctl.b_full[sbi]);
+            int g = 0;
+            for (int k = 0;; ++k) {
+                const int slot = k % NIQ;
+                if (k >= NIQ) wait(&ctl.iq_empty[slot], ((k / NIQ) - 1) & 1);
+                const int got = ok ? atomicAdd(queue, 1) : -1;
+                const int it = (got >= 0 && got < nitems) ? got : -1;
+                ctl.iq[slot] = it;
+                mbar_arrive(&ctl.iq_full[slot]);
+                if (it < 0) break;
+                const Geo gm = geo(it);
+                for (int c = 0; c < gm.n; ++c, ++g)
+                    copy_chunk<AMODE>(
+                        g, wait, ctl, sb, [&](auto& top, auto& bot, auto& kc) { fa(gm, c, top, bot, kc); },
+                        [&](uint32_t dst, uint64_t* bar) { fb(gm, c, dst, bar); });
             }
         }
         __syncwarp();
@@ -714,34 +897,43 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
     tc_end(tm);
 }
 
-// L_IJ = S_IJ Linv_J^T for I2 = J2 + 1 + blockIdx.x; grid (nt2 - J2 - 1, B)
-__global__ void __launch_bounds__(NTH, 1) chol_tc_panel(int J2, int nt, float* __restrict__ Ls,
+// L_IJ = S_IJ Linv_J^T for every I2 > J2 and batch element: items it = b (nt2 - J2 - 1) + I2 - J2 - 1,
+// taken in order from the work queue by persistent CTAs
+__global__ void __launch_bounds__(NTH, 1) chol_tc_panel(int J2, int nt, int B, float* __restrict__ Ls,
                                                         float* __restrict__ Lc, const float* __restrict__ Linv,
-                                                        int* __restrict__ err)
+                                                        int* __restrict__ queue, int* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ TcCtl ctl;
-    const int I2 = J2 + 1 + blockIdx.x, b = blockIdx.y, nt2 = nt / 2;
-    float* Lb = Ls + (size_t)b * ntiles_lower(nt) * SC_TILE;
-    float* Lcb = Lc + (size_t)b * ntiles_lower(nt) * C1_TILE;
-    const float* li = Linv + ((size_t)b * nt2 + J2) * LINV_SC;
+    const int nt2 = nt / 2, m = nt2 - J2 - 1;
+    const size_t ntile = (size_t)ntiles_lower(nt);
     const uint32_t tm = tc_begin(ctl);
+    struct Item {
+        int n, I2;
+        const float* Lcb;  // the batch element's S / L (C1)
+        const float* li;   // its Linv_J
+        size_t boff;       // its first tile
+    };
+    auto geo = [&](int it) {
+        const size_t b = it / m;
+        return Item{128 / KC, J2 + 1 + it % m, Lc + b * ntile * C1_TILE, Linv + (b * nt2 + J2) * LINV_SC, b * ntile};
+    };
     // A(r, m) = S_IJ(r, m), C1 tiles (2 I2 + r/64, 2 J2 + m/64); B(c, m) = Linv_J(c, m)
-    auto fa = [&](int c, const float*& top, const float*& bot, int& kc) {
-        top = Lcb + (size_t)tile_index(2 * I2, 2 * J2 + c / 2) * C1_TILE;
-        bot = Lcb + (size_t)tile_index(2 * I2 + 1, 2 * J2 + c / 2) * C1_TILE;
+    auto fa = [&](const Item& q, int c, const float*& top, const float*& bot, int& kc) {
+        top = q.Lcb + (size_t)tile_index(2 * q.I2, 2 * J2 + c / 2) * C1_TILE;
+        bot = q.Lcb + (size_t)tile_index(2 * q.I2 + 1, 2 * J2 + c / 2) * C1_TILE;
         kc = c % 2;
     };
-    auto fb = [&](int c, uint32_t dst, uint64_t* bar) { bulk_linv(li, c, dst, bar); };
+    auto fb = [&](const Item& q, int c, uint32_t dst, uint64_t* bar) { bulk_linv(q.li, c, dst, bar); };
+    // the item's S tiles were all read (its MMAs are done) before they are overwritten
+    auto epi = [&](const Item& q, float (&R)[64]) {
+        const int row = threadIdx.x % 128, h = threadIdx.x / 128;
+        const size_t tix = q.boff + tile_index(2 * q.I2 + row / 64, 2 * J2 + h);
+        st_sc_row(Ls + tix * SC_TILE, row % 64, R, 1.f);
+        st_c1_row(Lc + tix * C1_TILE, row % 64, R, 1.f);
+    };
     float R[64];
-    tc_kloop<A_SMEM_C1>(128 / KC, fa, fb, smem_raw, ctl, tm, R, err);
-    __syncthreads();  // every S read is done before the tiles are overwritten
-    const int row = threadIdx.x % 128, h = threadIdx.x / 128;
-    if (threadIdx.x < NPROD) {
-        const size_t tix = tile_index(2 * I2 + row / 64, 2 * J2 + h);
-        st_sc_row(Lb + tix * SC_TILE, row % 64, R, 1.f);
-        st_c1_row(Lcb + tix * C1_TILE, row % 64, R, 1.f);
-    }
+    tc_stream<A_SMEM_C1>(m * B, queue, geo, fa, fb, epi, smem_raw, ctl, tm, R, err);
     tc_end(tm);
 }
 
@@ -798,7 +990,10 @@ __global__ void __launch_bounds__(NTH, 1) trtri_tc_row(int I2, int nt, const flo
 }
 
 // V_IJ (128x128 supertile, lower) = sum over k of M_k,I^T M_k,J from the M^T storage; V in FP32
-// column-major tiles.  grid (supertiles of the lower triangle, B).
+// column-major tiles.  grid (supertiles of the lower triangle, B).  One CTA per supertile: lauum's
+// A operands are loaded by the producers (a persistent stream costs them the registers for it),
+// and the hardware's in-order CTA dispatch keeps the CTAs running together on one batch element,
+// whose M stays in L2.
 __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restrict__ Ms, float* __restrict__ V,
                                                    int* __restrict__ err)
 {
@@ -873,6 +1068,8 @@ static int set_smem(cg_ctx* ctx, K kern)
 size_t tc_split_elems(int nt) { return (size_t)ntiles_lower(nt) * SC_TILE; }
 size_t tc_c1_elems(int nt) { return (size_t)ntiles_lower(nt) * C1_TILE; }
 size_t tc_linv_elems(int nt) { return (size_t)(nt / 2) * LINV_SC; }
+// work-queue counters after the error flag: one per panel launch of the Cholesky
+int tc_queue_slots(int nt) { return nt / 2; }
 
 int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, float* Lc, float* Linv, float* Ms,
                       float* Mc, float* diag, int* status, int* d_err, cudaStream_t s)
@@ -885,7 +1082,9 @@ int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, flo
         chol_tc_update<<<B * (nt2 - J2), NTH, tc_smem(), s>>>(J2, nt, B, A, Ls, Lc, Linv, Ms, Mc, diag, status, d_err);
         count_launch(ctx);
         if (J2 + 1 < nt2) {
-            chol_tc_panel<<<dim3(nt2 - J2 - 1, B), NTH, tc_smem(), s>>>(J2, nt, Ls, Lc, Linv, d_err);
+            const int items = (nt2 - J2 - 1) * B;
+            chol_tc_panel<<<items < ctx->sm_count ? items : ctx->sm_count, NTH, tc_smem(), s>>>(
+                J2, nt, B, Ls, Lc, Linv, d_err + 1 + J2, d_err);
             count_launch(ctx);
         }
     }
@@ -908,7 +1107,8 @@ int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* Ls, const float* Lin
     return CG_OK;
 }
 
-int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, float* V, int* d_err, cudaStream_t s)
+int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, const float* Mc, float* V, int* d_err,
+                   cudaStream_t s)
 {
     if (nt % 2) { ctx->err = "tensor-core lauum needs an even tile count"; return CG_ERR_BAD_ARG; }
     int rc;
