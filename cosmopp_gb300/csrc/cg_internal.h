@@ -188,6 +188,10 @@ int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* Ls, const float* Lin
                    int* d_err, cudaStream_t s);
 int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, const float* Mc, float* V, int* d_err,
                    cudaStream_t s);
+// part[t][b][l] = sum_e w_e V_b[e] Ubar_l[e] over lower tile t (k_tc.cu), for lp % 16 == 0, lp <= 96
+bool adjoint_tc_ok(int lp);
+int adjoint_contract_tc(cg_ctx* ctx, int B, int nt, int lp, const float* U, const float* V, size_t strideA,
+                        float* part, int* d_err, cudaStream_t s);
 int selftest_wait_timeout(cg_ctx* ctx, int* host_status);
 // mixed path (k_mixed.cu)
 int mixed_prepare_reference(cg_ctx* ctx, const double* cl_ref_host);

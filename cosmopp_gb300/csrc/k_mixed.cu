@@ -756,19 +756,23 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
     count_launch(ctx, 7);
     stage_mark(ctx, ST_ADJOINT, s);
     if (d_grad) {
-        if (B <= 64) {
+        if (adjoint_tc_ok(lp)) {
+            if ((rc = adjoint_contract_tc(ctx, B, nt, lp, w.U, w.V, tiled, w.gpart, w.tcerr, s))) return rc;
+        } else if (B <= 64) {
             const size_t sma = sizeof(float) * (64 * ADJ_LD + 48 * ADJ_KE);
             CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_adj<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma));
             contract_adj<2><<<dim3(ntile, (B + 63) / 64, (lp + 47) / 48), 256, sma, s>>>(B, lp, w.U, w.V, tiled, w.gpart);
+            count_launch(ctx);
         } else {
             const size_t sma = sizeof(float) * (256 * ADJ_LD + 48 * ADJ_KE);
             CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_adj<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sma));
             contract_adj<8><<<dim3(ntile, (B + 255) / 256, (lp + 47) / 48), 256, sma, s>>>(B, lp, w.U, w.V, tiled, w.gpart);
+            count_launch(ctx);
         }
         const int nhp = nharm_pad(lmax);
         project_x<<<dim3(nhp / 64, (B + 63) / 64), 256, 0, s>>>(B, N, nhp, w.Zf, w.x, w.proj);
         adj_finish<<<B, 64, 0, s>>>(B, ntile, lmax, lp, nhp, w.gpart, w.proj, w.cref, d_grad);
-        count_launch(ctx, 3);
+        count_launch(ctx, 2);
     }
     merge_tc_status<<<(B + 127) / 128, 128, 0, s>>>(B, w.tcerr, w.st);
     count_launch(ctx);

@@ -794,22 +794,59 @@ __device__ void factor_block128(float* s, float* inv, float* tmp, int* bad)
     __syncthreads();
 }
 
-// Left-looking Cholesky, column block J2; 1-D grid of B (nt2 - J2) CTAs.  The first B are the
-// diagonal blocks (one per batch element), which also factorise, so they start first and their
-// factorisation overlaps the off-diagonal CTAs; those follow batch-major (CTAs of one batch
-// element run together and share its L_J panel in L2).
-// Off-diagonal blocks: S_IJ = A_IJ - sum_{k < 2 J2} L_I,k L_J,k^T into the L storage (SC).
+// Left-looking Cholesky, column block J2.  The first B CTAs of the 1-D grid are the diagonal blocks
+// (one per batch element), which also factorise, so they start first and their factorisation
+// overlaps the off-diagonal blocks.  Off-diagonal blocks: S_IJ = A_IJ - sum_{k < 2 J2} L_I,k L_J,k^T
+// into the L storage (C1); for J2 > 0 the CTAs after the first B are persistent and take them from
+// the work queue, batch element by batch element (the blocks of one element share its L_J panel
+// in L2); for J2 = 0 (no K loop, S = A) one CTA each.
 // Diagonal block: S_JJ factorised, L_JJ into the L storage, its inverse into Linv and, transposed,
 // into the M storage, its diagonal into diag.
 __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, const float* __restrict__ A,
                                                          float* __restrict__ Ls, float* __restrict__ Lc,
                                                          float* __restrict__ Linv, float* __restrict__ Ms,
                                                          float* __restrict__ Mc, float* __restrict__ diag,
-                                                         int* __restrict__ status, int* __restrict__ err)
+                                                         int* __restrict__ status, int* __restrict__ queue,
+                                                         int* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ TcCtl ctl;
     const int nt2 = nt / 2, noff = nt2 - J2 - 1;
+    const size_t ntile = (size_t)ntiles_lower(nt);
+    const int row = threadIdx.x % 128, h = threadIdx.x / 128;
+    const bool prod = threadIdx.x < NPROD;
+    const int nchunks = 2 * J2 * (TS / KC);
+    float R[64];
+    // S = A - R for the block's rows row, 64 h .. 64 h + 63 into the C1 tile
+    auto store_s = [&](size_t boff, int I2) {
+        const int ti = 2 * I2 + row / 64, tj = 2 * J2 + h;
+        const size_t tix = boff + tile_index(ti, tj);
+        const float* a = A + tix * TILE_ELEMS + row % 64;
+#pragma unroll
+        for (int j = 0; j < 64; ++j) R[j] = a[TS * j] - R[j];
+        st_c1_row(Lc + tix * C1_TILE, row % 64, R, 1.f);
+    };
+    if ((int)blockIdx.x >= B && J2 > 0) {
+        const uint32_t tm = tc_begin(ctl);
+        struct Item {
+            int n, I2;
+            size_t boff;  // the batch element's first tile
+        };
+        auto geo = [&](int it) { return Item{nchunks, J2 + 1 + it % noff, (size_t)(it / noff) * ntile}; };
+        auto fa = [&](const Item& q, int c, const float*& top, const float*& bot, int& kc) {
+            top = Lc + (q.boff + tile_index(2 * q.I2, c / 2)) * C1_TILE;
+            bot = Lc + (q.boff + tile_index(2 * q.I2 + 1, c / 2)) * C1_TILE;
+            kc = c % 2;
+        };
+        auto fb = [&](const Item& q, int c, uint32_t dst, uint64_t* bar) {
+            bulk_tiles(Ls + (q.boff + tile_index(2 * J2, c / 2)) * SC_TILE,
+                       Ls + (q.boff + tile_index(2 * J2 + 1, c / 2)) * SC_TILE, c % 2, dst, bar);
+        };
+        auto epi = [&](const Item& q, float (&)[64]) { store_s(q.boff, q.I2); };
+        tc_stream<A_SMEM_C1>(noff * B, queue, geo, fa, fb, epi, smem_raw, ctl, tm, R, err);
+        tc_end(tm);
+        return;
+    }
     int I2, b;
     if ((int)blockIdx.x < B) {
         I2 = J2;
@@ -819,12 +856,10 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
         b = k / noff;
         I2 = J2 + 1 + k % noff;
     }
-    const size_t ntile = (size_t)ntiles_lower(nt);
     const float* Ab = A + (size_t)b * ntile * TILE_ELEMS;
     float* Lb = Ls + (size_t)b * ntile * SC_TILE;
     float* Lcb = Lc + (size_t)b * ntile * C1_TILE;
     const uint32_t tm = tc_begin(ctl);
-    const int nchunks = 2 * J2 * (TS / KC);
     auto fa = [&](int c, const float*& top, const float*& bot, int& kc) {
         top = Lcb + (size_t)tile_index(2 * I2, c / 2) * C1_TILE;
         bot = Lcb + (size_t)tile_index(2 * I2 + 1, c / 2) * C1_TILE;
@@ -834,18 +869,9 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
         bulk_tiles(Lb + (size_t)tile_index(2 * J2, c / 2) * SC_TILE, Lb + (size_t)tile_index(2 * J2 + 1, c / 2) * SC_TILE,
                    c % 2, dst, bar);
     };
-    float R[64];
     tc_kloop<A_SMEM_C1>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
-    const int row = threadIdx.x % 128, h = threadIdx.x / 128;
-    const bool prod = threadIdx.x < NPROD;
     if (I2 > J2) {
-        if (prod) {
-            const int ti = 2 * I2 + row / 64, tj = 2 * J2 + h;
-            const float* a = Ab + (size_t)tile_index(ti, tj) * TILE_ELEMS + row % 64;
-#pragma unroll
-            for (int j = 0; j < 64; ++j) R[j] = a[TS * j] - R[j];
-            st_c1_row(Lcb + (size_t)tile_index(ti, tj) * C1_TILE, row % 64, R, 1.f);
-        }
+        if (prod) store_s((size_t)b * ntile, I2);
         tc_end(tm);
         return;
     }
@@ -1037,6 +1063,208 @@ __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restri
     tc_end(tm);
 }
 
+// ---- adjoint contraction ---------------------------------------------------------------------
+
+// part[t][b][l] = sum over the entries e of lower tile t of w_e V_b[e] Ubar_l[e], w_e = 2 below the
+// matrix diagonal, 1 on it, 0 above (V symmetric, stored lower): the per-tile terms of
+// Tr(V dA/dC_l).  One GEMM per tile and 128 batch elements: M = 128 (b), N = lp (l), K = the tile's
+// 4096 entries in 32-wide chunks, 3xTF32.  Each producer copies its own pieces of both operands
+// (cp.async, per thread) into a ring of NCP shared-memory slots, NCP - 1 chunks ahead: V streams
+// from DRAM, whose latency registers two chunks ahead did not cover.  It then stores them split:
+// V (A, weighted) into tensor memory, Ubar (B) into a shared-memory stage (K-major canonical, lp
+// rows), so the FP32 table needs no split copy.  One thread issues the MMAs; every chunk's
+// accumulator is folded into round-to-nearest registers (the tensor core's FP32 accumulation
+// drifts one way).  RC >= lp / 2: the accumulator columns a producer drains.
+// grid (tiles, ceil(B / 128)).
+constexpr int ADJ_NTH = NPROD + 32;
+
+template <int RC, int NCP>
+__global__ void __launch_bounds__(ADJ_NTH, 1) contract_adj_tc(int B, int lp, const float* __restrict__ U,
+                                                              const float* __restrict__ V, size_t strideA,
+                                                              float* __restrict__ part, int* __restrict__ err)
+{
+    constexpr int NBP = (8 * RC + NPROD - 1) / NPROD;  // B pieces (8 K values) per producer and chunk
+    constexpr uint32_t SLOT = NPROD * 16 * (4 + 2 * NBP);  // one copy slot: 16-byte pieces, piece-major
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ uint64_t mma_bar[2], acc_free[2], ab_full[NAST];
+    __shared__ uint32_t tbase;
+    const int t = blockIdx.x, b0 = blockIdx.y * 128;
+    int I, J;
+    tile_coords(t, I, J);
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    if (warp == 0) tmem_alloc(&tbase, TMEM_COLS);
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&mma_bar[i], 1);
+            mbar_init(&acc_free[i], NPROD / 32);
+        }
+        for (int i = 0; i < NAST; ++i) mbar_init(&ab_full[i], NPROD / 32);
+        fence_mbar_init();
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tm = tbase, sb = smem_u32(smem_raw);
+    const uint32_t plane = (uint32_t)lp * KC * 4, stb = 2 * plane;  // B stage: lp rows x 32 K, hi then lo
+    constexpr int NCH = TILE_ELEMS / KC;
+    bool ok = true;
+    auto wait = [&](uint64_t* bar, uint32_t parity) {
+        if (!ok) return;
+        ok = mbar_wait(bar, parity, kMaxIter, err);
+        if (!ok) atomicExch(err, 1);
+    };
+    if (warp < NPROD / 32) {
+        const int r = threadIdx.x % 128, h = threadIdx.x / 128, b = b0 + r;
+        // rows past B load row B - 1: their products are never stored, and a row touches only its own
+        const float* Vt = V + (size_t)(b < B ? b : B - 1) * strideA + (size_t)t * TILE_ELEMS;
+        const float* Ut = U + (size_t)t * TILE_ELEMS * lp;
+        float R[RC];
+#pragma unroll
+        for (int j = 0; j < RC; ++j) R[j] = 0.f;
+        // copy slots after the B stages: 16-byte piece q of thread t at slot + (q NPROD + t) 16, so that
+        // a warp's reads of one piece are consecutive.  Pieces 0-3: 16 V entries (row b, K half h);
+        // 4 + 2p, 5 + 2p: Ubar row l = i / 4, K columns 8 (i % 4) .. + 7 for i = t + NPROD p < 4 lp.
+        const uint32_t slots = sb + NAST * stb;
+        auto piece = [&](int c, int q) { return slots + (c % NCP) * SLOT + (q * NPROD + threadIdx.x) * 16; };
+        auto fetch = [&](int c) {
+            if (c < NCH) {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) cp_async16(piece(c, i), Vt + KC * c + 16 * h + 4 * i);
+#pragma unroll
+                for (int p = 0; p < NBP; ++p) {
+                    const int i = threadIdx.x + NPROD * p;
+                    if (i < 4 * lp) {
+                        const float* src = Ut + (size_t)(i / 4) * TILE_ELEMS + KC * c + 8 * (i % 4);
+                        cp_async16(piece(c, 4 + 2 * p), src);
+                        cp_async16(piece(c, 5 + 2 * p), src + 4);
+                    }
+                }
+            }
+            cp_async_commit();  // one group per chunk, empty past the end, so that waits count chunks
+        };
+        auto rd = [&](int c, int q) {
+            return *reinterpret_cast<const float4*>(smem_raw + (piece(c, q) - sb));
+        };
+        // chunk c into stage c % NAST: weighted, split V into tensor memory, split Ubar into shared
+        // memory (this thread's copies of chunk c have landed)
+        auto put = [&](int c) {
+            const int st = c % NAST;
+            float4 qh[4], ql[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const float4 v = rd(c, i);
+                float x[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const int e = KC * c + 16 * h + 4 * i + k, rr = e % TS, cc = e / TS;
+                    const float w = (I != J || rr > cc) ? 2.f : (rr == cc ? 1.f : 0.f);
+                    x[k] *= w;
+                }
+                qh[i] = make_float4(tf32_rn(x[0]), tf32_rn(x[1]), tf32_rn(x[2]), tf32_rn(x[3]));
+                ql[i] = make_float4(tf32_rn(x[0] - qh[i].x), tf32_rn(x[1] - qh[i].y), tf32_rn(x[2] - qh[i].z),
+                                    tf32_rn(x[3] - qh[i].w));
+            }
+            tmem_st16(tm + lane_base() + col_a_hi(st) + 16 * h, qh);
+            tmem_st16(tm + lane_base() + col_a_lo(st) + 16 * h, ql);
+            unsigned char* stage = smem_raw + st * stb;
+#pragma unroll
+            for (int p = 0; p < NBP; ++p) {
+                const int i = threadIdx.x + NPROD * p;
+                if (i < 4 * lp) {
+                    const int l = i / 4, k0 = 8 * (i % 4);
+#pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        const float4 x = rd(c, 4 + 2 * p + q);
+                        const float4 hi = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
+                        const float4 lo = make_float4(tf32_rn(x.x - hi.x), tf32_rn(x.y - hi.y), tf32_rn(x.z - hi.z),
+                                                      tf32_rn(x.w - hi.w));
+                        const uint32_t off = (l / 8) * 1024 + ((k0 / 4) + q) * 128 + (l % 8) * 16;
+                        *reinterpret_cast<float4*>(stage + off) = hi;
+                        *reinterpret_cast<float4*>(stage + plane + off) = lo;
+                    }
+                }
+            }
+            fence_proxy_async();
+            tmem_wait_st();
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&ab_full[st]);
+        };
+        // chunk c's MMAs are done: fold its lp / 2 columns of this thread into R and release the
+        // accumulator (the last chunks' waits ignore the abort flag: no MMA may outlive tensor memory)
+        auto retire = [&](int c, bool last) {
+            if (!last) {
+                wait(&mma_bar[c & 1], (c >> 1) & 1);
+            } else if (!mbar_wait(&mma_bar[c & 1], (c >> 1) & 1, kMaxIter)) {
+                ok = false;
+                atomicExch(err, 1);
+            }
+            fence_after();
+#pragma unroll
+            for (int j = 0; j < (RC + 7) / 8; ++j) {
+                if (8 * j < lp / 2) {
+                    float m[8];
+                    tmem_ld8w(tm + lane_base() + col_main(c & 1) + h * (lp / 2) + 8 * j, m);
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) R[8 * j + i] += m[i];
+                }
+            }
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&acc_free[c & 1]);
+        };
+        // copies run NCP - 1 chunks ahead of the stores, the stores two chunks ahead of the MMAs:
+        // step c retires chunk c - 2, stores chunk c + 2 into its stage and fetches chunk c + 1 + NCP
+        for (int c = 0; c < NCP - 1; ++c) fetch(c);
+        cp_async_wait<NCP - 2>();
+        put(0);
+        fetch(NCP - 1);
+        cp_async_wait<NCP - 2>();
+        put(1);
+        fetch(NCP);
+        for (int c = 0; c < NCH; ++c) {
+            if (c >= 2) retire(c - 2, false);
+            if (c + 2 < NCH) {
+                cp_async_wait<NCP - 2>();
+                put(c + 2);
+                fetch(c + 1 + NCP);
+            }
+        }
+        cp_async_wait<0>();
+        retire(NCH - 2, true);
+        retire(NCH - 1, true);
+        if (b < B) {
+            float* dst = part + ((size_t)t * B + b) * lp + h * (lp / 2);
+#pragma unroll
+            for (int j = 0; j < RC; ++j)
+                if (j < lp / 2) dst[j] = R[j];
+        }
+    } else if (lane == 0) {
+        // MMA issue: chunk c's 12 MMAs (M128 N lp K8) once its operands and its accumulator are ready
+        const uint32_t idesc = idesc_tf32(128, lp);
+        for (int c = 0; c < NCH; ++c) {
+            const int st = c % NAST;
+            wait(&ab_full[st], (c / NAST) & 1);
+            if (c >= 2) wait(&acc_free[c & 1], ((c - 2) >> 1) & 1);
+            fence_after();
+            const uint32_t bh = sb + st * stb, bl = bh + plane;
+            const uint32_t ah = tm + col_a_hi(st), al = tm + col_a_lo(st), d = tm + col_main(c & 1);
+#pragma unroll
+            for (int kk = 0; kk < KC / 8; ++kk) {
+                const uint32_t off = kk * 2 * LBO;
+                mma_tf32_ta(d, al + 8 * kk, smem_desc(bh + off, LBO, SBO), idesc, kk ? 1u : 0u);
+                mma_tf32_ta(d, ah + 8 * kk, smem_desc(bh + off, LBO, SBO), idesc, 1u);
+                mma_tf32_ta(d, ah + 8 * kk, smem_desc(bl + off, LBO, SBO), idesc, 1u);
+            }
+            mma_commit(&mma_bar[c & 1]);
+        }
+    }
+    __syncwarp();
+    fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_dealloc(tm, TMEM_COLS);
+}
+
 // Self-test of the bounded-wait path: one thread waits, with a short limit, on an mbarrier
 // that nothing arrives on; the wait must give up and report CG_ERR_TIMEOUT.
 __global__ void wait_timeout_probe(int* status)
@@ -1068,8 +1296,8 @@ static int set_smem(cg_ctx* ctx, K kern)
 size_t tc_split_elems(int nt) { return (size_t)ntiles_lower(nt) * SC_TILE; }
 size_t tc_c1_elems(int nt) { return (size_t)ntiles_lower(nt) * C1_TILE; }
 size_t tc_linv_elems(int nt) { return (size_t)(nt / 2) * LINV_SC; }
-// work-queue counters after the error flag: one per panel launch of the Cholesky
-int tc_queue_slots(int nt) { return nt / 2; }
+// work-queue counters after the error flag: one per update and one per panel launch of the Cholesky
+int tc_queue_slots(int nt) { return nt; }
 
 int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, float* Lc, float* Linv, float* Ms,
                       float* Mc, float* diag, int* status, int* d_err, cudaStream_t s)
@@ -1079,7 +1307,11 @@ int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, flo
     if ((rc = set_smem(ctx, chol_tc_update)) || (rc = set_smem(ctx, chol_tc_panel))) return rc;
     const int nt2 = nt / 2;
     for (int J2 = 0; J2 < nt2; ++J2) {
-        chol_tc_update<<<B * (nt2 - J2), NTH, tc_smem(), s>>>(J2, nt, B, A, Ls, Lc, Linv, Ms, Mc, diag, status, d_err);
+        // diagonal CTAs, then one CTA per off-diagonal block (J2 = 0) or persistent CTAs
+        const int noff = (nt2 - J2 - 1) * B;
+        const int grid = B + (J2 == 0 ? noff : (noff < ctx->sm_count ? noff : ctx->sm_count));
+        chol_tc_update<<<grid, NTH, tc_smem(), s>>>(J2, nt, B, A, Ls, Lc, Linv, Ms, Mc, diag, status,
+                                                    d_err + 1 + nt2 + J2, d_err);
         count_launch(ctx);
         if (J2 + 1 < nt2) {
             const int items = (nt2 - J2 - 1) * B;
@@ -1115,6 +1347,35 @@ int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, const float* Mc,
     if ((rc = set_smem(ctx, lauum_tc))) return rc;
     const int nt2 = nt / 2;
     lauum_tc<<<dim3(nt2 * (nt2 + 1) / 2, B), NTH, tc_smem(), s>>>(nt, Ms, V, d_err);
+    count_launch(ctx);
+    CG_CUDA_TRY(ctx, cudaGetLastError());
+    return CG_OK;
+}
+
+bool adjoint_tc_ok(int lp) { return lp % 16 == 0 && lp >= 16 && lp <= 96; }
+
+// copy slots: as many as fit beside the B stages in 220 KB
+template <int RC>
+static int launch_adj_tc(cg_ctx* ctx, dim3 grid, int B, int lp, const float* U, const float* V, size_t strideA,
+                         float* part, int* d_err, cudaStream_t s)
+{
+    constexpr int NBP = (8 * RC + NPROD - 1) / NPROD, SLOT = NPROD * 16 * (4 + 2 * NBP);
+    constexpr int NCP = (220 * 1024 - NAST * 2 * 2 * RC * KC * 4) / SLOT;
+    static_assert(NCP >= 3, "copy slots");
+    const int smem = NAST * 2 * lp * KC * 4 + NCP * SLOT;
+    CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_adj_tc<RC, NCP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    contract_adj_tc<RC, NCP><<<grid, ADJ_NTH, smem, s>>>(B, lp, U, V, strideA, part, d_err);
+    return CG_OK;
+}
+
+int adjoint_contract_tc(cg_ctx* ctx, int B, int nt, int lp, const float* U, const float* V, size_t strideA,
+                        float* part, int* d_err, cudaStream_t s)
+{
+    if (!adjoint_tc_ok(lp)) { ctx->err = "tensor-core adjoint contraction needs lp % 16 == 0, lp <= 96"; return CG_ERR_BAD_ARG; }
+    const dim3 grid(ntiles_lower(nt), (B + 127) / 128);
+    int rc = (lp <= 64) ? launch_adj_tc<32>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)
+                        : launch_adj_tc<48>(ctx, grid, B, lp, U, V, strideA, part, d_err, s);
+    if (rc) return rc;
     count_launch(ctx);
     CG_CUDA_TRY(ctx, cudaGetLastError());
     return CG_OK;
