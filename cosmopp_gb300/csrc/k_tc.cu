@@ -296,8 +296,10 @@ __device__ __forceinline__ void st_c1_row(float* tile, int rr, const float (&v)[
 //   A_REG_C1  fa(c, r, h, x[4]) loads it as FP32, split when stored to tensor memory;
 //   A_SMEM_C1 fa(c, top, bot, kc) names the two FP32 canonical tiles (rows 0-63, 64-127; nullptr =
 //             zero) and the K chunk within them; the copy warp brings them into a ring of NSTA
-//             shared-memory stages by bulk copies, ahead of the producers.
-enum { A_REG_SC = 0, A_REG_C1 = 1, A_SMEM_C1 = 2 };
+//             shared-memory stages by bulk copies, ahead of the producers;
+//   A_SMEM_PRE (at most NSTA chunks) the producers wrote the FP32 chunks into the ring stages
+//             themselves before the loop (fa unused).
+enum { A_REG_SC = 0, A_REG_C1 = 1, A_SMEM_C1 = 2, A_SMEM_PRE = 3 };
 
 // ---- pieces shared by the single-item K loop and the item stream -----------------------------
 
@@ -309,15 +311,17 @@ template <int AMODE, int NX, class W>
 __device__ __forceinline__ void put_a(int g, float4 (&qx)[NX], W& wait, const float* sa_f, TcCtl& ctl, uint32_t tm)
 {
     const int r = threadIdx.x % 128, h = threadIdx.x / 128, lane = threadIdx.x % 32, st = g % NAST;
-    if constexpr (AMODE == A_SMEM_C1) {
+    if constexpr (AMODE == A_SMEM_C1 || AMODE == A_SMEM_PRE) {
         // this thread's 16 values of the staged chunk (row r, K columns 16h .. 16h+15)
         const int si = g % NSTA;
-        wait(&ctl.as_full[si], (g / NSTA) & 1);
+        if constexpr (AMODE == A_SMEM_C1) wait(&ctl.as_full[si], (g / NSTA) & 1);
         const float* p = sa_f + si * (STA_BYTES / 4) + (r >> 3) * 256 + (r & 7) * 4 + 4 * h * 32;
 #pragma unroll
         for (int i = 0; i < 4; ++i) qx[i] = *reinterpret_cast<const float4*>(p + i * 32);
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&ctl.as_empty[si]);
+        if constexpr (AMODE == A_SMEM_C1) {
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&ctl.as_empty[si]);
+        }
     }
     float4 qh[4], ql[4];
     if constexpr (AMODE == A_REG_SC) {
@@ -425,26 +429,27 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
         // ---- producers
         const int r = threadIdx.x % 128, h = threadIdx.x / 128;
         constexpr int NX = (AMODE == A_REG_SC) ? 8 : 4;
+        constexpr bool REG = (AMODE == A_REG_SC || AMODE == A_REG_C1);
         float4 a0[NX], a1[NX];  // register modes: the loaded A of two chunks (slot = chunk & 1)
         // chunks 0 and 1 into the empty stages 0 and 1; register modes load two chunks ahead of the store
-        if constexpr (AMODE != A_SMEM_C1) {
+        if constexpr (REG) {
             if (nchunks > 0) fa(0, r, h, a0);
             if (nchunks > 1) fa(1, r, h, a1);
         }
         if (nchunks > 0) {
             put_a<AMODE>(0, a0, wait, sa_f, ctl, tm);
-            if constexpr (AMODE != A_SMEM_C1) { if (nchunks > 2) fa(2, r, h, a0); }
+            if constexpr (REG) { if (nchunks > 2) fa(2, r, h, a0); }
         }
         if (nchunks > 1) {
             put_a<AMODE>(1, a1, wait, sa_f, ctl, tm);
-            if constexpr (AMODE != A_SMEM_C1) { if (nchunks > 3) fa(3, r, h, a1); }
+            if constexpr (REG) { if (nchunks > 3) fa(3, r, h, a1); }
         }
         // step c: chunk c - 2 is retired and its A stage takes chunk c + 2 (held in slot qx = c & 1)
         auto step = [&](int c, float4 (&qx)[NX]) {
             if (c >= 2) retire_acc(c - 2, false, wait, ok, err, ctl, tm, R);
             if (c + 2 < nchunks) {
                 put_a<AMODE>(c + 2, qx, wait, sa_f, ctl, tm);
-                if constexpr (AMODE != A_SMEM_C1) { if (c + 4 < nchunks) fa(c + 4, r, h, qx); }
+                if constexpr (REG) { if (c + 4 < nchunks) fa(c + 4, r, h, qx); }
             }
         };
         for (int c = 0; c < nchunks; c += 2) {
@@ -964,7 +969,8 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_panel(int J2, int nt, int B, f
 }
 
 // Row block I2 of M = L^-1, off-diagonal blocks J2 = blockIdx.x < I2; grid (I2, B).  Computes
-// the transposes: S^T = sum_{k=2 J2}^{2 I2 - 1} M_kJ^T L_Ik^T, then (M_IJ)^T = -S^T Linv_I^T.
+// the transposes: S^T = sum_{k=2 J2}^{2 I2 - 1} M_kJ^T L_Ik^T, then (M_IJ)^T = -S^T Linv_I^T with
+// S^T kept in shared memory.
 __global__ void __launch_bounds__(NTH, 1) trtri_tc_row(int I2, int nt, const float* __restrict__ Ls,
                                                        const float* __restrict__ Linv, float* __restrict__ Ms,
                                                        float* __restrict__ Mc, int* __restrict__ err)
@@ -996,17 +1002,23 @@ __global__ void __launch_bounds__(NTH, 1) trtri_tc_row(int I2, int nt, const flo
     };
     float R[64];
     tc_kloop<A_SMEM_C1>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
-    // S^T into the M storage of block (I2, J2): row = M's column, K = M's rows 64h .. 64h+63
-    if (threadIdx.x < NPROD)
-        st_c1_row(Mcb + (size_t)tile_index(2 * I2 + h, 2 * J2 + row / 64) * C1_TILE, row % 64, R, 1.f);
-    tc_rearm(ctl);  // its __syncthreads also makes the S^T stores visible to the whole CTA
-    // A(c, m) = S^T(c, m): written above by this CTA (coherent loads); B(r, m) = Linv_I(r, m)
-    auto fa2 = [&](int c, int r, int hh, float4 (&x)[4]) {
-        ld_c1<true>(Mcb + (size_t)tile_index(2 * I2 + c / 2, 2 * J2 + r / 64) * C1_TILE, r % 64, c % 2, hh, x);
-    };
+    // S^T stays on chip: into the A ring as the four FP32 canonical K chunks of the second product
+    // (row = M's column, K = M's rows 64h .. 64h+63: chunks 2h, 2h+1).  Every producer's last ring
+    // read came before the last chunk's MMAs, which any producer leaving the loop has waited for.
+    if (threadIdx.x < NPROD) {
+        float* ring = reinterpret_cast<float*>(smem_raw + NSTB * STB_BYTES);
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const int k = 64 * h + 4 * q;
+            *reinterpret_cast<float4*>(ring + (k / KC) * (STA_BYTES / 4) + (row >> 3) * 256 + ((k % KC) >> 2) * 32 +
+                                       (row & 7) * 4) = make_float4(R[4 * q], R[4 * q + 1], R[4 * q + 2], R[4 * q + 3]);
+        }
+    }
+    tc_rearm(ctl);  // its __syncthreads also makes the ring writes visible to all producers
+    // A(c, m) = S^T(c, m) from the ring; B(r, m) = Linv_I(r, m)
+    auto fa2 = [](int, const float*&, const float*&, int&) {};
     auto fb2 = [&](int c, uint32_t dst, uint64_t* bar) { bulk_linv(li, c, dst, bar); };
-    tc_kloop<A_REG_C1>(128 / KC, fa2, fb2, smem_raw, ctl, tm, R, err);
-    __syncthreads();  // every S^T read is done before the tiles are overwritten
+    tc_kloop<A_SMEM_PRE>(128 / KC, fa2, fb2, smem_raw, ctl, tm, R, err);
     if (threadIdx.x < NPROD) {
         const size_t tix = tile_index(2 * I2 + h, 2 * J2 + row / 64);
         st_sc_row(Mb + tix * SC_TILE, row % 64, R, -1.f);
@@ -1068,23 +1080,24 @@ __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restri
 // part[t][b][l] = sum over the entries e of lower tile t of w_e V_b[e] Ubar_l[e], w_e = 2 below the
 // matrix diagonal, 1 on it, 0 above (V symmetric, stored lower): the per-tile terms of
 // Tr(V dA/dC_l).  One GEMM per tile and 128 batch elements: M = 128 (b), N = lp (l), K = the tile's
-// 4096 entries in 32-wide chunks, 3xTF32.  Each producer copies its own pieces of both operands
-// (cp.async, per thread) into a ring of NCP shared-memory slots, NCP - 1 chunks ahead: V streams
-// from DRAM, whose latency registers two chunks ahead did not cover.  It then stores them split:
-// V (A, weighted) into tensor memory, Ubar (B) into a shared-memory stage (K-major canonical, lp
-// rows), so the FP32 table needs no split copy.  One thread issues the MMAs; every chunk's
-// accumulator is folded into round-to-nearest registers (the tensor core's FP32 accumulation
-// drifts one way).  RC >= lp / 2: the accumulator columns a producer drains.
+// 4096 entries in 32-wide chunks, 3xTF32.  The operand rows (128 rows of V, lp of Ubar) are 16 KB
+// apart or more, so they are fetched in groups of G chunks: each warp copies (cp.async) G x 128
+// contiguous bytes of a row at a time into a group buffer, one buffer ahead (fetching 128 bytes of
+// every row per chunk left HBM at a third of its bandwidth).  The producers then store their
+// pieces split: V (A, weighted) into tensor memory, Ubar (B) into a shared-memory stage (K-major
+// canonical, lp rows), so the FP32 table needs no split copy.  One thread issues the MMAs; every
+// chunk's accumulator is folded into round-to-nearest registers (the tensor core's FP32
+// accumulation drifts one way).  RC >= lp / 2: the accumulator columns a producer drains.
 // grid (tiles, ceil(B / 128)).
 constexpr int ADJ_NTH = NPROD + 32;
 
-template <int RC, int NCP>
+template <int RC, int G>
 __global__ void __launch_bounds__(ADJ_NTH, 1) contract_adj_tc(int B, int lp, const float* __restrict__ U,
                                                               const float* __restrict__ V, size_t strideA,
                                                               float* __restrict__ part, int* __restrict__ err)
 {
     constexpr int NBP = (8 * RC + NPROD - 1) / NPROD;  // B pieces (8 K values) per producer and chunk
-    constexpr uint32_t SLOT = NPROD * 16 * (4 + 2 * NBP);  // one copy slot: 16-byte pieces, piece-major
+    constexpr int P = 8 * G;                            // 16-byte pieces of a row in a group
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ uint64_t mma_bar[2], acc_free[2], ab_full[NAST];
     __shared__ uint32_t tbase;
@@ -1115,50 +1128,54 @@ __global__ void __launch_bounds__(ADJ_NTH, 1) contract_adj_tc(int B, int lp, con
     };
     if (warp < NPROD / 32) {
         const int r = threadIdx.x % 128, h = threadIdx.x / 128, b = b0 + r;
-        // rows past B load row B - 1: their products are never stored, and a row touches only its own
-        const float* Vt = V + (size_t)(b < B ? b : B - 1) * strideA + (size_t)t * TILE_ELEMS;
-        const float* Ut = U + (size_t)t * TILE_ELEMS * lp;
         float R[RC];
 #pragma unroll
         for (int j = 0; j < RC; ++j) R[j] = 0.f;
-        // copy slots after the B stages: 16-byte piece q of thread t at slot + (q NPROD + t) 16, so that
-        // a warp's reads of one piece are consecutive.  Pieces 0-3: 16 V entries (row b, K half h);
-        // 4 + 2p, 5 + 2p: Ubar row l = i / 4, K columns 8 (i % 4) .. + 7 for i = t + NPROD p < 4 lp.
-        const uint32_t slots = sb + NAST * stb;
-        auto piece = [&](int c, int q) { return slots + (c % NCP) * SLOT + (q * NPROD + threadIdx.x) * 16; };
-        auto fetch = [&](int c) {
-            if (c < NCH) {
-#pragma unroll
-                for (int i = 0; i < 4; ++i) cp_async16(piece(c, i), Vt + KC * c + 16 * h + 4 * i);
-#pragma unroll
-                for (int p = 0; p < NBP; ++p) {
-                    const int i = threadIdx.x + NPROD * p;
-                    if (i < 4 * lp) {
-                        const float* src = Ut + (size_t)(i / 4) * TILE_ELEMS + KC * c + 8 * (i % 4);
-                        cp_async16(piece(c, 4 + 2 * p), src);
-                        cp_async16(piece(c, 5 + 2 * p), src + 4);
-                    }
+        // two group buffers after the B stages: 128 V rows then lp Ubar rows of P pieces, piece j of
+        // row q at physical piece j ^ (q % P), so that the producers' reads (one row per lane) and
+        // the warps' copies (one row per warp) both spread over the banks
+        const uint32_t gbuf = (uint32_t)(128 + lp) * P * 16;
+        auto gpiece = [&](int k, int q, int j) {
+            return (uint32_t)(NAST * stb + (k & 1) * gbuf + (q * P + (j ^ (q % P))) * 16);
+        };
+        // group k (chunks G k .. G k + G - 1): consecutive threads copy consecutive pieces of a row
+        auto fetch = [&](int k) {
+            if (G * k < NCH) {
+                for (int idx = threadIdx.x; idx < (128 + lp) * P; idx += NPROD) {
+                    const int q = idx / P, j = idx % P;
+                    // rows past B copy row B - 1: their products are never stored, and a row only
+                    // touches its own outputs
+                    const float* src = (q < 128)
+                                           ? V + (size_t)min(b0 + q, B - 1) * strideA + (size_t)t * TILE_ELEMS
+                                           : U + ((size_t)t * lp + (q - 128)) * TILE_ELEMS;
+                    cp_async16(sb + gpiece(k, q, j), src + KC * G * k + 4 * j);
                 }
             }
-            cp_async_commit();  // one group per chunk, empty past the end, so that waits count chunks
+            cp_async_commit();
         };
-        auto rd = [&](int c, int q) {
-            return *reinterpret_cast<const float4*>(smem_raw + (piece(c, q) - sb));
+        auto rd = [&](int k, int q, int j) {
+            return *reinterpret_cast<const float4*>(smem_raw + gpiece(k, q, j));
         };
         // chunk c into stage c % NAST: weighted, split V into tensor memory, split Ubar into shared
-        // memory (this thread's copies of chunk c have landed)
+        // memory.  At the first chunk of a group, the group's copies are waited for and published to
+        // all producers (named barrier), which also frees the other buffer for the next group.
         auto put = [&](int c) {
-            const int st = c % NAST;
+            const int st = c % NAST, k = c / G, cl = c % G;
+            if (cl == 0) {
+                cp_async_wait<0>();
+                asm volatile("bar.sync 1, %0;" ::"n"(NPROD) : "memory");
+                fetch(k + 1);
+            }
             float4 qh[4], ql[4];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                const float4 v = rd(c, i);
+                const float4 v = rd(k, r, 8 * cl + 4 * h + i);
                 float x[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const int e = KC * c + 16 * h + 4 * i + k, rr = e % TS, cc = e / TS;
+                for (int kk = 0; kk < 4; ++kk) {
+                    const int e = KC * c + 16 * h + 4 * i + kk, rr = e % TS, cc = e / TS;
                     const float w = (I != J || rr > cc) ? 2.f : (rr == cc ? 1.f : 0.f);
-                    x[k] *= w;
+                    x[kk] *= w;
                 }
                 qh[i] = make_float4(tf32_rn(x[0]), tf32_rn(x[1]), tf32_rn(x[2]), tf32_rn(x[3]));
                 ql[i] = make_float4(tf32_rn(x[0] - qh[i].x), tf32_rn(x[1] - qh[i].y), tf32_rn(x[2] - qh[i].z),
@@ -1174,7 +1191,7 @@ __global__ void __launch_bounds__(ADJ_NTH, 1) contract_adj_tc(int B, int lp, con
                     const int l = i / 4, k0 = 8 * (i % 4);
 #pragma unroll
                     for (int q = 0; q < 2; ++q) {
-                        const float4 x = rd(c, 4 + 2 * p + q);
+                        const float4 x = rd(k, 128 + l, 8 * cl + k0 / 4 + q);
                         const float4 hi = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
                         const float4 lo = make_float4(tf32_rn(x.x - hi.x), tf32_rn(x.y - hi.y), tf32_rn(x.z - hi.z),
                                                       tf32_rn(x.w - hi.w));
@@ -1213,22 +1230,14 @@ __global__ void __launch_bounds__(ADJ_NTH, 1) contract_adj_tc(int B, int lp, con
             __syncwarp();
             if (lane == 0) mbar_arrive(&acc_free[c & 1]);
         };
-        // copies run NCP - 1 chunks ahead of the stores, the stores two chunks ahead of the MMAs:
-        // step c retires chunk c - 2, stores chunk c + 2 into its stage and fetches chunk c + 1 + NCP
-        for (int c = 0; c < NCP - 1; ++c) fetch(c);
-        cp_async_wait<NCP - 2>();
+        // groups are fetched one ahead of the stores, the stores run two chunks ahead of the MMAs:
+        // step c retires chunk c - 2 and stores chunk c + 2 into its stage
+        fetch(0);
         put(0);
-        fetch(NCP - 1);
-        cp_async_wait<NCP - 2>();
         put(1);
-        fetch(NCP);
         for (int c = 0; c < NCH; ++c) {
             if (c >= 2) retire(c - 2, false);
-            if (c + 2 < NCH) {
-                cp_async_wait<NCP - 2>();
-                put(c + 2);
-                fetch(c + 1 + NCP);
-            }
+            if (c + 2 < NCH) put(c + 2);
         }
         cp_async_wait<0>();
         retire(NCH - 2, true);
@@ -1354,17 +1363,15 @@ int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, const float* Mc,
 
 bool adjoint_tc_ok(int lp) { return lp % 16 == 0 && lp >= 16 && lp <= 96; }
 
-// copy slots: as many as fit beside the B stages in 220 KB
-template <int RC>
+// G chunks per fetch group: two group buffers and the B stages within 224 KB
+template <int RC, int G>
 static int launch_adj_tc(cg_ctx* ctx, dim3 grid, int B, int lp, const float* U, const float* V, size_t strideA,
                          float* part, int* d_err, cudaStream_t s)
 {
-    constexpr int NBP = (8 * RC + NPROD - 1) / NPROD, SLOT = NPROD * 16 * (4 + 2 * NBP);
-    constexpr int NCP = (220 * 1024 - NAST * 2 * 2 * RC * KC * 4) / SLOT;
-    static_assert(NCP >= 3, "copy slots");
-    const int smem = NAST * 2 * lp * KC * 4 + NCP * SLOT;
-    CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_adj_tc<RC, NCP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    contract_adj_tc<RC, NCP><<<grid, ADJ_NTH, smem, s>>>(B, lp, U, V, strideA, part, d_err);
+    static_assert(NAST * 2 * 2 * RC * KC * 4 + 2 * (128 + 2 * RC) * G * 128 <= 224 * 1024, "shared memory");
+    const int smem = NAST * 2 * lp * KC * 4 + 2 * (128 + lp) * G * 128;
+    CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_adj_tc<RC, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    contract_adj_tc<RC, G><<<grid, ADJ_NTH, smem, s>>>(B, lp, U, V, strideA, part, d_err);
     return CG_OK;
 }
 
@@ -1373,8 +1380,9 @@ int adjoint_contract_tc(cg_ctx* ctx, int B, int nt, int lp, const float* U, cons
 {
     if (!adjoint_tc_ok(lp)) { ctx->err = "tensor-core adjoint contraction needs lp % 16 == 0, lp <= 96"; return CG_ERR_BAD_ARG; }
     const dim3 grid(ntiles_lower(nt), (B + 127) / 128);
-    int rc = (lp <= 64) ? launch_adj_tc<32>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)
-                        : launch_adj_tc<48>(ctx, grid, B, lp, U, V, strideA, part, d_err, s);
+    int rc = (lp <= 48)   ? launch_adj_tc<24, 4>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)
+             : (lp <= 64) ? launch_adj_tc<32, 2>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)
+                          : launch_adj_tc<48, 2>(ctx, grid, B, lp, U, V, strideA, part, d_err, s);
     if (rc) return rc;
     count_launch(ctx);
     CG_CUDA_TRY(ctx, cudaGetLastError());
