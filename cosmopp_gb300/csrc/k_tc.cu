@@ -640,30 +640,23 @@ __device__ __forceinline__ void store_block(const float (&R)[64], float* base, i
     for (int j = 0; j < 64; ++j) t[(row % 64) + TS * j] = sgn * R[j];
 }
 
-// Cholesky of the 128x128 block in s (column-major, leading dimension 129, lower part used)
-// and the inverse of its factor into inv (same layout, zero above the diagonal); all NTH
-// threads take part (every __syncthreads is reached by all).  Sets *bad on a non-positive pivot.
-//
-// Factorisation, panels of 8 columns.  The updates from factorised panels are summed in u
-// (inv's storage) and subtracted from a column once, when its panel is reached: subtracting
-// each term from s directly drops the terms below half an ulp of the diagonal (about 1 after
-// whitening) and biases the log-determinant upwards.  Per panel, every thread factors the
-// panel's 8x8 diagonal block itself (same operands and operation order in every thread, so the
-// same values) and then its own row's 8 values, so a panel needs no barrier until its
-// columns are written.  The trailing sums are then updated from those rows in registers,
-// two threads per row.
-// Inverse: L11^-1 and L22^-1 (64x64 halves) by per-column forward substitution, one thread
-// per column, both halves at once; then T = L21 L11^-1 and L21' = -L22^-1 T as register-
-// blocked 64x64 products (4x4 outputs per thread).
-__device__ void factor_block128(float* s, float* inv, float* tmp, int* bad)
+// Cholesky of the 64x64 diagonal block at (o, o) of s (column-major, leading dimension 129, lower
+// part), in place.  The updates from factorised panels are summed in u (the same positions of u's
+// storage) and subtracted from a column once, when its panel is reached: subtracting each term
+// from s directly drops the terms below half an ulp of the diagonal (about 1 after whitening) and
+// biases the log-determinant upwards.  Panels of 8 columns: every thread factors the panel's 8x8
+// diagonal block itself (same operands and operation order in every thread, so the same values) and
+// then its own row's 8 values, so a panel needs no barrier until its columns are written; the
+// trailing sums are then updated four threads per row.  All NTH threads take part (every barrier is
+// reached by all).  Sets *bad on a non-positive pivot.
+__device__ void factor_block64(float* s, float* u, int o, int* bad)
 {
     constexpr int L = 129;
     const int t = threadIdx.x;
-    float* u = inv;
-    for (int e = t; e < 128 * 128; e += NTH) u[(e / 128) * L + e % 128] = 0.f;
+    for (int e = t; e < 64 * 64; e += NTH) u[(o + e / 64) * L + o + e % 64] = 0.f;
     __syncthreads();
-    const int r = t % 128, part = t / 128;  // threads t >= 256 only reach the barriers
-    for (int kb = 0; kb < 128; kb += 8) {
+    const int r = o + t % 64, part = t / 64;  // parts 0-3 share the row's trailing sums; t >= 256 idle
+    for (int kb = o; kb < o + 64; kb += 8) {
         float lb[8][8], rv[8], lr[8];
         // the panel's 8x8 diagonal block, in every thread
 #pragma unroll
@@ -707,15 +700,15 @@ __device__ void factor_block128(float* s, float* inv, float* tmp, int* bad)
                 }
         }
         __syncthreads();  // every read of the panel's columns is done
-        if (t < 128) {
+        if (t < 64) {
 #pragma unroll
             for (int j = 0; j < 8; ++j)
                 if (r >= kb + j) s[(kb + j) * L + r] = lr[j];
         }
         __syncthreads();
-        // u[q][r] += sum_j L[r][kb+j] L[q][kb+j] for kb + 8 <= q <= r; q of this thread's parity
+        // u[q][r] += sum_j L[r][kb+j] L[q][kb+j] for kb + 8 <= q <= r; q = kb + 8 + part (mod 4)
         if (t < 256 && r >= kb + 8) {
-            for (int q = kb + 8 + part; q <= r; q += 2) {
+            for (int q = kb + 8 + part; q <= r; q += 4) {
                 float acc = u[q * L + r];
 #pragma unroll
                 for (int j = 0; j < 8; ++j) acc = fmaf(lr[j], s[(kb + j) * L + q], acc);
@@ -724,41 +717,120 @@ __device__ void factor_block128(float* s, float* inv, float* tmp, int* bad)
         }
         __syncthreads();
     }
-    // L11^-1 (t < 64) and L22^-1 (64 <= t < 128): column c of the half at offset o, by row blocks
-    // of 8; 1 / L_cc recomputed from the stored diagonal
-    if (t < 128) {
-        const int o = (t < 64) ? 0 : 64, c = o + t % 64;
-        for (int m = 0; m < 128; ++m)
-            if (m < c || m >= o + 64) inv[c * L + m] = 0.f;
-        for (int R = (c - o) / 8; R < 8; ++R) {
-            const int r0 = o + 8 * R;
-            float acc[8];
+}
+
+// inverse of the lower-triangular 64x64 block at (o, o) of s into the same block of inv (zero above
+// its diagonal): column c = o + t of the inverse by forward substitution in row blocks of 8, one
+// thread per column (t < 64); 1 / L_cc recomputed from the stored diagonal
+__device__ void invert_block64(const float* s, float* inv, int o)
+{
+    constexpr int L = 129;
+    const int t = threadIdx.x;
+    if (t >= 64) return;
+    const int c = o + t;
+    for (int m = o; m < c; ++m) inv[c * L + m] = 0.f;
+    for (int R = t / 8; R < 8; ++R) {
+        const int r0 = o + 8 * R;
+        float acc[8];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) acc[i] = (r0 + i == c) ? 1.f : 0.f;
+        for (int i = 0; i < 8; ++i) acc[i] = (r0 + i == c) ? 1.f : 0.f;
 #pragma unroll 2
-            for (int m = c; m < r0; ++m) {
-                const float x = inv[c * L + m];
+        for (int m = c; m < r0; ++m) {
+            const float x = inv[c * L + m];
 #pragma unroll
-                for (int i = 0; i < 8; ++i) acc[i] = fmaf(-s[m * L + r0 + i], x, acc[i]);
+            for (int i = 0; i < 8; ++i) acc[i] = fmaf(-s[m * L + r0 + i], x, acc[i]);
+        }
+        float y[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+            float v = acc[i];
+#pragma unroll
+            for (int k = 0; k < i; ++k) v = fmaf(-s[(r0 + k) * L + r0 + i], y[k], v);
+            y[i] = (r0 + i < c) ? 0.f : v / s[(r0 + i) * L + r0 + i];
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) inv[c * L + r0 + i] = y[i];
+    }
+}
+
+// Cholesky of the 128x128 block in s (column-major, leading dimension 129, lower part used) and
+// the inverse of its factor into inv (same layout, zero above the diagonal); all NTH threads take
+// part (every __syncthreads is reached by all).  Sets *bad on a non-positive pivot.  Blocked in
+// 64x64 halves, so that most of the work is in register-blocked 64x64 products (4x4 outputs per
+// thread, t < 256) rather than in the latency-bound panel steps:
+//   L11 = chol(S11), L11^-1;  L21 = S21 L11^-T;  S22' = S22 - L21 L21^T (one subtraction per
+//   element, the sum formed first);  L22 = chol(S22'), L22^-1;  (L^-1)21 = -L22^-1 (L21 L11^-1).
+__device__ void factor_block128(float* s, float* inv, float* tmp, int* bad)
+{
+    constexpr int L = 129;
+    const int t = threadIdx.x;
+    const int i0 = 4 * (t % 16), j0 = 4 * ((t / 16) % 16);  // this thread's 4x4 outputs of a 64x64 product
+    factor_block64(s, inv, 0, bad);
+    invert_block64(s, inv, 0);
+    for (int e = t; e < 64 * 64; e += NTH) inv[(64 + e / 64) * L + e % 64] = 0.f;  // upper-right block
+    __syncthreads();
+    // L21 = S21 L11^-T: L21[i][j] = sum_{k <= j} S21[i][k] L11^-1[j][k]
+    float acc[4][4] = {};
+    if (t < 256) {
+        for (int k = 0; k < j0 + 4; ++k) {
+            float a4[4], b4[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                a4[q] = s[k * L + 64 + i0 + q];
+                b4[q] = inv[k * L + j0 + q];
             }
-            float y[8];
 #pragma unroll
-            for (int i = 0; i < 8; ++i) {
-                float v = acc[i];
+            for (int p = 0; p < 4; ++p)
 #pragma unroll
-                for (int k = 0; k < i; ++k) v = fmaf(-s[(r0 + k) * L + r0 + i], y[k], v);
-                y[i] = (r0 + i < c) ? 0.f : v / s[(r0 + i) * L + r0 + i];
-            }
-#pragma unroll
-            for (int i = 0; i < 8; ++i) inv[c * L + r0 + i] = y[i];
+                for (int q = 0; q < 4; ++q) acc[p][q] = fmaf(a4[p], b4[q], acc[p][q]);
         }
     }
-    __syncthreads();
-    // T = L21 L11^-1 into tmp (tmp[j * 65 + i] = T[i][j]); thread: rows i0.., columns j0..
-    const int i0 = 4 * (t % 16), j0 = 4 * ((t / 16) % 16);
+    __syncthreads();  // every read of S21 is done
     if (t < 256) {
-        float acc[4][4] = {};
-        for (int k = j0; k < 64; ++k) {  // L11^-1[k][j] = 0 for k < j
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) s[(j0 + q) * L + 64 + i0 + p] = acc[p][q];
+    }
+    __syncthreads();
+    // S22' = S22 - L21 L21^T on the lower part (each thread reads and writes only its own outputs of S22)
+    if (t < 256 && i0 + 3 >= j0) {
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[p][q] = 0.f;
+        for (int k = 0; k < 64; ++k) {
+            float a4[4], b4[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                a4[q] = s[k * L + 64 + i0 + q];
+                b4[q] = s[k * L + 64 + j0 + q];
+            }
+#pragma unroll
+            for (int p = 0; p < 4; ++p)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[p][q] = fmaf(a4[p], b4[q], acc[p][q]);
+        }
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (i0 + p >= j0 + q) {
+                    float* x = &s[(64 + j0 + q) * L + 64 + i0 + p];
+                    *x = *x - acc[p][q];
+                }
+    }
+    __syncthreads();
+    factor_block64(s, inv, 64, bad);
+    invert_block64(s, inv, 64);
+    __syncthreads();
+    // T = L21 L11^-1 into tmp (tmp[j * 65 + i] = T[i][j]); L11^-1[k][j] = 0 for k < j
+    if (t < 256) {
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[p][q] = 0.f;
+        for (int k = j0; k < 64; ++k) {
             float a4[4], b4[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
@@ -776,10 +848,13 @@ __device__ void factor_block128(float* s, float* inv, float* tmp, int* bad)
             for (int q = 0; q < 4; ++q) tmp[(j0 + q) * 65 + i0 + p] = acc[p][q];
     }
     __syncthreads();
-    // L21' = -L22^-1 T into inv rows 64..127, columns 0..63; the upper-right block stays zero
+    // (L^-1)21 = -L22^-1 T into inv rows 64..127, columns 0..63; L22^-1[i][k] = 0 for k > i
     if (t < 256) {
-        float acc[4][4] = {};
-        for (int k = 0; k <= i0 + 3; ++k) {  // L22^-1[i][k] = 0 for k > i
+#pragma unroll
+        for (int p = 0; p < 4; ++p)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[p][q] = 0.f;
+        for (int k = 0; k <= i0 + 3; ++k) {
             float a4[4], b4[4];
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
