@@ -250,6 +250,15 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const float (&v)[32])
     asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
+// (r0, r1) += (m0, m1) as one packed two-lane FP32 add (round to nearest, like two FADDs)
+__device__ __forceinline__ void add2(float& r0, float& r1, float m0, float m1)
+{
+    asm("{\n\t.reg .b64 ra, rb;\n\tmov.b64 ra, {%0, %1};\n\tmov.b64 rb, {%2, %3};\n\t"
+        "add.rn.f32x2 ra, ra, rb;\n\tmov.b64 {%0, %1}, ra;\n\t}"
+        : "+f"(r0), "+f"(r1)
+        : "f"(m0), "f"(m1));
+}
+
 // the TF32 part the tensor core keeps (top 19 bits) and the FP32 remainder
 __device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
 // x rounded to the nearest TF32 value (ties away from zero); the tensor core then reads it exactly

@@ -4,9 +4,10 @@
 // and a_lo = a - a_hi rounded to nearest TF32 (unbiased; truncating instead
 // biases sums of squares).  The tensor core's FP32 accumulation is not
 // round-to-nearest and drifts by ~0.4 ulp per instruction, always the same
-// way, so each chunk's 12 MMAs (K = 32) go to a fresh tensor-memory
-// accumulator that is folded into a per-thread FP32 register sum
-// (round-to-nearest) two chunks later: the drift stays bounded by one chunk's.
+// way, so the 24 MMAs of each chunk pair (one 64-wide K tile) go to a fresh
+// tensor-memory accumulator that is folded into a per-thread FP32 register sum
+// (round-to-nearest) once the pair is done: the drift stays bounded by one
+// tile's.  (Every K loop covers whole tiles, so its chunk count is even.)
 //
 // Operand storage ("split canonical", SC): every factor these kernels consume
 // is stored already split, hi and lo planes, each 64-row x 32-K block in the
@@ -22,16 +23,17 @@
 // One CTA owns a 128x128 output supertile (2x2 storage tiles) and runs a
 // warp-specialised K loop over 32-wide chunks, the roles handing off through
 // mbarriers only:
-//   warps 0-7  (producers): when chunk c's MMAs are done, fold its accumulator
-//              into registers and release it, then store the A operand of chunk
-//              c + 4 into the tensor-memory stage chunk c used (four stages);
-//              thread t handles row t % 128, K half t / 128;
-//   warps 8,10 (MMA issue): one thread each, for the even and the odd chunks,
-//              issues the chunk's 12 MMAs (M128 N128 K8, A from tensor memory, B
-//              from shared memory) once its A, its B and its accumulator are ready,
-//              and commits them to the chunk's mbarriers.  Issue blocks while the
-//              tensor pipe is busy, so with one issuer the pipe idled during every
-//              barrier wait; with two, one issuer waits while the other's MMAs run;
+//   warps 0-7  (producers): when chunk c's MMAs are done, store the A operand of
+//              chunk c + 4 into the tensor-memory stage chunk c used (four stages)
+//              and, at the end of a chunk pair, fold the pair's accumulator into
+//              registers and release it; thread t handles row t % 128, K half t / 128;
+//   warps 8,10 (MMA issue): one thread each, for alternate chunk pairs (chunks
+//              4k, 4k + 1 and 4k + 2, 4k + 3), issues a chunk's 12 MMAs (M128 N128
+//              K8, A from tensor memory, B from shared memory) once its A, its B and
+//              its accumulator are ready, and commits them to the stage's mbarriers.
+//              Issue blocks while the tensor pipe is busy, so with one issuer the pipe
+//              idled during every barrier wait; with two, one issuer waits while the
+//              other's MMAs run;
 //   warp 9     (copies): one thread keeps a ring of NSTB shared-memory B stages
 //              (and NSTA A stages, for A streamed through shared memory) filled
 //              with bulk copies, refilling a stage when its readers are done.
@@ -80,11 +82,11 @@ constexpr int LINV_SC = 4 * LI_CHUNK;           // floats per Linv block (128 KB
 
 static_assert(SC_CHUNK * 4 == 8192 && LI_CHUNK * 4 == (int)STB_BYTES, "layout sizes");
 // Chunk c goes to B stage c % NSTB and tensor-memory A stage c % NAST, and is issued by the issuer
-// of parity c % 2.  Even stage counts give every stage to one issuer, which then waits on the
-// stage's barriers phase by phase in order.  With an odd count the issuer that is ahead could
-// wait for a phase two ahead of the barrier, which a parity wait reports as complete: it would
-// read a stage whose copy is still in flight.
-static_assert(NSTB % 2 == 0 && NAST % 2 == 0, "stage counts must be even (one issuer per stage)");
+// of pair parity (c / 2) % 2.  Stage counts of 4 give every stage to one issuer, which then waits
+// on the stage's barriers phase by phase in order.  Otherwise the issuer that is ahead could wait
+// for a phase two ahead of the barrier, which a parity wait reports as complete: it would read a
+// stage whose copy is still in flight.
+static_assert(NSTB == 4 && NAST == 4, "one issuer per stage");
 
 // zero 64 x 32 block: the source of bulk copies for operand tiles above the diagonal
 __device__ __align__(128) float g_zero_block[SC_CHUNK];
@@ -107,13 +109,13 @@ __device__ __forceinline__ void drain(uint32_t tm, uint32_t col, float (&R)[64])
         float m[32];
         tmem_ld32w(tm + lane_base() + col + 64 * (threadIdx.x / 128) + 32 * half, m);
 #pragma unroll
-        for (int i = 0; i < 32; ++i) R[32 * half + i] += m[i];
+        for (int i = 0; i < 32; i += 2) add2(R[32 * half + i], R[32 * half + i + 1], m[i], m[i + 1]);
     }
 }
 
 struct TcCtl {
-    uint64_t mma_bar[2];      // chunk parity: the chunk's MMAs completed (A stage free, sum ready)
-    uint64_t acc_free[2];     // chunk parity: the accumulator was drained (one arrival per producer warp)
+    uint64_t mma_bar[NAST];   // stage: the MMAs of its chunk completed (its A and B stages are free)
+    uint64_t acc_free[2];     // pair parity: the pair's accumulator was drained (one arrival per producer warp)
     uint64_t a_full[NAST];    // A stage: the chunk's A is in tensor memory (one arrival per producer warp)
     uint64_t b_full[NSTB];    // B stage landed
     uint64_t b_empty[NSTB];   // B stage's MMAs completed
@@ -128,10 +130,8 @@ struct TcCtl {
 
 __device__ __forceinline__ void init_bars(TcCtl& ctl)
 {
-    for (int i = 0; i < 2; ++i) {
-        mbar_init(&ctl.mma_bar[i], 1);
-        mbar_init(&ctl.acc_free[i], NPROD / 32);
-    }
+    for (int i = 0; i < NAST; ++i) mbar_init(&ctl.mma_bar[i], 1);
+    for (int i = 0; i < 2; ++i) mbar_init(&ctl.acc_free[i], NPROD / 32);
     for (int i = 0; i < NAST; ++i) mbar_init(&ctl.a_full[i], NPROD / 32);
     for (int i = 0; i < NSTB; ++i) {
         mbar_init(&ctl.b_full[i], 1);
@@ -175,7 +175,7 @@ __device__ __forceinline__ void tc_rearm(TcCtl& ctl)
     __syncthreads();
     if (threadIdx.x == 0) {
         uint64_t* all = &ctl.mma_bar[0];  // every barrier of TcCtl, contiguous
-        for (int i = 0; i < 4 + NAST + 2 * NSTB + 2 * NSTA + 2 * NIQ; ++i)
+        for (int i = 0; i < 2 * NAST + 2 + 2 * NSTB + 2 * NSTA + 2 * NIQ; ++i)
             asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(all + i)));
         init_bars(ctl);
     }
@@ -209,14 +209,17 @@ __device__ __forceinline__ void ld_c1(const float* t, int rr, int kc, int h, flo
     }
 }
 
-// x = hi + lo with hi = x rounded to nearest TF32 and lo = (x - hi) rounded to nearest TF32
+// x = hi + lo with hi = x rounded to nearest TF32 and lo = (x - hi) rounded to nearest TF32 (the
+// differences are exact; formed as packed two-lane adds of -hi)
 __device__ __forceinline__ void split4(const float4 (&x)[4], float4 (&hi)[4], float4 (&lo)[4])
 {
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         hi[i] = make_float4(tf32_rn(x[i].x), tf32_rn(x[i].y), tf32_rn(x[i].z), tf32_rn(x[i].w));
-        lo[i] = make_float4(tf32_rn(x[i].x - hi[i].x), tf32_rn(x[i].y - hi[i].y), tf32_rn(x[i].z - hi[i].z),
-                            tf32_rn(x[i].w - hi[i].w));
+        float d0 = x[i].x, d1 = x[i].y, d2 = x[i].z, d3 = x[i].w;
+        add2(d0, d1, -hi[i].x, -hi[i].y);
+        add2(d2, d3, -hi[i].z, -hi[i].w);
+        lo[i] = make_float4(tf32_rn(d0), tf32_rn(d1), tf32_rn(d2), tf32_rn(d3));
     }
 }
 
@@ -341,47 +344,48 @@ __device__ __forceinline__ void put_a(int g, float4 (&qx)[NX], W& wait, const fl
     if (lane == 0) mbar_arrive(&ctl.a_full[st]);
 }
 
-// chunk g's MMAs are done: fold its accumulator into R and release it (one arrival per warp).  With
-// `last` the wait ignores the abort flag: every MMA that was issued completes, and none may still
-// run when tensor memory is freed.
+// chunk g's MMAs are done (its stages are free); with `fold` (g ends its pair) fold the pair's
+// accumulator into R and release it (one arrival per warp).  With `last` the wait ignores the abort
+// flag: every MMA that was issued completes, and none may still run when tensor memory is freed.
 template <class W>
-__device__ __forceinline__ void retire_acc(int g, bool last, W& wait, bool& ok, int* err, TcCtl& ctl, uint32_t tm,
-                                           float (&R)[64])
+__device__ __forceinline__ void retire_acc(int g, bool last, bool fold, W& wait, bool& ok, int* err, TcCtl& ctl,
+                                           uint32_t tm, float (&R)[64])
 {
     if (!last) {
-        wait(&ctl.mma_bar[g & 1], (g >> 1) & 1);
-    } else if (!mbar_wait(&ctl.mma_bar[g & 1], (g >> 1) & 1, kMaxIter)) {
+        wait(&ctl.mma_bar[g % NAST], (g / NAST) & 1);
+    } else if (!mbar_wait(&ctl.mma_bar[g % NAST], (g / NAST) & 1, kMaxIter)) {
         ok = false;
         atomicExch(err, 1);
     }
+    if (!fold) return;
     fence_after();
-    drain(tm, col_main(g & 1), R);
+    drain(tm, col_main((g >> 1) & 1), R);
     fence_before();
     __syncwarp();
-    if (threadIdx.x % 32 == 0) mbar_arrive(&ctl.acc_free[g & 1]);
+    if (threadIdx.x % 32 == 0) mbar_arrive(&ctl.acc_free[(g >> 1) & 1]);
 }
 
 // one issuer thread: chunk g's 12 MMAs (M128 N128 K8, A from tensor-memory stage g % NAST, B from
-// shared-memory stage g % NSTB) into the accumulator of parity g & 1, once its A, its B and its
-// accumulator are ready, committed to the chunk's mbarriers
+// shared-memory stage g % NSTB) into the accumulator of its pair's parity (fresh at the pair's first
+// chunk), once its A, its B and its accumulator are ready, committed to the stage's mbarriers
 template <class W>
 __device__ __forceinline__ void issue_chunk(int g, W& wait, TcCtl& ctl, uint32_t tm, uint32_t sb)
 {
-    const int st = g % NAST, sbi = g % NSTB;
+    const int st = g % NAST, sbi = g % NSTB, pr = g >> 1;
     wait(&ctl.a_full[st], (g / NAST) & 1);
     wait(&ctl.b_full[sbi], (g / NSTB) & 1);
-    if (g >= 2) wait(&ctl.acc_free[g & 1], ((g - 2) >> 1) & 1);
+    if ((g & 1) == 0 && pr >= 2) wait(&ctl.acc_free[pr & 1], ((pr - 2) >> 1) & 1);
     fence_after();
     const uint32_t bh = sb + sbi * STB_BYTES, bl = bh + STB_BYTES / 2;
-    const uint32_t ah = tm + col_a_hi(st), al = tm + col_a_lo(st), d = tm + col_main(g & 1);
+    const uint32_t ah = tm + col_a_hi(st), al = tm + col_a_lo(st), d = tm + col_main(pr & 1);
 #pragma unroll
     for (int kk = 0; kk < KC / 8; ++kk) {
         const uint32_t off = kk * 2 * LBO;
-        mma_tf32_ta(d, al + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, kk ? 1u : 0u);
+        mma_tf32_ta(d, al + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, ((g & 1) || kk) ? 1u : 0u);
         mma_tf32_ta(d, ah + 8 * kk, smem_desc(bh + off, LBO, SBO), IDESC, 1u);
         mma_tf32_ta(d, ah + 8 * kk, smem_desc(bl + off, LBO, SBO), IDESC, 1u);
     }
-    mma_commit(&ctl.mma_bar[g & 1]);
+    mma_commit(&ctl.mma_bar[st]);
     mma_commit(&ctl.b_empty[sbi]);
 }
 
@@ -405,7 +409,7 @@ __device__ __forceinline__ void copy_chunk(int g, W& wait, TcCtl& ctl, uint32_t 
 
 // ---- the K loop of one item ------------------------------------------------------------------
 
-// nchunks chunks; fb(c, dst, bar) issues the B chunk's bulk copies into shared memory at dst.
+// nchunks chunks (even); fb(c, dst, bar) issues the B chunk's bulk copies into shared memory at dst.
 // Called by every thread of the CTA.  On return the producer threads (t < NPROD) hold in R[j] the
 // product for row t % 128, column 64 (t / 128) + j (0 if nchunks == 0).  Returns false if an
 // mbarrier wait gave up; waits give up early once *err is set (by this or any other CTA), and a
@@ -446,7 +450,7 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
         }
         // step c: chunk c - 2 is retired and its A stage takes chunk c + 2 (held in slot qx = c & 1)
         auto step = [&](int c, float4 (&qx)[NX]) {
-            if (c >= 2) retire_acc(c - 2, false, wait, ok, err, ctl, tm, R);
+            if (c >= 2) retire_acc(c - 2, false, (c & 1) != 0, wait, ok, err, ctl, tm, R);
             if (c + 2 < nchunks) {
                 put_a<AMODE>(c + 2, qx, wait, sa_f, ctl, tm);
                 if constexpr (REG) { if (c + 4 < nchunks) fa(c + 4, r, h, qx); }
@@ -456,11 +460,15 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
             step(c, a0);
             if (c + 1 < nchunks) step(c + 1, a1);
         }
-        for (int c = (nchunks >= 2 ? nchunks - 2 : 0); c < nchunks; ++c) retire_acc(c, true, wait, ok, err, ctl, tm, R);
+        for (int c = (nchunks >= 2 ? nchunks - 2 : 0); c < nchunks; ++c)
+            retire_acc(c, true, (c & 1) || c == nchunks - 1, wait, ok, err, ctl, tm, R);
     } else if (warp == NPROD / 32 || warp == NPROD / 32 + 2) {
-        // ---- MMA issue: the even chunks from warp 8, the odd ones from warp 10
+        // ---- MMA issue: chunk pairs 0, 2, 4, ... from warp 8, pairs 1, 3, 5, ... from warp 10
         if (lane == 0)
-            for (int c = (warp == NPROD / 32) ? 0 : 1; c < nchunks; c += 2) issue_chunk(c, wait, ctl, tm, sb);
+            for (int c = (warp == NPROD / 32) ? 0 : 2; c < nchunks; c += 4) {
+                issue_chunk(c, wait, ctl, tm, sb);
+                if (c + 1 < nchunks) issue_chunk(c + 1, wait, ctl, tm, sb);
+            }
         __syncwarp();
     } else {
         // ---- copies: one thread keeps the B ring (and, for A_SMEM_C1, the A ring) full
@@ -483,7 +491,7 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
 // while the previous item is still in the tensor pipe and a CTA pays its set-up and its first
 // loads' latency once, not per item.  Taking items in order keeps the CTAs running together on
 // neighbouring items (a static share per CTA lets them drift apart).
-// geo(it) gives item it's geometry (a struct whose member n >= 1 is its chunk count), worked out
+// geo(it) gives item it's geometry (a struct whose member n, even and >= 2, is its chunk count), worked out
 // once per item by each role; fa(gm, c, ...) (as for tc_kloop) and fb(gm, c, dst, bar) receive it.
 // Once the last chunk of an item is folded in, the producer threads (t < NPROD) call epi(gm, R)
 // with R[j] its product at row t % 128, column 64 (t / 128) + j, then clear R.  Called by every
@@ -558,7 +566,7 @@ __device__ bool tc_stream(int nitems, int* queue, GEO geo, FA fa, FB fb, FE epi,
             next(pq, REL_NONE);
         };
         auto retire = [&](int g, bool last) {
-            retire_acc(g, last, wait, ok, err, ctl, tm, R);
+            retire_acc(g, last, (g & 1) || dq.c == dq.gm.n - 1, wait, ok, err, ctl, tm, R);
             if (dq.c == dq.gm.n - 1) {
                 epi(dq.gm, R);
 #pragma unroll
@@ -592,13 +600,13 @@ __device__ bool tc_stream(int nitems, int* queue, GEO geo, FA fa, FB fb, FE epi,
         }
         for (int g = (nput >= 2 ? nput - 2 : 0); g < nput; ++g) retire(g, true);
     } else if (warp == NPROD / 32 || warp == NPROD / 32 + 2) {
-        // ---- MMA issue: the even chunks of the stream from warp 8, the odd ones from warp 10
+        // ---- MMA issue: chunk pairs 0, 2, 4, ... of the stream from warp 8, pairs 1, 3, ... from warp 10
         const int par = (warp == NPROD / 32) ? 0 : 1;
         if (lane == 0) {
             Cur q{};
             enter(q);
             for (int g = 0; q.gm.n; ++g) {
-                if ((g & 1) == par) issue_chunk(g, wait, ctl, tm, sb);
+                if (((g >> 1) & 1) == par) issue_chunk(g, wait, ctl, tm, sb);
                 next(q, REL_ONE);
             }
         }
