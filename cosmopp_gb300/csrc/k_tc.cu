@@ -209,8 +209,11 @@ __device__ __forceinline__ void ld_c1(const float* t, int rr, int kc, int h, flo
     }
 }
 
-// x = hi + lo with hi = x rounded to nearest TF32 and lo = (x - hi) rounded to nearest TF32 (the
-// differences are exact; formed as packed two-lane adds of -hi)
+// x = hi + lo with hi = x rounded to nearest TF32 and lo = x - hi (exact; formed as packed two-lane
+// adds of -hi).  lo is left for the tensor core to truncate to TF32: its sign is that of the
+// rounding of hi, so the truncation is as often up as down, and the error (below 2^-21 of x) is of
+// the size of the a_lo * b_lo term the 3xTF32 split drops anyway.  (Truncating hi instead would make
+// lo always of x's sign and bias sums of squares.)
 __device__ __forceinline__ void split4(const float4 (&x)[4], float4 (&hi)[4], float4 (&lo)[4])
 {
 #pragma unroll
@@ -219,7 +222,7 @@ __device__ __forceinline__ void split4(const float4 (&x)[4], float4 (&hi)[4], fl
         float d0 = x[i].x, d1 = x[i].y, d2 = x[i].z, d3 = x[i].w;
         add2(d0, d1, -hi[i].x, -hi[i].y);
         add2(d2, d3, -hi[i].z, -hi[i].w);
-        lo[i] = make_float4(tf32_rn(d0), tf32_rn(d1), tf32_rn(d2), tf32_rn(d3));
+        lo[i] = make_float4(d0, d1, d2, d3);
     }
 }
 
