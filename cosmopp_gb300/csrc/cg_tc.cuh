@@ -259,6 +259,16 @@ __device__ __forceinline__ void add2(float& r0, float& r1, float m0, float m1)
         : "f"(m0), "f"(m1));
 }
 
+// (d0, d1) = (a0 * b0 + d0, a1 * b1 + d1) as one packed two-lane FP32 FMA (each lane rounded once,
+// like fmaf)
+__device__ __forceinline__ void fma2(float& d0, float& d1, float a0, float a1, float b0, float b1)
+{
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "mov.b64 rd, {%0, %1};\n\tfma.rn.f32x2 rd, ra, rb, rd;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "+f"(d0), "+f"(d1)
+        : "f"(a0), "f"(a1), "f"(b0), "f"(b1));
+}
+
 // the TF32 part the tensor core keeps (top 19 bits) and the FP32 remainder
 __device__ __forceinline__ float tf32_hi(float x) { return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u); }
 // x rounded to the nearest TF32 value (ties away from zero); the tensor core then reads it exactly

@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(256) contract_fwd(int B, int lp, const float* 
 #pragma unroll
                 for (int a = 0; a < 8; ++a)
 #pragma unroll
-                    for (int q = 0; q < 8; ++q) acc[a][q] = fmaf(u[a], w[q], acc[a][q]);
+                    for (int q = 0; q < 8; q += 2) tc::fma2(acc[a][q], acc[a][q + 1], u[a], u[a], w[q], w[q + 1]);
             }
         }
         __syncthreads();  // buffer i & 1 is read: refill it with block i + 2

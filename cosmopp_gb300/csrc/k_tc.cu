@@ -214,16 +214,19 @@ __device__ __forceinline__ void ld_c1(const float* t, int rr, int kc, int h, flo
 // rounding of hi, so the truncation is as often up as down, and the error (below 2^-21 of x) is of
 // the size of the a_lo * b_lo term the 3xTF32 split drops anyway.  (Truncating hi instead would make
 // lo always of x's sign and bias sums of squares.)
+__device__ __forceinline__ void split1(const float4& x, float4& hi, float4& lo)
+{
+    hi = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
+    float d0 = x.x, d1 = x.y, d2 = x.z, d3 = x.w;
+    add2(d0, d1, -hi.x, -hi.y);
+    add2(d2, d3, -hi.z, -hi.w);
+    lo = make_float4(d0, d1, d2, d3);
+}
+
 __device__ __forceinline__ void split4(const float4 (&x)[4], float4 (&hi)[4], float4 (&lo)[4])
 {
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        hi[i] = make_float4(tf32_rn(x[i].x), tf32_rn(x[i].y), tf32_rn(x[i].z), tf32_rn(x[i].w));
-        float d0 = x[i].x, d1 = x[i].y, d2 = x[i].z, d3 = x[i].w;
-        add2(d0, d1, -hi[i].x, -hi[i].y);
-        add2(d2, d3, -hi[i].z, -hi[i].w);
-        lo[i] = make_float4(d0, d1, d2, d3);
-    }
+    for (int i = 0; i < 4; ++i) split1(x[i], hi[i], lo[i]);
 }
 
 // B operand of one chunk from two stacked SC tiles (rows 0-63: top, 64-127: bot; nullptr = zero)
@@ -890,7 +893,7 @@ __device__ void factor_block128(float* s, float* inv, float* tmp, int* bad)
 // overlaps the off-diagonal blocks.  Off-diagonal blocks: S_IJ = A_IJ - sum_{k < 2 J2} L_I,k L_J,k^T
 // into the L storage (C1); for J2 > 0 the CTAs after the first B are persistent and take them from
 // the work queue, batch element by batch element (the blocks of one element share its L_J panel
-// in L2); for J2 = 0 (no K loop, S = A) one CTA each.
+// in L2); for J2 = 0 (no K loop, S = A) they copy the blocks, grid-stride, without tensor memory.
 // Diagonal block: S_JJ factorised, L_JJ into the L storage, its inverse into Linv and, transposed,
 // into the M storage, its diagonal into diag.
 __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, const float* __restrict__ A,
@@ -938,15 +941,17 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
         tc_end(tm);
         return;
     }
-    int I2, b;
-    if ((int)blockIdx.x < B) {
-        I2 = J2;
-        b = blockIdx.x;
-    } else {
-        const int k = blockIdx.x - B;
-        b = k / noff;
-        I2 = J2 + 1 + k % noff;
+    if ((int)blockIdx.x >= B) {
+        // J2 = 0: no K loop, S = A; the CTAs after the first B stride over the off-diagonal blocks
+        for (int k = blockIdx.x - B; k < noff * B; k += gridDim.x - B) {
+#pragma unroll
+            for (int j = 0; j < 64; ++j) R[j] = 0.f;
+            if (prod) store_s((size_t)(k / noff) * ntile, J2 + 1 + k % noff);
+        }
+        return;
     }
+    // a diagonal block
+    const int I2 = J2, b = blockIdx.x;
     const float* Ab = A + (size_t)b * ntile * TILE_ELEMS;
     float* Lb = Ls + (size_t)b * ntile * SC_TILE;
     float* Lcb = Lc + (size_t)b * ntile * C1_TILE;
@@ -961,11 +966,6 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
                    c % 2, dst, bar);
     };
     tc_kloop<A_SMEM_C1>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
-    if (I2 > J2) {
-        if (prod) store_s((size_t)b * ntile, I2);
-        tc_end(tm);
-        return;
-    }
     // diagonal block: S = A_JJ - P into shared memory (column-major, ld 129), lower part
     float* s = reinterpret_cast<float*>(smem_raw);
     float* inv = s + 128 * 129;
@@ -1168,16 +1168,18 @@ __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restri
 // Tr(V dA/dC_l).  One GEMM per tile and 128 batch elements: M = 128 (b), N = lp (l), K = the tile's
 // 4096 entries in 32-wide chunks, 3xTF32.  The operand rows (128 rows of V, lp of Ubar) are 16 KB
 // apart or more, so they are fetched in groups of G chunks: each warp copies (cp.async) G x 128
-// contiguous bytes of a row at a time into a group buffer, one buffer ahead (fetching 128 bytes of
-// every row per chunk left HBM at a third of its bandwidth).  The producers then store their
+// contiguous bytes of a row at a time into one of NB group buffers, NB - 1 groups ahead (fetching
+// 128 bytes of every row per chunk left HBM at a third of its bandwidth, and one group of 512-byte
+// runs in flight at about 40%).  The producers then store their
 // pieces split: V (A, weighted) into tensor memory, Ubar (B) into a shared-memory stage (K-major
-// canonical, lp rows), so the FP32 table needs no split copy.  One thread issues the MMAs; every
-// chunk's accumulator is folded into round-to-nearest registers (the tensor core's FP32
-// accumulation drifts one way).  RC >= lp / 2: the accumulator columns a producer drains.
+// canonical, lp rows), so the FP32 table needs no split copy.  One thread issues the MMAs; each
+// chunk pair's accumulator is folded into round-to-nearest registers (the tensor core's FP32
+// accumulation drifts one way).  The weight 2 of the off-diagonal tiles is applied to the sums
+// at the end.  RC >= lp / 2: the accumulator columns a producer drains.
 // grid (tiles, ceil(B / 128)).
 constexpr int ADJ_NTH = NPROD + 32;
 
-template <int RC, int G>
+template <int RC, int G, int NB>
 __global__ void __launch_bounds__(ADJ_NTH, 1) contract_adj_tc(int B, int lp, const float* __restrict__ U,
                                                               const float* __restrict__ V, size_t strideA,
                                                               float* __restrict__ part, int* __restrict__ err)
@@ -1185,7 +1187,7 @@ __global__ void __launch_bounds__(ADJ_NTH, 1) contract_adj_tc(int B, int lp, con
     constexpr int NBP = (8 * RC + NPROD - 1) / NPROD;  // B pieces (8 K values) per producer and chunk
     constexpr int P = 8 * G;                            // 16-byte pieces of a row in a group
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    __shared__ uint64_t mma_bar[2], acc_free[2], ab_full[NAST];
+    __shared__ uint64_t mma_bar[NAST], acc_free[2], ab_full[NAST];
     __shared__ uint32_t tbase;
     const int t = blockIdx.x, b0 = blockIdx.y * 128;
     int I, J;
@@ -1193,11 +1195,11 @@ __global__ void __launch_bounds__(ADJ_NTH, 1) contract_adj_tc(int B, int lp, con
     const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     if (warp == 0) tmem_alloc(&tbase, TMEM_COLS);
     if (threadIdx.x == 0) {
-        for (int i = 0; i < 2; ++i) {
+        for (int i = 0; i < 2; ++i) mbar_init(&acc_free[i], NPROD / 32);
+        for (int i = 0; i < NAST; ++i) {
             mbar_init(&mma_bar[i], 1);
-            mbar_init(&acc_free[i], NPROD / 32);
+            mbar_init(&ab_full[i], NPROD / 32);
         }
-        for (int i = 0; i < NAST; ++i) mbar_init(&ab_full[i], NPROD / 32);
         fence_mbar_init();
     }
     fence_before();
@@ -1217,12 +1219,12 @@ __global__ void __launch_bounds__(ADJ_NTH, 1) contract_adj_tc(int B, int lp, con
         float R[RC];
 #pragma unroll
         for (int j = 0; j < RC; ++j) R[j] = 0.f;
-        // two group buffers after the B stages: 128 V rows then lp Ubar rows of P pieces, piece j of
+        // NB group buffers after the B stages: 128 V rows then lp Ubar rows of P pieces, piece j of
         // row q at physical piece j ^ (q % P), so that the producers' reads (one row per lane) and
         // the warps' copies (one row per warp) both spread over the banks
         const uint32_t gbuf = (uint32_t)(128 + lp) * P * 16;
         auto gpiece = [&](int k, int q, int j) {
-            return (uint32_t)(NAST * stb + (k & 1) * gbuf + (q * P + (j ^ (q % P))) * 16);
+            return (uint32_t)(NAST * stb + (k % NB) * gbuf + (q * P + (j ^ (q % P))) * 16);
         };
         // group k (chunks G k .. G k + G - 1): consecutive threads copy consecutive pieces of a row
         auto fetch = [&](int k) {
@@ -1243,30 +1245,31 @@ __global__ void __launch_bounds__(ADJ_NTH, 1) contract_adj_tc(int B, int lp, con
             return *reinterpret_cast<const float4*>(smem_raw + gpiece(k, q, j));
         };
         // chunk c into stage c % NAST: weighted, split V into tensor memory, split Ubar into shared
-        // memory.  At the first chunk of a group, the group's copies are waited for and published to
-        // all producers (named barrier), which also frees the other buffer for the next group.
+        // memory.  At the first chunk of group k, its copies are waited for (the NB - 2 later groups
+        // may still be in flight) and published to all producers (named barrier), which also frees
+        // group k - 1's buffer for group k + NB - 1.
         auto put = [&](int c) {
             const int st = c % NAST, k = c / G, cl = c % G;
             if (cl == 0) {
-                cp_async_wait<0>();
+                cp_async_wait<NB - 2>();
                 asm volatile("bar.sync 1, %0;" ::"n"(NPROD) : "memory");
-                fetch(k + 1);
+                fetch(k + NB - 1);
             }
-            float4 qh[4], ql[4];
+            float4 x[4], qh[4], ql[4];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const float4 v = rd(k, r, 8 * cl + 4 * h + i);
-                float x[4] = {v.x, v.y, v.z, v.w};
+            for (int i = 0; i < 4; ++i) x[i] = rd(k, r, 8 * cl + 4 * h + i);
+            if (I == J) {  // diagonal tile: weight 2 below the diagonal, 1 on it, 0 above (1/2 of that here)
 #pragma unroll
-                for (int kk = 0; kk < 4; ++kk) {
-                    const int e = KC * c + 16 * h + 4 * i + kk, rr = e % TS, cc = e / TS;
-                    const float w = (I != J || rr > cc) ? 2.f : (rr == cc ? 1.f : 0.f);
-                    x[kk] *= w;
+                for (int i = 0; i < 4; ++i) {
+                    float* xi = reinterpret_cast<float*>(&x[i]);
+#pragma unroll
+                    for (int kk = 0; kk < 4; ++kk) {
+                        const int e = KC * c + 16 * h + 4 * i + kk, rr = e % TS, cc = e / TS;
+                        xi[kk] *= (rr > cc) ? 1.f : (rr == cc ? 0.5f : 0.f);
+                    }
                 }
-                qh[i] = make_float4(tf32_rn(x[0]), tf32_rn(x[1]), tf32_rn(x[2]), tf32_rn(x[3]));
-                ql[i] = make_float4(tf32_rn(x[0] - qh[i].x), tf32_rn(x[1] - qh[i].y), tf32_rn(x[2] - qh[i].z),
-                                    tf32_rn(x[3] - qh[i].w));
             }
+            split4(x, qh, ql);
             tmem_st16(tm + lane_base() + col_a_hi(st) + 16 * h, qh);
             tmem_st16(tm + lane_base() + col_a_lo(st) + 16 * h, ql);
             unsigned char* stage = smem_raw + st * stb;
@@ -1277,10 +1280,8 @@ __global__ void __launch_bounds__(ADJ_NTH, 1) contract_adj_tc(int B, int lp, con
                     const int l = i / 4, k0 = 8 * (i % 4);
 #pragma unroll
                     for (int q = 0; q < 2; ++q) {
-                        const float4 x = rd(k, 128 + l, 8 * cl + k0 / 4 + q);
-                        const float4 hi = make_float4(tf32_rn(x.x), tf32_rn(x.y), tf32_rn(x.z), tf32_rn(x.w));
-                        const float4 lo = make_float4(tf32_rn(x.x - hi.x), tf32_rn(x.y - hi.y), tf32_rn(x.z - hi.z),
-                                                      tf32_rn(x.w - hi.w));
+                        float4 hi, lo;
+                        split1(rd(k, 128 + l, 8 * cl + k0 / 4 + q), hi, lo);
                         const uint32_t off = (l / 8) * 1024 + ((k0 / 4) + q) * 128 + (l % 8) * 16;
                         *reinterpret_cast<float4*>(stage + off) = hi;
                         *reinterpret_cast<float4*>(stage + plane + off) = lo;
@@ -1295,30 +1296,34 @@ __global__ void __launch_bounds__(ADJ_NTH, 1) contract_adj_tc(int B, int lp, con
         };
         // chunk c's MMAs are done: fold its lp / 2 columns of this thread into R and release the
         // accumulator (the last chunks' waits ignore the abort flag: no MMA may outlive tensor memory)
+        // chunk c's MMAs are done (its stages are free); at the end of a chunk pair, fold the pair's
+        // lp / 2 columns of this thread into R and release the accumulator (the last chunks' waits
+        // ignore the abort flag: no MMA may outlive tensor memory)
         auto retire = [&](int c, bool last) {
             if (!last) {
-                wait(&mma_bar[c & 1], (c >> 1) & 1);
-            } else if (!mbar_wait(&mma_bar[c & 1], (c >> 1) & 1, kMaxIter)) {
+                wait(&mma_bar[c % NAST], (c / NAST) & 1);
+            } else if (!mbar_wait(&mma_bar[c % NAST], (c / NAST) & 1, kMaxIter)) {
                 ok = false;
                 atomicExch(err, 1);
             }
+            if (!(c & 1)) return;
             fence_after();
 #pragma unroll
             for (int j = 0; j < (RC + 7) / 8; ++j) {
                 if (8 * j < lp / 2) {
                     float m[8];
-                    tmem_ld8w(tm + lane_base() + col_main(c & 1) + h * (lp / 2) + 8 * j, m);
+                    tmem_ld8w(tm + lane_base() + col_main((c >> 1) & 1) + h * (lp / 2) + 8 * j, m);
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) R[8 * j + i] += m[i];
+                    for (int i = 0; i < 8; i += 2) add2(R[8 * j + i], R[8 * j + i + 1], m[i], m[i + 1]);
                 }
             }
             fence_before();
             __syncwarp();
-            if (lane == 0) mbar_arrive(&acc_free[c & 1]);
+            if (lane == 0) mbar_arrive(&acc_free[(c >> 1) & 1]);
         };
-        // groups are fetched one ahead of the stores, the stores run two chunks ahead of the MMAs:
+        // groups are fetched NB - 1 ahead of the stores, the stores run two chunks ahead of the MMAs:
         // step c retires chunk c - 2 and stores chunk c + 2 into its stage
-        fetch(0);
+        for (int k = 0; k < NB - 1; ++k) fetch(k);
         put(0);
         put(1);
         for (int c = 0; c < NCH; ++c) {
@@ -1332,26 +1337,26 @@ __global__ void __launch_bounds__(ADJ_NTH, 1) contract_adj_tc(int B, int lp, con
             float* dst = part + ((size_t)t * B + b) * lp + h * (lp / 2);
 #pragma unroll
             for (int j = 0; j < RC; ++j)
-                if (j < lp / 2) dst[j] = R[j];
+                if (j < lp / 2) dst[j] = 2.f * R[j];
         }
     } else if (lane == 0) {
         // MMA issue: chunk c's 12 MMAs (M128 N lp K8) once its operands and its accumulator are ready
         const uint32_t idesc = idesc_tf32(128, lp);
         for (int c = 0; c < NCH; ++c) {
-            const int st = c % NAST;
+            const int st = c % NAST, pr = c >> 1;
             wait(&ab_full[st], (c / NAST) & 1);
-            if (c >= 2) wait(&acc_free[c & 1], ((c - 2) >> 1) & 1);
+            if ((c & 1) == 0 && pr >= 2) wait(&acc_free[pr & 1], ((pr - 2) >> 1) & 1);
             fence_after();
             const uint32_t bh = sb + st * stb, bl = bh + plane;
-            const uint32_t ah = tm + col_a_hi(st), al = tm + col_a_lo(st), d = tm + col_main(c & 1);
+            const uint32_t ah = tm + col_a_hi(st), al = tm + col_a_lo(st), d = tm + col_main(pr & 1);
 #pragma unroll
             for (int kk = 0; kk < KC / 8; ++kk) {
                 const uint32_t off = kk * 2 * LBO;
-                mma_tf32_ta(d, al + 8 * kk, smem_desc(bh + off, LBO, SBO), idesc, kk ? 1u : 0u);
+                mma_tf32_ta(d, al + 8 * kk, smem_desc(bh + off, LBO, SBO), idesc, ((c & 1) || kk) ? 1u : 0u);
                 mma_tf32_ta(d, ah + 8 * kk, smem_desc(bh + off, LBO, SBO), idesc, 1u);
                 mma_tf32_ta(d, ah + 8 * kk, smem_desc(bl + off, LBO, SBO), idesc, 1u);
             }
-            mma_commit(&mma_bar[c & 1]);
+            mma_commit(&mma_bar[st]);
         }
     }
     __syncwarp();
@@ -1404,7 +1409,8 @@ int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, flo
     for (int J2 = 0; J2 < nt2; ++J2) {
         // diagonal CTAs, then one CTA per off-diagonal block (J2 = 0) or persistent CTAs
         const int noff = (nt2 - J2 - 1) * B;
-        const int grid = B + (J2 == 0 ? noff : (noff < ctx->sm_count ? noff : ctx->sm_count));
+        const int cap = (J2 == 0 ? 4 : 1) * ctx->sm_count;
+        const int grid = B + (noff < cap ? noff : cap);
         chol_tc_update<<<grid, NTH, tc_smem(), s>>>(J2, nt, B, A, Ls, Lc, Linv, Ms, Mc, diag, status,
                                                     d_err + 1 + nt2 + J2, d_err);
         count_launch(ctx);
@@ -1449,15 +1455,16 @@ int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, const float* Mc,
 
 bool adjoint_tc_ok(int lp) { return lp % 16 == 0 && lp >= 16 && lp <= 96; }
 
-// G chunks per fetch group: two group buffers and the B stages within 224 KB
-template <int RC, int G>
+// G chunks per fetch group, NB group buffers: buffers and B stages within 224 KB
+template <int RC, int G, int NB>
 static int launch_adj_tc(cg_ctx* ctx, dim3 grid, int B, int lp, const float* U, const float* V, size_t strideA,
                          float* part, int* d_err, cudaStream_t s)
 {
-    static_assert(NAST * 2 * 2 * RC * KC * 4 + 2 * (128 + 2 * RC) * G * 128 <= 224 * 1024, "shared memory");
-    const int smem = NAST * 2 * lp * KC * 4 + 2 * (128 + lp) * G * 128;
-    CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_adj_tc<RC, G>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-    contract_adj_tc<RC, G><<<grid, ADJ_NTH, smem, s>>>(B, lp, U, V, strideA, part, d_err);
+    static_assert(NB >= 2 && NAST * 2 * 2 * RC * KC * 4 + NB * (128 + 2 * RC) * G * 128 <= 224 * 1024, "shared memory");
+    const int smem = NAST * 2 * lp * KC * 4 + NB * (128 + lp) * G * 128;
+    CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_adj_tc<RC, G, NB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          smem));
+    contract_adj_tc<RC, G, NB><<<grid, ADJ_NTH, smem, s>>>(B, lp, U, V, strideA, part, d_err);
     return CG_OK;
 }
 
@@ -1466,9 +1473,9 @@ int adjoint_contract_tc(cg_ctx* ctx, int B, int nt, int lp, const float* U, cons
 {
     if (!adjoint_tc_ok(lp)) { ctx->err = "tensor-core adjoint contraction needs lp % 16 == 0, lp <= 96"; return CG_ERR_BAD_ARG; }
     const dim3 grid(ntiles_lower(nt), (B + 127) / 128);
-    int rc = (lp <= 48)   ? launch_adj_tc<24, 4>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)
-             : (lp <= 64) ? launch_adj_tc<32, 2>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)
-                          : launch_adj_tc<48, 2>(ctx, grid, B, lp, U, V, strideA, part, d_err, s);
+    int rc = (lp <= 48)   ? launch_adj_tc<24, 2, 4>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)
+             : (lp <= 64) ? launch_adj_tc<32, 2, 3>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)
+                          : launch_adj_tc<48, 2, 2>(ctx, grid, B, lp, U, V, strideA, part, d_err, s);
     if (rc) return rc;
     count_launch(ctx);
     CG_CUDA_TRY(ctx, cudaGetLastError());
