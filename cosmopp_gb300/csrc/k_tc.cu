@@ -309,6 +309,12 @@ __device__ __forceinline__ void st_c1_row(float* tile, int rr, const float (&v)[
 //   A_SMEM_PRE (at most NSTA chunks) the producers wrote the FP32 chunks into the ring stages
 //             themselves before the loop (fa unused).
 enum { A_REG_SC = 0, A_REG_C1 = 1, A_SMEM_C1 = 2, A_SMEM_PRE = 3 };
+// How the B operand reaches its shared-memory stage:
+//   B_COPY    fb(c, dst, bar) issues bulk copies of the split chunk into the stage;
+//   B_FROM_A  (A_SMEM_C1 only, fb unused) B is the same matrix as A (a diagonal block's L_J L_J^T):
+//             the producers write the A chunk they split into the B stage too, so the rows are read
+//             from memory once, in FP32, instead of twice.
+enum { B_COPY = 0, B_FROM_A = 1 };
 
 // ---- pieces shared by the single-item K loop and the item stream -----------------------------
 
@@ -316,7 +322,7 @@ constexpr uint32_t kMaxIter = 1u << 22;  // try_wait attempts before a wait give
 
 // chunk g's A (row r, K half h: from qx, or for A_SMEM_C1 from the shared-memory ring) into
 // tensor-memory stage g % NAST, then one arrival per warp on the stage's a_full barrier
-template <int AMODE, int NX, class W>
+template <int AMODE, int BMODE = B_COPY, int NX, class W>
 __device__ __forceinline__ void put_a(int g, float4 (&qx)[NX], W& wait, const float* sa_f, TcCtl& ctl, uint32_t tm)
 {
     const int r = threadIdx.x % 128, h = threadIdx.x / 128, lane = threadIdx.x % 32, st = g % NAST;
@@ -344,6 +350,17 @@ __device__ __forceinline__ void put_a(int g, float4 (&qx)[NX], W& wait, const fl
     }
     tmem_st16(tm + lane_base() + col_a_hi(st) + 16 * h, qh);
     tmem_st16(tm + lane_base() + col_a_lo(st) + 16 * h, ql);
+    if constexpr (BMODE == B_FROM_A) {
+        // the same piece into B stage g % NSTB (free: the caller retired chunk g - 4), hi and lo planes
+        float* stage = const_cast<float*>(sa_f) - (NSTB * STB_BYTES) / 4 + (g % NSTB) * (STB_BYTES / 4) +
+                       (r >> 3) * 256 + (r & 7) * 4 + 4 * h * 32;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            *reinterpret_cast<float4*>(stage + i * 32) = qh[i];
+            *reinterpret_cast<float4*>(stage + STB_BYTES / 8 + i * 32) = ql[i];
+        }
+        fence_proxy_async();  // the MMA reads the stage through the async proxy
+    }
     tmem_wait_st();
     fence_before();
     __syncwarp();
@@ -374,12 +391,12 @@ __device__ __forceinline__ void retire_acc(int g, bool last, bool fold, W& wait,
 // one issuer thread: chunk g's 12 MMAs (M128 N128 K8, A from tensor-memory stage g % NAST, B from
 // shared-memory stage g % NSTB) into the accumulator of its pair's parity (fresh at the pair's first
 // chunk), once its A, its B and its accumulator are ready, committed to the stage's mbarriers
-template <class W>
+template <int BMODE = B_COPY, class W>
 __device__ __forceinline__ void issue_chunk(int g, W& wait, TcCtl& ctl, uint32_t tm, uint32_t sb)
 {
     const int st = g % NAST, sbi = g % NSTB, pr = g >> 1;
     wait(&ctl.a_full[st], (g / NAST) & 1);
-    wait(&ctl.b_full[sbi], (g / NSTB) & 1);
+    if constexpr (BMODE == B_COPY) wait(&ctl.b_full[sbi], (g / NSTB) & 1);
     if ((g & 1) == 0 && pr >= 2) wait(&ctl.acc_free[pr & 1], ((pr - 2) >> 1) & 1);
     fence_after();
     const uint32_t bh = sb + sbi * STB_BYTES, bl = bh + STB_BYTES / 2;
@@ -392,12 +409,12 @@ __device__ __forceinline__ void issue_chunk(int g, W& wait, TcCtl& ctl, uint32_t
         mma_tf32_ta(d, ah + 8 * kk, smem_desc(bl + off, LBO, SBO), IDESC, 1u);
     }
     mma_commit(&ctl.mma_bar[st]);
-    mma_commit(&ctl.b_empty[sbi]);
+    if constexpr (BMODE == B_COPY) mma_commit(&ctl.b_empty[sbi]);
 }
 
 // the copy thread's share of chunk g: its A (A_SMEM_C1: fa(..., top, bot, kc) names the tiles) into
 // the A ring and its B (fb(..., dst, bar)) into the B ring, once their stages are free
-template <int AMODE, class W, class FA, class FB>
+template <int AMODE, int BMODE = B_COPY, class W, class FA, class FB>
 __device__ __forceinline__ void copy_chunk(int g, W& wait, TcCtl& ctl, uint32_t sb, FA&& fa, FB&& fb)
 {
     if constexpr (AMODE == A_SMEM_C1) {
@@ -408,9 +425,11 @@ __device__ __forceinline__ void copy_chunk(int g, W& wait, TcCtl& ctl, uint32_t 
         fa(top, bot, kc);
         bulk_a_c1(top, bot, kc, sb + NSTB * STB_BYTES + si * STA_BYTES, &ctl.as_full[si]);
     }
-    const int sbi = g % NSTB;
-    if (g >= NSTB) wait(&ctl.b_empty[sbi], ((g / NSTB) - 1) & 1);
-    fb(sb + sbi * STB_BYTES, &ctl.b_full[sbi]);
+    if constexpr (BMODE == B_COPY) {
+        const int sbi = g % NSTB;
+        if (g >= NSTB) wait(&ctl.b_empty[sbi], ((g / NSTB) - 1) & 1);
+        fb(sb + sbi * STB_BYTES, &ctl.b_full[sbi]);
+    }
 }
 
 // ---- the K loop of one item ------------------------------------------------------------------
@@ -420,10 +439,11 @@ __device__ __forceinline__ void copy_chunk(int g, W& wait, TcCtl& ctl, uint32_t 
 // product for row t % 128, column 64 (t / 128) + j (0 if nchunks == 0).  Returns false if an
 // mbarrier wait gave up; waits give up early once *err is set (by this or any other CTA), and a
 // thread whose wait gave up skips its later waits, so a failure ends the launch quickly.
-template <int AMODE, class FA, class FB>
+template <int AMODE, int BMODE = B_COPY, class FA, class FB>
 __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& ctl, uint32_t tm, float (&R)[64],
                          int* err)
 {
+    static_assert(BMODE == B_COPY || AMODE == A_SMEM_C1, "B_FROM_A needs the A chunk staged in shared memory");
     bool ok = true;
     auto wait = [&](uint64_t* bar, uint32_t parity) {
         if (!ok) return;
@@ -447,18 +467,18 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
             if (nchunks > 1) fa(1, r, h, a1);
         }
         if (nchunks > 0) {
-            put_a<AMODE>(0, a0, wait, sa_f, ctl, tm);
+            put_a<AMODE, BMODE>(0, a0, wait, sa_f, ctl, tm);
             if constexpr (REG) { if (nchunks > 2) fa(2, r, h, a0); }
         }
         if (nchunks > 1) {
-            put_a<AMODE>(1, a1, wait, sa_f, ctl, tm);
+            put_a<AMODE, BMODE>(1, a1, wait, sa_f, ctl, tm);
             if constexpr (REG) { if (nchunks > 3) fa(3, r, h, a1); }
         }
         // step c: chunk c - 2 is retired and its A stage takes chunk c + 2 (held in slot qx = c & 1)
         auto step = [&](int c, float4 (&qx)[NX]) {
             if (c >= 2) retire_acc(c - 2, false, (c & 1) != 0, wait, ok, err, ctl, tm, R);
             if (c + 2 < nchunks) {
-                put_a<AMODE>(c + 2, qx, wait, sa_f, ctl, tm);
+                put_a<AMODE, BMODE>(c + 2, qx, wait, sa_f, ctl, tm);
                 if constexpr (REG) { if (c + 4 < nchunks) fa(c + 4, r, h, qx); }
             }
         };
@@ -472,15 +492,15 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
         // ---- MMA issue: chunk pairs 0, 2, 4, ... from warp 8, pairs 1, 3, 5, ... from warp 10
         if (lane == 0)
             for (int c = (warp == NPROD / 32) ? 0 : 2; c < nchunks; c += 4) {
-                issue_chunk(c, wait, ctl, tm, sb);
-                if (c + 1 < nchunks) issue_chunk(c + 1, wait, ctl, tm, sb);
+                issue_chunk<BMODE>(c, wait, ctl, tm, sb);
+                if (c + 1 < nchunks) issue_chunk<BMODE>(c + 1, wait, ctl, tm, sb);
             }
         __syncwarp();
     } else {
         // ---- copies: one thread keeps the B ring (and, for A_SMEM_C1, the A ring) full
         if (lane == 0)
             for (int c = 0; c < nchunks; ++c)
-                copy_chunk<AMODE>(
+                copy_chunk<AMODE, BMODE>(
                     c, wait, ctl, sb, [&](auto& top, auto& bot, auto& kc) { fa(c, top, bot, kc); },
                     [&](uint32_t dst, uint64_t* bar) { fb(c, dst, bar); });
         __syncwarp();
@@ -961,11 +981,9 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
         bot = Lcb + (size_t)tile_index(2 * I2 + 1, c / 2) * C1_TILE;
         kc = c % 2;
     };
-    auto fb = [&](int c, uint32_t dst, uint64_t* bar) {
-        bulk_tiles(Lb + (size_t)tile_index(2 * J2, c / 2) * SC_TILE, Lb + (size_t)tile_index(2 * J2 + 1, c / 2) * SC_TILE,
-                   c % 2, dst, bar);
-    };
-    tc_kloop<A_SMEM_C1>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
+    // B = A (S_JJ = A_JJ - L_J L_J^T): the producers copy the split A chunk into the B stage
+    auto fb = [](int, uint32_t, uint64_t*) {};
+    tc_kloop<A_SMEM_C1, B_FROM_A>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
     // diagonal block: S = A_JJ - P into shared memory (column-major, ld 129), lower part
     float* s = reinterpret_cast<float*>(smem_raw);
     float* inv = s + 128 * 129;
