@@ -34,9 +34,13 @@
 //              Issue blocks while the tensor pipe is busy, so with one issuer the pipe
 //              idled during every barrier wait; with two, one issuer waits while the
 //              other's MMAs run;
-//   warp 9     (copies): one thread keeps a ring of NSTB shared-memory B stages
-//              (and NSTA A stages, for A streamed through shared memory) filled
-//              with bulk copies, refilling a stage when its readers are done.
+//   warps 9,11 (copies): one thread each keeps a ring filled with bulk copies,
+//              refilling a stage when its readers are done: warp 9 the NSTB
+//              shared-memory B stages, warp 11 the NSTA A stages (for A streamed
+//              through shared memory).  With one thread for both, every A copy
+//              waited behind the previous chunk's B stage, which frees only when that
+//              stage's MMAs complete, so A ran only a chunk or two ahead of use, short
+//              of DRAM latency, and the producers waited for it (clock64 trace).
 //
 //   chol_tc_update: left-looking Cholesky, column block J: S_IJ = A_IJ - sum_{k<J} L_Ik L_Jk^T;
 //                   the diagonal CTA factors S_JJ = L_JJ L_JJ^T, inverts L_JJ in shared memory and
@@ -66,7 +70,7 @@ constexpr int KC = 32;                          // K columns per chunk
 constexpr uint32_t LBO = 128, SBO = KC / 4 * 128;
 constexpr uint32_t IDESC = idesc_tf32(128, 128);
 constexpr int NPROD = 256;                      // producers (warps 0-7)
-constexpr int NTH = NPROD + 96;                 // + the MMA issuers (warps 8, 10) and the copy warp (9)
+constexpr int NTH = NPROD + 128;                // + the MMA issuers (warps 8, 10) and the copy warps (9: B, 11: A)
 constexpr int NAST = 4;                         // A stages in tensor memory
 constexpr int NIQ = 8;                          // item ids in flight in a CTA's stream
 constexpr int NSTB = 4;                         // B stages in shared memory
@@ -122,7 +126,7 @@ struct TcCtl {
     uint64_t as_full[NSTA];   // A shared-memory stage landed
     uint64_t as_empty[NSTA];  // A shared-memory stage read by every producer warp
     uint64_t iq_full[NIQ];    // item slot written by the copy thread
-    uint64_t iq_empty[NIQ];   // item slot released by every producer warp and both issuers
+    uint64_t iq_empty[NIQ];   // item slot released by every producer warp, both issuers and the A copy thread
     int iq[NIQ];              // item ids of the stream, -1 = end
     uint32_t tbase;
     int bad;
@@ -143,7 +147,7 @@ __device__ __forceinline__ void init_bars(TcCtl& ctl)
     }
     for (int i = 0; i < NIQ; ++i) {
         mbar_init(&ctl.iq_full[i], 1);
-        mbar_init(&ctl.iq_empty[i], NPROD / 32 + 2);
+        mbar_init(&ctl.iq_empty[i], NPROD / 32 + 3);
         ctl.iq[i] = -1;
     }
     fence_mbar_init();
@@ -412,10 +416,10 @@ __device__ __forceinline__ void issue_chunk(int g, W& wait, TcCtl& ctl, uint32_t
     if constexpr (BMODE == B_COPY) mma_commit(&ctl.b_empty[sbi]);
 }
 
-// the copy thread's share of chunk g: its A (A_SMEM_C1: fa(..., top, bot, kc) names the tiles) into
-// the A ring and its B (fb(..., dst, bar)) into the B ring, once their stages are free
-template <int AMODE, int BMODE = B_COPY, class W, class FA, class FB>
-__device__ __forceinline__ void copy_chunk(int g, W& wait, TcCtl& ctl, uint32_t sb, FA&& fa, FB&& fb)
+// the A copy thread's share of chunk g (A_SMEM_C1: fa(..., top, bot, kc) names the tiles): into the A
+// ring once its stage is free
+template <int AMODE, class W, class FA>
+__device__ __forceinline__ void copy_a(int g, W& wait, TcCtl& ctl, uint32_t sb, FA&& fa)
 {
     if constexpr (AMODE == A_SMEM_C1) {
         const int si = g % NSTA;
@@ -425,6 +429,12 @@ __device__ __forceinline__ void copy_chunk(int g, W& wait, TcCtl& ctl, uint32_t 
         fa(top, bot, kc);
         bulk_a_c1(top, bot, kc, sb + NSTB * STB_BYTES + si * STA_BYTES, &ctl.as_full[si]);
     }
+}
+
+// the B copy thread's share of chunk g (fb(..., dst, bar)): into the B ring once its stage's MMAs are done
+template <int BMODE, class W, class FB>
+__device__ __forceinline__ void copy_b(int g, W& wait, TcCtl& ctl, uint32_t sb, FB&& fb)
+{
     if constexpr (BMODE == B_COPY) {
         const int sbi = g % NSTB;
         if (g >= NSTB) wait(&ctl.b_empty[sbi], ((g / NSTB) - 1) & 1);
@@ -496,13 +506,17 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
                 if (c + 1 < nchunks) issue_chunk<BMODE>(c + 1, wait, ctl, tm, sb);
             }
         __syncwarp();
-    } else {
-        // ---- copies: one thread keeps the B ring (and, for A_SMEM_C1, the A ring) full
+    } else if (warp == NPROD / 32 + 1) {
+        // ---- B copies
         if (lane == 0)
             for (int c = 0; c < nchunks; ++c)
-                copy_chunk<AMODE, BMODE>(
-                    c, wait, ctl, sb, [&](auto& top, auto& bot, auto& kc) { fa(c, top, bot, kc); },
-                    [&](uint32_t dst, uint64_t* bar) { fb(c, dst, bar); });
+                copy_b<BMODE>(c, wait, ctl, sb, [&](uint32_t dst, uint64_t* bar) { fb(c, dst, bar); });
+        __syncwarp();
+    } else {
+        // ---- A copies
+        if (lane == 0)
+            for (int c = 0; c < nchunks; ++c)
+                copy_a<AMODE>(c, wait, ctl, sb, [&](auto& top, auto& bot, auto& kc) { fa(c, top, bot, kc); });
         __syncwarp();
     }
     return ok;
@@ -511,7 +525,7 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
 // ---- the K loop over a stream of items -------------------------------------------------------
 
 // Items taken in order from a counter shared by the CTAs of a launch (zero before the launch): the
-// copy thread takes them and publishes the ids, in order, through a ring of NIQ shared-memory slots
+// B copy thread takes them and publishes the ids, in order, through a ring of NIQ shared-memory slots
 // (-1 = no more items); every role walks the same sequence of (item, chunk) pairs, and the chunks
 // of all the items pass through the stages as one sequence, so an item's copies and A stores start
 // while the previous item is still in the tensor pipe and a CTA pays its set-up and its first
@@ -637,8 +651,19 @@ __device__ bool tc_stream(int nitems, int* queue, GEO geo, FA fa, FB fb, FE epi,
             }
         }
         __syncwarp();
+    } else if (warp == NPROD / 32 + 3) {
+        // ---- A copies, following the published items
+        if (lane == 0) {
+            Cur q{};
+            enter(q);
+            for (int g = 0; q.gm.n; ++g) {
+                copy_a<AMODE>(g, wait, ctl, sb, [&](auto& top, auto& bot, auto& kc) { fa(q.gm, q.c, top, bot, kc); });
+                next(q, REL_ONE);
+            }
+        }
+        __syncwarp();
     } else {
-        // ---- copies: one thread takes the items, publishes them and keeps the rings full
+        // ---- B copies: this thread takes the items and publishes them
         if (lane == 0) {
             int g = 0;
             for (int k = 0;; ++k) {
@@ -651,9 +676,7 @@ __device__ bool tc_stream(int nitems, int* queue, GEO geo, FA fa, FB fb, FE epi,
                 if (it < 0) break;
                 const Geo gm = geo(it);
                 for (int c = 0; c < gm.n; ++c, ++g)
-                    copy_chunk<AMODE>(
-                        g, wait, ctl, sb, [&](auto& top, auto& bot, auto& kc) { fa(gm, c, top, bot, kc); },
-                        [&](uint32_t dst, uint64_t* bar) { fb(gm, c, dst, bar); });
+                    copy_b<B_COPY>(g, wait, ctl, sb, [&](uint32_t dst, uint64_t* bar) { fb(gm, c, dst, bar); });
             }
         }
         __syncwarp();
