@@ -310,7 +310,7 @@ def run_ours(args):
                 "peak_note": "measured bf16 sustained / 6 (TF32 = bf16 / 2, three MMAs per product)",
                 # ncu dram__bytes_read + dram__bytes_write of all 39 Cholesky launches of one batch-32
                 # step, x B / 32 (traffic grows with the batch): profiles/tc_kernels_nside16_b32.md
-                "traffic": 5.165e9 * B / 32.0 if args.workload == WORKLOAD else None,
+                "traffic": 4.891e9 * B / 32.0 if args.workload == WORKLOAD else None,
                 "traffic_unit": "bytes per step (whole Cholesky stage)"}
         roof["frac"] = roof["achieved"] / roof["peak"]
         # the forward contraction A_b = I + sum_l eps_bl Ubar_l: reads the FP32 table once
