@@ -22,7 +22,7 @@ import os
 import numpy as np
 
 __all__ = ["Context", "Likelihood", "LikelihoodWithDerivs", "CGError", "library", "DET_OFFSET",
-           "ring2nest", "nest2ring", "pix2vec", "beam"]
+           "ring2nest", "nest2ring", "pix2vec", "beam", "mh_sample"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libcosmopp_gb300.so")
@@ -57,6 +57,12 @@ class _Config(ctypes.Structure):
                 ("recenter_radius", ctypes.c_double)]
 
 
+# int (*)(void* user, int nchains, const double* x, double* m2lnl)
+_BATCH_LIKE = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                               ctypes.POINTER(ctypes.c_double))
+
+PRIOR = {"uniform": 0, "gauss": 1}
+
 _lib = None
 
 
@@ -87,6 +93,10 @@ def library():
     L.cg_reference_count.argtypes = [ctypes.c_void_p]
     L.cg_hmc_run.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, _dp, _dp, ctypes.c_int, ctypes.c_int,
                              ctypes.c_double, _dp, ctypes.c_int, ctypes.c_ulonglong, _dp, _dp]
+    _mh_tail = [_dp, _ip, _dp, _dp, ctypes.c_int, _ip, ctypes.c_int, ctypes.c_ulonglong, _dp, _dp, _dp]
+    L.cg_mh_sample.argtypes = [ctypes.c_int, ctypes.c_int, _BATCH_LIKE, ctypes.c_void_p, _dp, ctypes.c_int] + _mh_tail
+    L.cg_mh_run.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, _dp, _dp, ctypes.c_int] + _mh_tail
+    L.cg_noise_matrix_from_sims.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
     L.cg_selftest_wait_timeout.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
     L.cg_launch_count.restype = ctypes.c_longlong
     L.cg_launch_count.argtypes = [ctypes.c_void_p]
@@ -312,6 +322,29 @@ class Context:
                                        _p(acc)))
         return chain, acc
 
+    def noise_matrix_from_sims(self, sims):
+        """Averaging step of CMatrixGenerator::calculateNoiseMatrix
+        (source/c_matrix_generator.cpp:887-910) on the device: sims [nsims, n] simulated
+        noise maps at the kept pixels -> (packed noise matrix, max |per-pixel mean|)."""
+        sims = _f64(sims)
+        ns, n = sims.shape
+        out = np.zeros(n * (n + 1) // 2)
+        mx = ctypes.c_double(0)
+        self._check(self._L.cg_noise_matrix_from_sims(self._h, ns, n, _p(sims), _p(out), ctypes.byref(mx)))
+        return out, mx.value
+
+    def mh(self, d, x0, cl_template, niter, sampling_width, priors=None, blocks=None, adapt=True, seed=0):
+        """Batched Metropolis-Hastings over ln C_l (l = 2..lmax), one chain per row of x0
+        (cg_mh_run).  Returns (chain [niter+1, nchains, lmax]: -2lnL then x,
+        accept_rate [nchains, nblocks], final adaptive proposal covariance [lmax-1, lmax-1])."""
+        x0 = _f64(x0)
+        nchains, npar = x0.shape
+        out = _mh_buffers(niter, nchains, npar, blocks)
+        _keep, args = _mh_args(npar, sampling_width, priors, blocks, adapt, seed, out)
+        self._check(self._L.cg_mh_run(self._h, _p(_f64(d)), nchains, _p(x0), _p(_f64(cl_template)), int(niter),
+                                      *args))
+        return out[0], out[1], out[2]
+
     def selftest_wait_timeout(self):
         """Status a bounded device wait reports when it gives up (CG_ERR_TIMEOUT expected)."""
         st = ctypes.c_int(-1)
@@ -332,6 +365,60 @@ class Context:
         ms = np.zeros(7)
         self._check(self._L.cg_stage_times(self._h, _p(ms)))
         return dict(zip(self.STAGES, ms))
+
+
+def _mh_buffers(niter, nchains, npar, blocks):
+    nb = npar if blocks is None else len(blocks)
+    return (np.zeros((niter + 1, nchains, npar + 1)), np.zeros((nchains, nb)), np.zeros((npar, npar)))
+
+
+def _mh_args(npar, sampling_width, priors, blocks, adapt, seed, out):
+    """priors: None (flat) or a list of (kind, p1, p2) per parameter, kind "uniform"
+    (p1 = min, p2 = max) or "gauss" (p1 = mean, p2 = sigma)."""
+    w = _f64(np.broadcast_to(np.asarray(sampling_width, dtype=np.float64), (npar,)))
+    mode = p1 = p2 = None
+    if priors is not None:
+        if len(priors) != npar:
+            raise ValueError("one prior per parameter")
+        mode = np.array([PRIOR[k] for k, _, _ in priors], dtype=np.int32)
+        p1 = _f64([a for _, a, _ in priors])
+        p2 = _f64([b for _, _, b in priors])
+    blk = None if blocks is None else np.ascontiguousarray(blocks, dtype=np.int32)
+    keep = (w, mode, p1, p2, blk)  # the caller holds these while the call runs
+    return keep, [_p(w), None if mode is None else mode.ctypes.data_as(_ip), _p(p1), _p(p2),
+            0 if blk is None else len(blk), None if blk is None else blk.ctypes.data_as(_ip), int(bool(adapt)),
+            int(seed), _p(out[0]), _p(out[1]), _p(out[2])]
+
+
+def mh_sample(like, x0, niter, sampling_width, priors=None, blocks=None, adapt=True, seed=0):
+    """Batched Metropolis-Hastings (cg_mh_sample) over a host likelihood:
+    ``like(x [nchains, npar]) -> -2lnL [nchains]``, called once per block move for all
+    chains.  The rules are MetropolisHastings::run's (source/mcmc.cpp:455-700); no device
+    is used.  Returns (chain [niter+1, nchains, npar+1], accept_rate [nchains, nblocks],
+    final adaptive proposal covariance [npar, npar])."""
+    L = library()
+    x0 = _f64(x0)
+    nchains, npar = x0.shape
+    failure = []
+
+    def _cb(_user, nc, xp, outp):
+        try:
+            x = np.ctypeslib.as_array(xp, shape=(nc, npar))
+            np.ctypeslib.as_array(outp, shape=(nc,))[:] = like(x.copy())
+            return 0
+        except Exception as e:  # surfaced after the call returns
+            failure.append(e)
+            return CG_ERR_BAD_ARG
+
+    cb = _BATCH_LIKE(_cb)
+    out = _mh_buffers(niter, nchains, npar, blocks)
+    _keep, args = _mh_args(npar, sampling_width, priors, blocks, adapt, seed, out)
+    rc = L.cg_mh_sample(nchains, npar, cb, None, _p(x0), int(niter), *args)
+    if failure:
+        raise failure[0]
+    if rc:
+        raise CGError(rc, "cg_mh_sample")
+    return out
 
 
 class Likelihood:

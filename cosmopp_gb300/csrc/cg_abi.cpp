@@ -3,6 +3,7 @@
 //
 // Entry points and the reference interfaces they replace are declared in
 // include/cosmopp_gb300.h.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -279,6 +280,45 @@ extern "C" int cg_fiducial_matrix(cg_ctx* ctx, const double* cl, int lmax, int l
     }
     cudaFree(d_tab);
     cudaFree(d_out);
+    return rc;
+}
+
+extern "C" int cg_noise_matrix_from_sims(cg_ctx* ctx, int nsims, int n, const double* sims, double* out_packed,
+                                         double* max_abs_mean)
+{
+    if (!ctx || nsims < 1 || n < 1 || !sims || !out_packed) {
+        if (ctx) ctx->err = "bad arguments to cg_noise_matrix_from_sims";
+        return CG_ERR_BAD_ARG;
+    }
+    CG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const size_t ns = (size_t)nsims * n, np = (size_t)n * (n + 1) / 2;
+    double *d_sims = nullptr, *d_out = nullptr, *d_mean = nullptr;
+    if (cudaMalloc((void**)&d_sims, sizeof(double) * ns) != cudaSuccess ||
+        cudaMalloc((void**)&d_out, sizeof(double) * np) != cudaSuccess ||
+        cudaMalloc((void**)&d_mean, sizeof(double) * n) != cudaSuccess) {
+        cudaFree(d_sims);
+        cudaFree(d_out);
+        cudaFree(d_mean);
+        ctx->err = "cg_noise_matrix_from_sims: out of device memory";
+        return CG_ERR_ALLOC;
+    }
+    std::vector<double> mean(n);
+    cudaMemcpyAsync(d_sims, sims, sizeof(double) * ns, cudaMemcpyHostToDevice, ctx->stream);
+    int rc = cg::fp64_noise_matrix(ctx, nsims, n, d_sims, d_out, d_mean, ctx->stream);
+    if (rc == CG_OK) {
+        cudaMemcpyAsync(out_packed, d_out, sizeof(double) * np, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaMemcpyAsync(mean.data(), d_mean, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream);
+        cudaError_t e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = CG_ERR_CUDA; }
+    }
+    if (rc == CG_OK && max_abs_mean) {
+        double mx = 0;
+        for (int j = 0; j < n; ++j) mx = std::max(mx, std::fabs(mean[j]));
+        *max_abs_mean = mx;
+    }
+    cudaFree(d_sims);
+    cudaFree(d_out);
+    cudaFree(d_mean);
     return rc;
 }
 

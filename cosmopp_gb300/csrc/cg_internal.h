@@ -163,6 +163,9 @@ int fp64_ensure(cg_ctx* ctx, int B);
 int fp64_build_tiled(cg_ctx* ctx, int B, const double* d_cl, bool add_noise, cudaStream_t s);
 int fp64_build_tiled_into(cg_ctx* ctx, int B, const double* d_cl, bool add_noise, double* A, cudaStream_t s);
 int fp64_build_packed(cg_ctx* ctx, int B, const double* d_cl, double* d_out, cudaStream_t s);
+// packed noise covariance from simulations [nsims][n] and per-pixel means (device pointers)
+int fp64_noise_matrix(cg_ctx* ctx, int nsims, int n, const double* d_sims, double* d_out, double* d_mean,
+                      cudaStream_t s);
 int fp64_build_fiducial(cg_ctx* ctx, int lo, int hi, const double* d_tables, double m0, double* d_out,
                         cudaStream_t s);
 int fp64_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* d_d, int d_stride, double* d_m2lnl,

@@ -412,6 +412,72 @@ __global__ void dot_kernel(int n, const double* __restrict__ a, const double* __
     if (threadIdx.x == 0) *out = red[0];
 }
 
+// Averaging step of CMatrixGenerator::calculateNoiseMatrix (source/c_matrix_generator.cpp:887-910):
+// N_ij = (sum_k s_k[i] s_k[j]) / nsims, k in order, every product and sum rounded on its own
+// (the reference's loop, compiled without contraction), so the packed result is
+// bit-identical.  A CTA computes one 64x64 tile (I <= J) of the upper triangle; 16-deep
+// slices of the two 64-pixel panels are staged in shared memory; each thread keeps a
+// 4x4 block of sums at rows ty + 16a and columns tx + 16b.
+constexpr int kNoiseT = 64, kNoiseK = 16;
+
+__global__ void __launch_bounds__(kThreads, 2) noise_syrk_packed(int nsims, int n, const double* __restrict__ sims,
+                                                              double* __restrict__ out)
+{
+    const long t = blockIdx.x;
+    int J = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while ((long)J * (J + 1) / 2 > t) --J;
+    while ((long)(J + 1) * (J + 2) / 2 <= t) ++J;
+    const int I = (int)(t - (long)J * (J + 1) / 2);
+    __shared__ double si[kNoiseK][kNoiseT], sj[kNoiseK][kNoiseT];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    double acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+    for (int k0 = 0; k0 < nsims; k0 += kNoiseK) {
+#pragma unroll
+        for (int r = 0; r < kNoiseK * kNoiseT / kThreads; ++r) {
+            const int e = threadIdx.x + r * kThreads, kk = e / kNoiseT, c = e % kNoiseT, k = k0 + kk;
+            const int gi = I * kNoiseT + c, gj = J * kNoiseT + c;
+            si[kk][c] = (k < nsims && gi < n) ? sims[(size_t)k * n + gi] : 0.0;
+            sj[kk][c] = (k < nsims && gj < n) ? sims[(size_t)k * n + gj] : 0.0;
+        }
+        __syncthreads();
+        const int kend = min(kNoiseK, nsims - k0);
+        for (int kk = 0; kk < kend; ++kk) {
+            double x[4], y[4];
+#pragma unroll
+            for (int a = 0; a < 4; ++a) x[a] = si[kk][ty + 16 * a];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) y[b] = sj[kk][tx + 16 * b];
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) acc[a][b] = __dadd_rn(acc[a][b], __dmul_rn(x[a], y[b]));
+        }
+        __syncthreads();
+    }
+    const double dn = (double)nsims;
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int i = I * kNoiseT + ty + 16 * a, j = J * kNoiseT + tx + 16 * b;
+            if (i <= j && j < n) out[(size_t)j * (j + 1) / 2 + i] = __ddiv_rn(acc[a][b], dn);
+        }
+}
+
+// per-pixel mean over the simulations, summed in order (source/c_matrix_generator.cpp:901-910)
+__global__ void sim_means(int nsims, int n, const double* __restrict__ sims, double* __restrict__ mean)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    double s = 0.0;
+    for (int k = 0; k < nsims; ++k) s = __dadd_rn(s, sims[(size_t)k * n + j]);
+    mean[j] = __ddiv_rn(s, (double)nsims);
+}
+
 }  // namespace
 
 void fp64_packed_to_tiled(int n, int nt, const double* c, const double* f, const double* nz, double* A, cudaStream_t s)
@@ -504,6 +570,17 @@ int fp64_build_fiducial(cg_ctx* ctx, int lo, int hi, const double* d_tab, double
     build_fid_packed<<<(unsigned)((np + 4 * kThreads - 1) / (4 * kThreads)), kThreads, smem, s>>>(
         ctx->n, ctx->N, lo, hi, ctx->d_xyz, d_tab, m0, d_out);
     count_launch(ctx);
+    CG_CUDA_TRY(ctx, cudaGetLastError());
+    return CG_OK;
+}
+
+int fp64_noise_matrix(cg_ctx* ctx, int nsims, int n, const double* d_sims, double* d_out, double* d_mean,
+                      cudaStream_t s)
+{
+    const long nt = (n + kNoiseT - 1) / kNoiseT;
+    noise_syrk_packed<<<(unsigned)(nt * (nt + 1) / 2), kThreads, 0, s>>>(nsims, n, d_sims, d_out);
+    sim_means<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(nsims, n, d_sims, d_mean);
+    count_launch(ctx, 2);
     CG_CUDA_TRY(ctx, cudaGetLastError());
     return CG_OK;
 }

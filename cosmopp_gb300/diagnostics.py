@@ -1,4 +1,4 @@
-"""Chain diagnostics for the batched HMC output (host-side analysis)."""
+"""Chain diagnostics for the batched HMC and Metropolis-Hastings output (host-side analysis)."""
 import numpy as np
 
 
@@ -26,3 +26,22 @@ def ess(chain):
     """chain [n, nchains, npar] -> ESS summed over chains, per parameter [npar]."""
     n, nc, npar = chain.shape
     return np.array([sum(ess_1d(chain[:, c, k]) for c in range(nc)) for k in range(npar)])
+
+
+def gelman_rubin(chain):
+    """Potential scale reduction R per parameter over chains [n, nchains, npar], the
+    statistic MetropolisHastings uses as its GELMAN_RUBIN stopping rule
+    (include/mcmc.hpp:486-520): B = n var(chain means) (ddof 1), W = the mean of the
+    per-chain variances (ddof 1), R = sqrt(((n-1) W / n + B / n) / W); R = 1 when every
+    chain is constant at one value, 100 when W = 0 but the chains differ."""
+    x = np.asarray(chain, dtype=np.float64)
+    n, nc, _ = x.shape
+    if n < 2 or nc < 2:
+        raise ValueError("needs at least 2 chains of 2 states")
+    means = x.mean(axis=0)
+    b = n * means.var(axis=0, ddof=1)
+    w = x.var(axis=0, ddof=1).mean(axis=0)
+    var = (n - 1) * w / n + b / n
+    with np.errstate(divide="ignore", invalid="ignore"):
+        r = np.sqrt(var / w)
+    return np.where(w == 0, np.where(var == 0, 1.0, 100.0), r)

@@ -95,6 +95,17 @@ int cg_build_cmatrix_batched(cg_ctx* ctx, int B, const double* cl, double* out_p
 int cg_fiducial_matrix(cg_ctx* ctx, const double* cl, int lmax, int lmax_max, const double* beam,
                        double* out_packed);
 
+/* The averaging step of CMatrixGenerator::calculateNoiseMatrix
+   (include/c_matrix_generator.hpp:161, source/c_matrix_generator.cpp:887-910): packed
+   N_ij = (sum_k s_k[i] s_k[j]) / nsims from noise simulations sims [nsims][n] (each row one
+   simulated map at the kept pixels), the sum over k in order with every product and sum
+   rounded on its own, as the reference's loop: bit-identical to it.  max_abs_mean
+   (nullable) receives the largest |mean over the simulations| of any pixel, the figure the
+   reference prints.  Drawing and smoothing the simulations (HEALPix map2alm / alm2map)
+   is the caller's.  Uses the context's device only; n need not be the context's n. */
+int cg_noise_matrix_from_sims(cg_ctx* ctx, int nsims, int n, const double* sims, double* out_packed,
+                              double* max_abs_mean);
+
 /* ---- likelihood + gradient ---------------------------------------------- */
 /* -2lnL = d^T C^-1 d + ln det C for B C_l vectors, C = C(cl_b) + noise
    (the reference's Likelihood(C, 0, N, goodPixels).calculate(d),
@@ -129,6 +140,38 @@ int cg_reference_count(const cg_ctx* ctx);
 int cg_hmc_run(cg_ctx* ctx, const double* map, int nchains, const double* x0, const double* cl_template,
                int niter, int nleap, double tau, const double* mass, int jitter, unsigned long long seed,
                double* chain, double* accept_rate);
+
+/* ---- batched Metropolis-Hastings (MetropolisHastings::run, source/mcmc.cpp:455-700) ---- */
+#define CG_PRIOR_UNIFORM 0    /* 1/(max - min) on [p1 = min, p2 = max] (include/mcmc.hpp:350-357) */
+#define CG_PRIOR_GAUSS   1    /* normal density, mean p1, sigma p2 (include/mcmc.hpp:360-365) */
+/* A batched likelihood: -2lnL of nchains parameter vectors x [nchains][npar] into
+   m2lnl [nchains]; returns CG_OK or an error code that ends the run.  The batched form
+   of LikelihoodFunction::calculate (include/likelihood_function.hpp:7-17). */
+typedef int (*cg_batch_like_fn)(void* user, int nchains, const double* x, double* m2lnl);
+/* nchains chains from x0 [nchains][npar] for niter iterations.  Each iteration moves the
+   parameter blocks in turn (blocks[b] = the index after block b's last parameter, as
+   specifyParameterBlocks takes them; nblocks = 0 gives one block per parameter): the
+   proposal is x_j + N(0,1) sampling_width[j] on the block, or, with adapt != 0 and the
+   adaptive covariance ready, x + L g (g ~ N(0,1) on the block, L its Cholesky factor).
+   Every block move is ONE like() call over all chains.  Priors per parameter
+   (prior_mode CG_PRIOR_*, p1, p2; prior_mode NULL = flat); accept with
+   min(1, prior ratio exp(-d(-2lnL)/2)).  The adaptive covariance is updated every
+   100 iterations from all chains (factor 2.4^2/npar, diagonal epsilon 1e-7) and used once
+   more than 100 states entered it.  chain [niter+1][nchains][npar+1]: -2lnL then x
+   (row 0 = the start); accept_rate [nchains][nblocks'] (nullable) with nblocks' the
+   block count used; proposal_cov [npar][npar] (nullable): the final adaptive covariance.
+   Needs no device. */
+int cg_mh_sample(int nchains, int npar, cg_batch_like_fn like, void* user, const double* x0, int niter,
+                 const double* sampling_width, const int* prior_mode, const double* prior_p1,
+                 const double* prior_p2, int nblocks, const int* blocks, int adapt, unsigned long long seed,
+                 double* chain, double* accept_rate, double* proposal_cov);
+/* cg_mh_sample over this context's pixel likelihood of `map`, parameters x = ln C_l for
+   l = 2..lmax (npar = lmax - 1), the rest of C_l from cl_template; nchains <= max_batch.
+   A proposal the likelihood cannot evaluate (not positive definite) is rejected. */
+int cg_mh_run(cg_ctx* ctx, const double* map, int nchains, const double* x0, const double* cl_template,
+              int niter, const double* sampling_width, const int* prior_mode, const double* prior_p1,
+              const double* prior_p2, int nblocks, const int* blocks, int adapt, unsigned long long seed,
+              double* chain, double* accept_rate, double* proposal_cov);
 
 /* ---- instrumentation ------------------------------------------------------ */
 /* self-test of the failure path of the device's bounded waits: one thread waits, with a short

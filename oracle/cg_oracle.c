@@ -369,3 +369,32 @@ int orc_eval(const double* cl, int lmax, const double* xyz, int n, double fwhm,
     free(cinv);
     return st;
 }
+
+/* source/c_matrix_generator.cpp:887-910: each element summed over k in order, every
+   product and sum rounded on its own (-ffp-contract=off), then divided by nsims */
+void orc_noise_matrix(int nsims, int n, const double* sims, double* packed, double* max_abs_mean)
+{
+    /* pixel-major copy so the k loop reads contiguously; the summation order is unchanged */
+    double* st = (double*)malloc(sizeof(double) * (size_t)nsims * n);
+    for (int k = 0; k < nsims; ++k)
+        for (int i = 0; i < n; ++i) st[(size_t)i * nsims + k] = sims[(size_t)k * n + i];
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i <= j; ++i) {
+            const double* a = st + (size_t)i * nsims;
+            const double* b = st + (size_t)j * nsims;
+            double e = 0;
+            for (int k = 0; k < nsims; ++k) e += a[k] * b[k];
+            e /= nsims;
+            packed[(long)j * (j + 1) / 2 + i] = e;
+        }
+    free(st);
+    double mx = 0;
+    for (int j = 0; j < n; ++j) {
+        double avg = 0;
+        for (int k = 0; k < nsims; ++k) avg += sims[(long)k * n + j];
+        avg /= nsims;
+        if (fabs(avg) > mx) mx = fabs(avg);
+    }
+    if (max_abs_mean) *max_abs_mean = mx;
+}

@@ -57,6 +57,7 @@ def lib():
         L.orc_eval.argtypes = [_dp, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_double, _dp, _dp, ctypes.c_int,
                                _dp, _dp, _dp, _dp]
         L.orc_adjoint.argtypes = [_dp, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_double, _dp]
+        L.orc_noise_matrix.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_get_threads.restype = ctypes.c_int
         L.hp_ring2nest.restype = ctypes.c_long
@@ -182,6 +183,17 @@ def adjoint(w_packed, lmax, xyz, fwhm_deg):
     g = np.zeros(lmax + 1)
     lib().orc_adjoint(_p(w), int(lmax), _p(xyz), xyz.shape[0], float(fwhm_deg), _p(g))
     return g
+
+
+def noise_matrix(sims):
+    """Averaging step of calculateNoiseMatrix (source/c_matrix_generator.cpp:887-910) over
+    sims [nsims, n]: (packed noise matrix, max |per-pixel mean|)."""
+    sims = np.ascontiguousarray(sims, dtype=np.float64)
+    ns, n = sims.shape
+    out = np.zeros(n * (n + 1) // 2)
+    mx = ctypes.c_double(0)
+    lib().orc_noise_matrix(ns, n, _p(sims), _p(out), ctypes.byref(mx))
+    return out, mx.value
 
 
 # ---- the reference itself, compiled here by oracle/ref/Makefile (absent on machines

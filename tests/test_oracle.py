@@ -120,3 +120,24 @@ def test_healpix_ring_nest_roundtrip(oracle_mod):
     xyz = oracle_mod.unit_vectors(1, None, "RING")
     assert np.allclose(xyz[:4, 2], 2 / 3) and np.allclose(xyz[4:8, 2], 0) and np.allclose(xyz[8:, 2], -2 / 3)
     assert np.allclose(np.arctan2(xyz[4:8, 1], xyz[4:8, 0]) % (2 * np.pi), [0, np.pi / 2, np.pi, 3 * np.pi / 2])
+
+
+def test_oracle_noise_matrix_matches_an_independent_restatement(oracle_mod):
+    """calculateNoiseMatrix's averaging loop (source/c_matrix_generator.cpp:887-910) needs the
+    HEALPix transforms to run as shipped, so its oracle is pinned to a second restatement:
+    the same k-ordered sums formed as numpy rank-1 updates, every product and sum rounded on
+    its own, then divided by the simulation count."""
+    rng = np.random.default_rng(12)
+    for nsims, n in ((1, 5), (37, 61), (150, 130)):
+        sims = rng.standard_normal((nsims, n))
+        acc = np.zeros((n, n))
+        for k in range(nsims):
+            acc += np.outer(sims[k], sims[k])
+        acc /= nsims
+        want = np.concatenate([acc[:j + 1, j] for j in range(n)])
+        got, mx = oracle_mod.noise_matrix(sims)
+        assert np.array_equal(got, want)
+        means = np.zeros(n)
+        for k in range(nsims):
+            means += sims[k]
+        assert mx == np.abs(means / nsims).max()
