@@ -22,7 +22,7 @@ import os
 import numpy as np
 
 __all__ = ["Context", "Likelihood", "LikelihoodWithDerivs", "CGError", "library", "DET_OFFSET",
-           "ring2nest", "nest2ring", "pix2vec", "beam", "mh_sample"]
+           "ring2nest", "nest2ring", "pix2vec", "beam", "mh_sample", "LegendrePolynomialContainer"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libcosmopp_gb300.so")
@@ -96,6 +96,7 @@ def library():
     _mh_tail = [_dp, _ip, _dp, _dp, ctypes.c_int, _ip, ctypes.c_int, ctypes.c_ulonglong, _dp, _dp, _dp]
     L.cg_mh_sample.argtypes = [ctypes.c_int, ctypes.c_int, _BATCH_LIKE, ctypes.c_void_p, _dp, ctypes.c_int] + _mh_tail
     L.cg_mh_run.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, _dp, _dp, ctypes.c_int] + _mh_tail
+    L.cg_legendre_table.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp]
     L.cg_noise_matrix_from_sims.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
     L.cg_selftest_wait_timeout.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
     L.cg_launch_count.restype = ctypes.c_longlong
@@ -322,6 +323,14 @@ class Context:
                                        _p(acc)))
         return chain, acc
 
+    def legendre_table(self, lmax, l0=0):
+        """LegendrePolynomialContainer's table for this context's pixels (cg_legendre_table):
+        [lmax + 1 - l0, n(n+1)/2] with P_l(n_i . n_j) at j(j+1)/2 + i."""
+        n = self.n
+        out = np.zeros((lmax + 1 - l0, n * (n + 1) // 2))
+        self._check(self._L.cg_legendre_table(self._h, int(l0), int(lmax) + 1, _p(out)))
+        return out
+
     def noise_matrix_from_sims(self, sims):
         """Averaging step of CMatrixGenerator::calculateNoiseMatrix
         (source/c_matrix_generator.cpp:887-910) on the device: sims [nsims, n] simulated
@@ -419,6 +428,41 @@ def mh_sample(like, x0, niter, sampling_width, priors=None, blocks=None, adapt=T
     if rc:
         raise CGError(rc, "cg_mh_sample")
     return out
+
+
+class LegendrePolynomialContainer:
+    """The reference's LegendrePolynomialContainer (include/c_matrix_generator.hpp:10-36):
+    ``LegendrePolynomialContainer(lmax, nside, good_pixels)`` builds P_l(n_i . n_j) on the GPU
+    (NEST pixel indices, None = all); ``LegendrePolynomialContainer(file_name=...)`` reads the
+    reference's binary file (int lMax, int nPix, then the packed table of every l)."""
+
+    def __init__(self, lmax=None, nside=None, good_pixels=None, file_name=None, device=0):
+        if file_name is not None:
+            raw = open(file_name, "rb").read()
+            if len(raw) < 8:
+                raise CGError(CG_ERR_BAD_ARG, "truncated Legendre table in %s" % file_name)
+            lm, npix = (int(v) for v in np.frombuffer(raw[:8], dtype=np.int32))
+            if lm < 0 or npix < 0:
+                raise CGError(CG_ERR_BAD_ARG, "invalid header in %s" % file_name)
+            np_ = npix * (npix + 1) // 2
+            if len(raw) < 8 + 8 * (lm + 1) * np_:
+                raise CGError(CG_ERR_BAD_ARG, "truncated Legendre table in %s" % file_name)
+            data = np.frombuffer(raw[8:8 + 8 * (lm + 1) * np_], dtype=np.float64)
+            self.lmax, self.npix, self.table = lm, npix, data.reshape(lm + 1, np_).copy()
+            return
+        with Context(lmax=max(2, int(lmax)), fwhm_deg=1.0, nside=nside, good_pixels=good_pixels, scheme="NEST",
+                     max_batch=1, precision="fp64", device=device) as ctx:
+            self.lmax, self.npix, self.table = int(lmax), ctx.n, ctx.legendre_table(int(lmax))
+
+    def value(self, l, j, i):
+        """P_l(n_i . n_j), i <= j (source/c_matrix_generator.cpp:78-87)."""
+        return float(self.table[l, j * (j + 1) // 2 + i])
+
+    def write_into_file(self, file_name):
+        """The reference's file format (source/c_matrix_generator.cpp:136-162)."""
+        with open(file_name, "wb") as f:
+            f.write(np.array([self.lmax, self.npix], dtype=np.int32).tobytes())
+            f.write(np.ascontiguousarray(self.table, dtype=np.float64).tobytes())
 
 
 class Likelihood:

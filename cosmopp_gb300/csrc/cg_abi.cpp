@@ -283,6 +283,45 @@ extern "C" int cg_fiducial_matrix(cg_ctx* ctx, const double* cl, int lmax, int l
     return rc;
 }
 
+extern "C" int cg_legendre_table(cg_ctx* ctx, int l0, int l1, double* out)
+{
+    if (!ctx || !out || l0 < 0 || l1 <= l0 || l1 > CG_FIDUCIAL_LMAX_MAX + 1) {
+        if (ctx) ctx->err = "bad arguments to cg_legendre_table (need 0 <= l0 < l1 <= 4097)";
+        return CG_ERR_BAD_ARG;
+    }
+    CG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const size_t np = (size_t)ctx->n * (ctx->n + 1) / 2;
+    // the l range goes through a device buffer of at most 1 GiB, a slab of l values at a time
+    const int slab = (int)std::max<size_t>(1, std::min<size_t>((size_t)(l1 - l0), ((size_t)1 << 30) / (8 * np)));
+    std::vector<double> ab((size_t)2 * l1, 0.0);
+    for (int l = 1; l < l1; ++l) {  // include/legendre.hpp:34
+        ab[l] = 2 - 1.0 / l;
+        ab[l1 + l] = 1 - 1.0 / l;
+    }
+    double *d_ab = nullptr, *d_out = nullptr;
+    CG_CUDA_TRY(ctx, cudaMalloc((void**)&d_ab, sizeof(double) * ab.size()));
+    if (cudaMalloc((void**)&d_out, sizeof(double) * np * slab) != cudaSuccess) {
+        cudaFree(d_ab);
+        ctx->err = "cg_legendre_table: out of device memory";
+        return CG_ERR_ALLOC;
+    }
+    cudaMemcpyAsync(d_ab, ab.data(), sizeof(double) * ab.size(), cudaMemcpyHostToDevice, ctx->stream);
+    int rc = CG_OK;
+    for (int a = l0; a < l1 && rc == CG_OK; a += slab) {
+        const int b = std::min(l1, a + slab);
+        rc = cg::fp64_legendre_table(ctx, a, b, d_ab, d_ab + l1, d_out, ctx->stream);
+        if (rc == CG_OK) {
+            cudaMemcpyAsync(out + (size_t)(a - l0) * np, d_out, sizeof(double) * np * (b - a), cudaMemcpyDeviceToHost,
+                            ctx->stream);
+            cudaError_t e = cudaStreamSynchronize(ctx->stream);
+            if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = CG_ERR_CUDA; }
+        }
+    }
+    cudaFree(d_ab);
+    cudaFree(d_out);
+    return rc;
+}
+
 extern "C" int cg_noise_matrix_from_sims(cg_ctx* ctx, int nsims, int n, const double* sims, double* out_packed,
                                          double* max_abs_mean)
 {

@@ -163,6 +163,10 @@ int fp64_ensure(cg_ctx* ctx, int B);
 int fp64_build_tiled(cg_ctx* ctx, int B, const double* d_cl, bool add_noise, cudaStream_t s);
 int fp64_build_tiled_into(cg_ctx* ctx, int B, const double* d_cl, bool add_noise, double* A, cudaStream_t s);
 int fp64_build_packed(cg_ctx* ctx, int B, const double* d_cl, double* d_out, cudaStream_t s);
+// P_l(x_ij) for l0 <= l < l1 into d_out [(l1 - l0)][n(n+1)/2]; d_a, d_b = the recurrence
+// coefficients, at least l1 entries each (device pointers)
+int fp64_legendre_table(cg_ctx* ctx, int l0, int l1, const double* d_a, const double* d_b, double* d_out,
+                        cudaStream_t s);
 // packed noise covariance from simulations [nsims][n] and per-pixel means (device pointers)
 int fp64_noise_matrix(cg_ctx* ctx, int nsims, int n, const double* d_sims, double* d_out, double* d_mean,
                       cudaStream_t s);

@@ -412,6 +412,41 @@ __global__ void dot_kernel(int n, const double* __restrict__ a, const double* __
     if (threadIdx.x == 0) *out = red[0];
 }
 
+// LegendrePolynomialContainer's table (source/c_matrix_generator.cpp:30-76): P_l(x_ij) for
+// l0 <= l < l1 at out[(l - l0) np + j(j+1)/2 + i], i <= j, by Math::Legendre's recurrence
+// (include/legendre.hpp:26-37: P_0 = 1, P_1 = x, P_l = ((2 - 1/l) x) P_{l-1} - (1 - 1/l) P_{l-2},
+// coefficients a_l, b_l from the host) with the reference's dot product and clamp, so the
+// table is bit-identical.  One thread per pair; stores of one l are coalesced over pairs.
+__global__ void __launch_bounds__(kThreads) legendre_table(int n, int N, int l0, int l1,
+                                                           const double* __restrict__ xyz,
+                                                           const double* __restrict__ a,
+                                                           const double* __restrict__ b,
+                                                           double* __restrict__ out)
+{
+    const long np = (long)n * (n + 1) / 2;
+    const long k = (long)blockIdx.x * kThreads + threadIdx.x;
+    if (k >= np) return;
+    long j = (long)((sqrt(8.0 * (double)k + 1.0) - 1.0) * 0.5);
+    while (j * (j + 1) / 2 > k) --j;
+    while ((j + 1) * (j + 2) / 2 <= k) ++j;
+    const int i = (int)(k - j * (j + 1) / 2);
+    const double x = pair_dot(xyz, N, i, (int)j);
+    double p0 = 1.0, p1 = x;
+    for (int l = 0; l < l1; ++l) {
+        double p;
+        if (l == 0) {
+            p = 1.0;
+        } else if (l == 1) {
+            p = x;
+        } else {
+            p = __dsub_rn(__dmul_rn(__dmul_rn(a[l], x), p1), __dmul_rn(b[l], p0));
+            p0 = p1;
+            p1 = p;
+        }
+        if (l >= l0) out[(size_t)(l - l0) * np + k] = p;
+    }
+}
+
 // Averaging step of CMatrixGenerator::calculateNoiseMatrix (source/c_matrix_generator.cpp:887-910):
 // N_ij = (sum_k s_k[i] s_k[j]) / nsims, k in order, every product and sum rounded on its own
 // (the reference's loop, compiled without contraction), so the packed result is
@@ -569,6 +604,17 @@ int fp64_build_fiducial(cg_ctx* ctx, int lo, int hi, const double* d_tab, double
         CG_CUDA_TRY(ctx, cudaFuncSetAttribute(build_fid_packed, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     build_fid_packed<<<(unsigned)((np + 4 * kThreads - 1) / (4 * kThreads)), kThreads, smem, s>>>(
         ctx->n, ctx->N, lo, hi, ctx->d_xyz, d_tab, m0, d_out);
+    count_launch(ctx);
+    CG_CUDA_TRY(ctx, cudaGetLastError());
+    return CG_OK;
+}
+
+int fp64_legendre_table(cg_ctx* ctx, int l0, int l1, const double* d_a, const double* d_b, double* d_out,
+                        cudaStream_t s)
+{
+    const long np = (long)ctx->n * (ctx->n + 1) / 2;
+    legendre_table<<<(unsigned)((np + kThreads - 1) / kThreads), kThreads, 0, s>>>(ctx->n, ctx->N, l0, l1, ctx->d_xyz,
+                                                                                 d_a, d_b, d_out);
     count_launch(ctx);
     CG_CUDA_TRY(ctx, cudaGetLastError());
     return CG_OK;

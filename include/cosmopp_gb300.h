@@ -95,6 +95,13 @@ int cg_build_cmatrix_batched(cg_ctx* ctx, int B, const double* cl, double* out_p
 int cg_fiducial_matrix(cg_ctx* ctx, const double* cl, int lmax, int lmax_max, const double* beam,
                        double* out_packed);
 
+/* LegendrePolynomialContainer's table (include/c_matrix_generator.hpp:10-36,
+   source/c_matrix_generator.cpp:30-76) for this context's pixels: P_l(n_i . n_j) for
+   l0 <= l < l1 at out[(l - l0) * n(n+1)/2 + j(j+1)/2 + i], i <= j -- the order of the
+   reference's table file after its two int header fields (source/c_matrix_generator.cpp:136-162).
+   Math::Legendre's recurrence and the reference's clamped dot product: bit-identical.
+   0 <= l0 < l1 <= CG_FIDUCIAL_LMAX_MAX + 1. */
+int cg_legendre_table(cg_ctx* ctx, int l0, int l1, double* out);
 /* The averaging step of CMatrixGenerator::calculateNoiseMatrix
    (include/c_matrix_generator.hpp:161, source/c_matrix_generator.cpp:887-910): packed
    N_ij = (sum_k s_k[i] s_k[j]) / nsims from noise simulations sims [nsims][n] (each row one

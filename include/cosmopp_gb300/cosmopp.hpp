@@ -4,7 +4,10 @@
 // Same class names, signatures, argument meaning and error behaviour as the
 // reference (Cosmo++ 3.1):
 //   CMatrix           include/c_matrix.hpp:10-83, source/c_matrix.cpp
-//   CMatrixGenerator  include/c_matrix_generator.hpp:40-160 (clToCMatrix, generateNoiseMatrix)
+//   LegendrePolynomialContainer include/c_matrix_generator.hpp:10-36, source/c_matrix_generator.cpp:30-162
+//   CMatrixGenerator  include/c_matrix_generator.hpp:40-160 (clToCMatrix, getFiducialMatrix,
+//                     generateNoiseMatrix, the noise matrix's averaging step)
+//   Utils::readClFromFile source/utils.cpp:173-217
 //   LikelihoodResult  include/likelihood.hpp:18-30
 //   Likelihood        include/likelihood.hpp:36-132, source/likelihood.cpp:38-328
 //   StandardException include/exception_handler.hpp:10-30
@@ -143,17 +146,125 @@ private:
     std::string comment_;
 };
 
+/// Table of P_l(n_i . n_j), l = 0..lMax, i <= j, for a pixel set
+/// (include/c_matrix_generator.hpp:10-36).  Built on the GPU with the reference's
+/// recurrence and dot product (bit-identical values); the file format is the
+/// reference's (int lMax, int nPix, then the packed table of every l).
+class LegendrePolynomialContainer
+{
+public:
+    /// source/c_matrix_generator.cpp:30-76; goodPixels in NEST ordering (NULL = all pixels)
+    LegendrePolynomialContainer(int lMax, long nSide, const std::vector<int>* goodPixels = NULL, int device = 0)
+        : lMax_(lMax)
+    {
+        if (lMax < 0 || lMax > CG_FIDUCIAL_LMAX_MAX) cosmopp_gb300_detail::raise("LegendrePolynomialContainer: invalid lMax");
+        cg_config cfg;
+        cg_config_init(&cfg);
+        cfg.nside = nSide;
+        cfg.scheme = CG_SCHEME_NEST;
+        if (goodPixels) {
+            cfg.good_pixels = goodPixels->data();
+            cfg.n = (int)goodPixels->size();
+        }
+        cfg.lmax = lMax < 2 ? 2 : lMax;
+        cfg.fwhm_deg = 1.0;
+        cfg.device = device;
+        cg_ctx* ctx = NULL;
+        cosmopp_gb300_detail::check(cg_create(&ctx, &cfg), "LegendrePolynomialContainer", cg_last_error(NULL));
+        nPix_ = cg_get_n(ctx);
+        data_.resize((size_t)(lMax + 1) * pairs());
+        const int rc = cg_legendre_table(ctx, 0, lMax + 1, data_.data());
+        std::string err = rc ? cg_last_error(ctx) : "";
+        cg_destroy(ctx);
+        cosmopp_gb300_detail::check(rc, "LegendrePolynomialContainer", err.c_str());
+    }
+    /// source/c_matrix_generator.cpp:89-134
+    explicit LegendrePolynomialContainer(const char* fileName)
+    {
+        std::ifstream in(fileName, std::ios::in | std::ios::binary);
+        if (!in) cosmopp_gb300_detail::raise(std::string("Cannot open input file ") + fileName + ".");
+        int lMax = -1, nPix = -1;
+        in.read((char*)&lMax, sizeof(int));
+        if (lMax < 0) cosmopp_gb300_detail::raise("Invalid lMax = " + std::to_string(lMax) + " read from file " + fileName + ".");
+        in.read((char*)&nPix, sizeof(int));
+        if (nPix < 0) cosmopp_gb300_detail::raise("Invalid nPix = " + std::to_string(nPix) + " read from file " + fileName + ".");
+        lMax_ = lMax;
+        nPix_ = nPix;
+        data_.resize((size_t)(lMax + 1) * pairs());
+        in.read((char*)data_.data(), (std::streamsize)(sizeof(double) * data_.size()));
+        if (!in) cosmopp_gb300_detail::raise(std::string("Truncated Legendre table in ") + fileName + ".");
+    }
+    /// P_l(n_i . n_j) for i <= j (source/c_matrix_generator.cpp:78-87)
+    double value(int l, int j, int i) const { return data_[(size_t)l * pairs() + (size_t)j * (j + 1) / 2 + i]; }
+    /// source/c_matrix_generator.cpp:136-162
+    void writeIntoFile(const char* fileName) const
+    {
+        std::ofstream out(fileName, std::ios::binary | std::ios::out);
+        if (!out) cosmopp_gb300_detail::raise(std::string("Cannot write into file ") + fileName + ".");
+        out.write((const char*)&lMax_, sizeof(int));
+        out.write((const char*)&nPix_, sizeof(int));
+        out.write((const char*)data_.data(), (std::streamsize)(sizeof(double) * data_.size()));
+    }
+    int lMax() const { return lMax_; }
+    int nPix() const { return nPix_; }
+
+private:
+    size_t pairs() const { return (size_t)nPix_ * (nPix_ + 1) / 2; }
+    int lMax_ = -1, nPix_ = 0;
+    std::vector<double> data_;  // [l][j(j+1)/2 + i]
+};
+
+namespace Utils
+{
+/// source/utils.cpp:173-217: one C_l per line from l = 0 (hasL: each line starts with l;
+/// isDl: the values are D_l = l(l+1) C_l / (2 pi) for l > 0); stops at the first empty line
+inline void readClFromFile(const char* fileName, std::vector<double>& cl, bool hasL = false, bool isDl = false)
+{
+    std::ifstream in(fileName);
+    if (!in) cosmopp_gb300_detail::raise(std::string("Cannot open the input file ") + fileName + ".");
+    cl.clear();
+    int l = 0;
+    while (!in.eof()) {
+        std::string s;
+        std::getline(in, s);
+        if (s == "") break;
+        std::stringstream str(s);
+        int dummyL;
+        double val;
+        if (hasL) {
+            str >> dummyL;
+            if (dummyL != l)
+                cosmopp_gb300_detail::raise(std::string("Invalid format of the input file ") + fileName +
+                                            ". Expected to read l = " + std::to_string(l) + " but found l = " +
+                                            std::to_string(dummyL) + ".");
+        }
+        str >> val;
+        if (isDl && l) val *= (2 * M_PI / (l * (l + 1)));
+        cl.push_back(val);
+        ++l;
+    }
+}
+}  // namespace Utils
+
 /// Converts C_l to pixel-space covariance matrices on the GPU.
 class CMatrixGenerator
 {
 public:
     /// source/c_matrix_generator.cpp:164-232; goodPixels in NEST ordering (NULL = all pixels),
     /// fwhm in degrees, lmax = cl.size() - 1.  Bit-identical to the reference.  Returns a new
-    /// CMatrix the caller deletes, as the reference does.
+    /// CMatrix the caller deletes, as the reference does.  A table lp is checked against the
+    /// pixel count and lmax but not read: its values are the ones the device's recurrence
+    /// computes, so the matrix is the same with or without it.
     static CMatrix* clToCMatrix(const std::vector<double>& cl, long nSide, double fwhm,
-                                const std::vector<int>* goodPixels = NULL, const void* /*lp*/ = NULL, int device = 0)
+                                const std::vector<int>* goodPixels = NULL, const LegendrePolynomialContainer* lp = NULL,
+                                int device = 0)
     {
         if (cl.size() < 3) cosmopp_gb300_detail::raise("clToCMatrix: cl must reach at least l = 2");
+        if (lp) {
+            const long nPix = goodPixels ? (long)goodPixels->size() : (long)cg_nside2npix(nSide);
+            if (lp->nPix() != nPix || lp->lMax() < (int)cl.size() - 1)
+                cosmopp_gb300_detail::raise("clToCMatrix: the Legendre table does not cover these pixels and l");
+        }
         cg_config cfg;
         cg_config_init(&cfg);
         cfg.nside = nSide;
@@ -177,15 +288,30 @@ public:
         }
         return m;
     }
+    /// source/c_matrix_generator.cpp:234-240: C_l read from a text file (Utils::readClFromFile,
+    /// one value per line from l = 0); lMax is not used, as in the reference
+    static CMatrix* clToCMatrix(const char* clFileName, long nSide, int /*lMax*/, double fwhm,
+                                const std::vector<int>* goodPixels = NULL, const LegendrePolynomialContainer* lp = NULL,
+                                int device = 0)
+    {
+        std::vector<double> cl;
+        Utils::readClFromFile(clFileName, cl);
+        return clToCMatrix(cl, nSide, fwhm, goodPixels, lp, device);
+    }
     /// source/c_matrix_generator.cpp:706-772: sum over l = lMax+1 .. 4 nSide plus the
     /// monopole/dipole term 100 C_2 (1 + x) B_2^2; cl must reach l = 4 nSide.  Bit-identical
     /// to the reference.  Returns a new CMatrix the caller deletes.
     static CMatrix* getFiducialMatrix(const std::vector<double>& cl, long nSide, int lMax, double fwhm,
-                                      const std::vector<int>* goodPixels = NULL, const void* /*lp*/ = NULL,
-                                      int device = 0)
+                                      const std::vector<int>* goodPixels = NULL,
+                                      const LegendrePolynomialContainer* lp = NULL, int device = 0)
     {
         const int lMaxMax = (int)(4 * nSide);
         if ((long)cl.size() < lMaxMax + 1) cosmopp_gb300_detail::raise("getFiducialMatrix: cl must reach l = 4 nSide");
+        if (lp) {
+            const long nPix = goodPixels ? (long)goodPixels->size() : (long)cg_nside2npix(nSide);
+            if (lp->nPix() != nPix || lp->lMax() < lMaxMax)
+                cosmopp_gb300_detail::raise("getFiducialMatrix: the Legendre table does not cover these pixels and l");
+        }
         cg_config cfg;
         cg_config_init(&cfg);
         cfg.nside = nSide;
@@ -209,6 +335,15 @@ public:
             cosmopp_gb300_detail::check(rc, "getFiducialMatrix", err.c_str());
         }
         return m;
+    }
+    /// source/c_matrix_generator.cpp:697-703: C_l read from a text file
+    static CMatrix* getFiducialMatrix(const char* clFileName, long nSide, int lMax, double fwhm,
+                                      const std::vector<int>* goodPixels = NULL,
+                                      const LegendrePolynomialContainer* lp = NULL, int device = 0)
+    {
+        std::vector<double> cl;
+        Utils::readClFromFile(clFileName, cl);
+        return getFiducialMatrix(cl, nSide, lMax, fwhm, goodPixels, lp, device);
     }
     /// source/c_matrix_generator.cpp:774-787 (full sky, noise^2 on the diagonal)
     static CMatrix* generateNoiseMatrix(long nSide, double noise = 1e-3)

@@ -398,3 +398,16 @@ void orc_noise_matrix(int nsims, int n, const double* sims, double* packed, doub
     }
     if (max_abs_mean) *max_abs_mean = mx;
 }
+
+/* LegendrePolynomialContainer(lMax, nSide, goodPixels) (source/c_matrix_generator.cpp:30-76):
+   out[l * np + j(j+1)/2 + i] = Legendre::calculate(l, clamped dot), np = n(n+1)/2 */
+void orc_legendre_table(int lmax, const double* xyz, int n, double* out)
+{
+    const long np = (long)n * (n + 1) / 2;
+#pragma omp parallel for schedule(dynamic, 8)
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i <= j; ++i) {
+            const double dot = clamped_dot(xyz + 3 * i, xyz + 3 * j);
+            for (int l = 0; l <= lmax; ++l) out[(long)l * np + (long)j * (j + 1) / 2 + i] = orc_legendre(l, dot);
+        }
+}

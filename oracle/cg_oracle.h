@@ -74,6 +74,10 @@ int orc_eval(const double* cl, int lmax, const double* xyz, int n, double fwhm_d
 /* The adjoint alone: grad_l = sum_ij W_ij (2l+1)/(4pi) B_l^2 P_l(x_ij) for a packed symmetric W */
 void orc_adjoint(const double* w_packed, int lmax, const double* xyz, int n, double fwhm_deg, double* grad);
 
+/* LegendrePolynomialContainer's table (source/c_matrix_generator.cpp:30-76):
+   out[l * n(n+1)/2 + j(j+1)/2 + i] = P_l(clamped n_i . n_j), l = 0..lmax */
+void orc_legendre_table(int lmax, const double* xyz, int n, double* out);
+
 /* The averaging step of CMatrixGenerator::calculateNoiseMatrix
    (source/c_matrix_generator.cpp:887-910): packed N_ij = (sum_k s_k[i] s_k[j]) / nsims over
    noise simulations sims [nsims][n] at the kept pixels, k summed in order, and the largest

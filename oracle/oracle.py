@@ -58,6 +58,7 @@ def lib():
                                _dp, _dp, _dp, _dp]
         L.orc_adjoint.argtypes = [_dp, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_double, _dp]
         L.orc_noise_matrix.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
+        L.orc_legendre_table.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _dp]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_get_threads.restype = ctypes.c_int
         L.hp_ring2nest.restype = ctypes.c_long
@@ -183,6 +184,25 @@ def adjoint(w_packed, lmax, xyz, fwhm_deg):
     g = np.zeros(lmax + 1)
     lib().orc_adjoint(_p(w), int(lmax), _p(xyz), xyz.shape[0], float(fwhm_deg), _p(g))
     return g
+
+
+def legendre_table(lmax, xyz):
+    """LegendrePolynomialContainer's table (source/c_matrix_generator.cpp:30-76):
+    [lmax + 1, n(n+1)/2] with P_l(x_ij) at j(j+1)/2 + i."""
+    xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+    n = xyz.shape[0]
+    out = np.zeros((lmax + 1, n * (n + 1) // 2))
+    lib().orc_legendre_table(int(lmax), _p(xyz), n, _p(out))
+    return out
+
+
+def read_legendre_file(path):
+    """A LegendrePolynomialContainer file (source/c_matrix_generator.cpp:89-134): int lMax,
+    int nPix, then (lMax + 1) packed tables -> (lmax, npix, [lmax + 1, npix(npix+1)/2])."""
+    raw = open(path, "rb").read()
+    lmax, npix = np.frombuffer(raw[:8], dtype=np.int32)
+    data = np.frombuffer(raw[8:], dtype=np.float64)
+    return int(lmax), int(npix), data.reshape(int(lmax) + 1, int(npix) * (int(npix) + 1) // 2)
 
 
 def noise_matrix(sims):

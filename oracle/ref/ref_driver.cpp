@@ -107,6 +107,34 @@ extern "C" int ref_fiducial_matrix(const double* cl, int cl_size, long nside, in
     } catch (std::exception& e) { g_err = e.what(); return 1; }
 }
 
+/* LegendrePolynomialContainer(lMax, nSide, goodPixels) written by its own writeIntoFile
+   (source/c_matrix_generator.cpp:30-76,136-162) */
+extern "C" int ref_legendre_table_write(int lmax, long nside, const int* good_nest, int n, const char* path)
+{
+    try {
+        std::vector<int> good(good_nest, good_nest + n);
+        LegendrePolynomialContainer lp(lmax, nside, &good);
+        lp.writeIntoFile(path);
+        return 0;
+    } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
+/* clToCMatrix with a LegendrePolynomialContainer read back by its file constructor
+   (source/c_matrix_generator.cpp:89-134,164-232) */
+extern "C" int ref_cl_to_cmatrix_lp_file(const double* cl, int lmax, long nside, double fwhm_deg,
+                                         const int* good_nest, int n, const char* path, double* out_packed)
+{
+    try {
+        std::vector<double> c(cl, cl + lmax + 1);
+        std::vector<int> good(good_nest, good_nest + n);
+        LegendrePolynomialContainer lp(path);
+        CMatrix* m = CMatrixGenerator::clToCMatrix(c, nside, fwhm_deg, &good, &lp);
+        copy_packed(*m, out_packed);
+        delete m;
+        return 0;
+    } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
 /* Utils::beamFunction (source/utils.cpp:54-64) and the pixel-window reader
    with the unit window the shim serves (source/utils.cpp:66-170). */
 extern "C" double ref_beam(int l, double fwhm_deg) { return Utils::beamFunction(l, fwhm_deg); }

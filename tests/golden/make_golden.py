@@ -15,9 +15,13 @@ them through ctypes.  Every number stored below comes from the reference:
   pin the adjoint gradient the reference does not have.
 * getFiducialMatrix (l = lmax+1 .. 4 nside plus the monopole/dipole term) and
   the full low-l flow Likelihood(C, fiducial, N, goodPixels).calculate(d) of
-  source/test_like_low.cpp:181-193 that uses it.
+  source/test_like_low.cpp:181-193 that uses it;
+* a LegendrePolynomialContainer table file written by the reference's own
+  writeIntoFile, and the clToCMatrix covariance computed from that file read
+  back by the reference's file constructor.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py [part ...]   (parts: main, fiducial,
+legendre; default all)
 """
 import ctypes
 import hashlib
@@ -98,6 +102,28 @@ def fiducial_cases(R):
         print(name, "n", n, "like", lk, "chi2", chi2)
 
 
+LEGENDRE_CASE = ("legendre_nside2_lmax8", 2, 8, 440.0, 0.8)
+
+
+def legendre_cases(R):
+    name, nside, lmax, fwhm_am, keep = LEGENDRE_CASE
+    fwhm = fwhm_am / 60.0
+    ring = W.bernoulli_mask(nside, keep, 1234)
+    nest = O.ring2nest(nside, ring)
+    n = len(nest)
+    path = os.path.join(HERE, name + ".bin")
+    rc = R.ref_legendre_table_write(lmax, nside, nest.ctypes.data_as(ip), n, path.encode())
+    assert rc == 0, R.ref_last_error()
+    cl = W.fiducial_cl(lmax)
+    c_lp = np.zeros(n * (n + 1) // 2)
+    rc = R.ref_cl_to_cmatrix_lp_file(cl.ctypes.data_as(dp), lmax, nside, fwhm, nest.ctypes.data_as(ip), n,
+                                     path.encode(), c_lp.ctypes.data_as(dp))
+    assert rc == 0, R.ref_last_error()
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), nside=nside, lmax=lmax, fwhm_deg=fwhm, ring_kept=ring,
+                        nest_good=nest, cl=cl, c_lp=c_lp, c_plain=ref_cmatrix(R, cl, nside, fwhm, nest))
+    print(name, "n", n, "bytes", os.path.getsize(path))
+
+
 def ref_cmatrix(R, cl, nside, fwhm, nest):
     n = len(nest)
     out = np.zeros(n * (n + 1) // 2)
@@ -115,10 +141,19 @@ def ref_like(R, cl, nside, fwhm, nest, sigma, d):
     return chi2.value, ld.value, lk.value
 
 
-def main():
+def main(parts):
     if not O.ref_available():
         raise SystemExit("build the reference first: make -C oracle/ref")
     R = O.ref()
+    R.ref_legendre_table_write.argtypes = [ctypes.c_int, ctypes.c_long, ip, ctypes.c_int, ctypes.c_char_p]
+    R.ref_cl_to_cmatrix_lp_file.argtypes = [dp, ctypes.c_int, ctypes.c_long, ctypes.c_double, ip, ctypes.c_int,
+                                            ctypes.c_char_p, dp]
+    if "legendre" in parts:
+        legendre_cases(R)
+    if "main" not in parts:
+        if "fiducial" in parts:
+            fiducial_cases(R)
+        return
     os.makedirs(os.path.join(HERE, "_kat", "test_files"), exist_ok=True)
     cwd = os.getcwd()
     os.chdir(os.path.join(HERE, "_kat"))  # the matrix subtests write text files under test_files/
@@ -166,8 +201,9 @@ def main():
             out["c_packed"] = c_fid
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
         print(name, "n", n, "m2lnl", out["m2lnl"][0], "chi2", rows[0, 0])
-    fiducial_cases(R)
+    if "fiducial" in parts:
+        fiducial_cases(R)
 
 
 if __name__ == "__main__":
-    main()
+    main(set(sys.argv[1:]) or {"main", "fiducial", "legendre"})

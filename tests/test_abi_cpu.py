@@ -73,3 +73,26 @@ def test_bad_config_rejected_before_device():
     assert ei.value.code == cg.CG_ERR_BAD_ARG
     with pytest.raises(cg.CGError):
         cg.Context(lmax=8, fwhm_deg=7.0, nside=2, good_pixels=[0, 1, 999])
+
+
+def test_legendre_file_reader_and_writer_match_the_reference_format(oracle_mod, tmp_path):
+    """The reference's own LegendrePolynomialContainer file reads into the values the oracle
+    computes, and writes back byte for byte (no device needed for file I/O)."""
+    g = load_golden("legendre_nside2_lmax8")
+    path = os.path.join(ROOT, "tests", "golden", "legendre_nside2_lmax8.bin")
+    lp = cg.LegendrePolynomialContainer(file_name=path)
+    assert lp.lmax == int(g["lmax"]) and lp.npix == len(g["nest_good"])
+    xyz = oracle_mod.unit_vectors(int(g["nside"]), g["nest_good"], "NEST")
+    want = oracle_mod.legendre_table(lp.lmax, xyz)
+    assert np.array_equal(lp.table, want)
+    j, i = 20, 7
+    x = float(np.clip(xyz[i] @ xyz[j], -1, 1))
+    assert lp.value(3, j, i) == want[3, j * (j + 1) // 2 + i]
+    assert abs(lp.value(3, j, i) - 0.5 * (5 * x ** 3 - 3 * x)) < 1e-14
+    out = tmp_path / "lp.bin"
+    lp.write_into_file(str(out))
+    assert open(out, "rb").read() == open(path, "rb").read()
+    short = tmp_path / "short.bin"
+    short.write_bytes(open(path, "rb").read()[:100])
+    with pytest.raises(cg.CGError):
+        cg.LegendrePolynomialContainer(file_name=str(short))

@@ -74,3 +74,31 @@ def test_low_l_flow_with_fiducial_matrix_through_cxx_dropin(exe, tmp_path):
     assert abs(chi2 - float(g["chi2"])) <= 1e-6
     assert abs(logdet - float(g["logdet_ref"])) <= 1e-6
     assert abs(like - float(g["like_ref"])) <= 2e-6
+
+
+def test_legendre_container_and_cl_file_through_cxx_dropin(tmp_path):
+    """LegendrePolynomialContainer built on the GPU writes the reference's file byte for
+    byte; the reference's own file reads back to the same values; clToCMatrix with that
+    table and clToCMatrix from a C_l text file give the reference's matrices."""
+    g = load_golden("legendre_nside2_lmax8")
+    cg.library()
+    exe = str(tmp_path / "test_legendre_lp")
+    libdir = os.path.join(ROOT, "cosmopp_gb300", "_lib")
+    subprocess.check_call(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+                           os.path.join(ROOT, "tests", "cxx", "test_legendre_lp.cpp"), "-L", libdir,
+                           "-lcosmopp_gb300", "-Wl,-rpath," + libdir, "-o", exe])
+    inp = tmp_path / "in.txt"
+    with open(inp, "w") as f:
+        f.write("%d %d %.17g %d\n" % (int(g["nside"]), int(g["lmax"]), float(g["fwhm_deg"]), len(g["nest_good"])))
+        f.write(" ".join(str(int(v)) for v in g["nest_good"]) + "\n")
+    clf = tmp_path / "cl.txt"
+    with open(clf, "w") as f:
+        f.write("".join("%.17g\n" % v for v in g["cl"]))
+    ref_file = os.path.join(ROOT, "tests", "golden", "legendre_nside2_lmax8.bin")
+    p = subprocess.run([exe, str(inp), ref_file, str(clf), str(tmp_path)], capture_output=True, text=True,
+                       timeout=300)
+    assert p.returncode == 0, p.stderr
+    assert p.stdout.split() == ["0", "refused"]
+    assert open(tmp_path / "lp.bin", "rb").read() == open(ref_file, "rb").read()
+    assert np.array_equal(np.fromfile(tmp_path / "c_lp.bin", dtype=np.float64), g["c_lp"])
+    assert np.array_equal(np.fromfile(tmp_path / "c_file.bin", dtype=np.float64), g["c_plain"])

@@ -2,11 +2,12 @@
 fixtures made by tests/golden/make_golden.py from the reference compiled from
 its sources) and to the reference's known-answer tests."""
 import hashlib
+import os
 
 import numpy as np
 import pytest
 
-from conftest import load_golden
+from conftest import ROOT, load_golden
 from cosmopp_gb300 import workload as W
 
 DET_OFFSET = 29677.0566
@@ -141,3 +142,15 @@ def test_oracle_noise_matrix_matches_an_independent_restatement(oracle_mod):
         for k in range(nsims):
             means += sims[k]
         assert mx == np.abs(means / nsims).max()
+
+
+def test_oracle_legendre_table_matches_reference_file(oracle_mod):
+    """The reference's LegendrePolynomialContainer, written by its own writeIntoFile
+    (tests/golden/legendre_nside2_lmax8.bin), equals the oracle's table bit for bit; the
+    covariance the reference computes from that file read back equals its plain one."""
+    g = load_golden("legendre_nside2_lmax8")
+    lmax, npix, tab = oracle_mod.read_legendre_file(os.path.join(ROOT, "tests", "golden", "legendre_nside2_lmax8.bin"))
+    assert lmax == int(g["lmax"]) and npix == len(g["nest_good"])
+    xyz = oracle_mod.unit_vectors(int(g["nside"]), g["nest_good"], "NEST")
+    assert np.array_equal(oracle_mod.legendre_table(lmax, xyz), tab)
+    assert np.array_equal(g["c_lp"], g["c_plain"])
