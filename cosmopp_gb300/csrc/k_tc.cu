@@ -777,36 +777,58 @@ __device__ void factor_block64(float* s, float* u, int o, int* bad)
 }
 
 // inverse of the lower-triangular 64x64 block at (o, o) of s into the same block of inv (zero above
-// its diagonal): column c = o + t of the inverse by forward substitution in row blocks of 8, one
-// thread per column (t < 64); 1 / L_cc recomputed from the stored diagonal
-__device__ void invert_block64(const float* s, float* inv, int o)
+// its diagonal), blocked by 8: the eight 8x8 diagonal blocks by forward substitution (one thread per
+// column), then the block diagonals d = 1..7 below it in turn, M_IJ = -M_II (sum_{k=J}^{I-1} L_Ik M_kJ)
+// for I - J = d: the sums one thread per element into tmp, a barrier, the products with M_II one
+// thread per element.  All NTH threads take part (every barrier is reached by all).  A forward
+// substitution per column (one thread per column, row blocks in turn) took 2.7 times as long: its
+// 64 threads ran one long dependent chain each.
+__device__ void invert_block64(const float* s, float* inv, float* tmp, int o)
 {
     constexpr int L = 129;
     const int t = threadIdx.x;
-    if (t >= 64) return;
-    const int c = o + t;
-    for (int m = o; m < c; ++m) inv[c * L + m] = 0.f;
-    for (int R = t / 8; R < 8; ++R) {
-        const int r0 = o + 8 * R;
-        float acc[8];
-#pragma unroll
-        for (int i = 0; i < 8; ++i) acc[i] = (r0 + i == c) ? 1.f : 0.f;
-#pragma unroll 2
-        for (int m = c; m < r0; ++m) {
-            const float x = inv[c * L + m];
-#pragma unroll
-            for (int i = 0; i < 8; ++i) acc[i] = fmaf(-s[m * L + r0 + i], x, acc[i]);
-        }
+    for (int e = t; e < 64 * 64; e += NTH) {
+        const int r = e % 64, c = e / 64;
+        if (r < c) inv[(o + c) * L + o + r] = 0.f;
+    }
+    if (t < 64) {
+        const int base = o + 8 * (t / 8), j = t % 8;
         float y[8];
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
-            float v = acc[i];
+            float v = (i == j) ? 1.f : 0.f;
 #pragma unroll
-            for (int k = 0; k < i; ++k) v = fmaf(-s[(r0 + k) * L + r0 + i], y[k], v);
-            y[i] = (r0 + i < c) ? 0.f : v / s[(r0 + i) * L + r0 + i];
+            for (int k = 0; k < i; ++k) v = fmaf(-s[(base + k) * L + base + i], y[k], v);
+            y[i] = (i < j) ? 0.f : v / s[(base + i) * L + base + i];
         }
 #pragma unroll
-        for (int i = 0; i < 8; ++i) inv[c * L + r0 + i] = y[i];
+        for (int i = 0; i < 8; ++i)
+            if (i >= j) inv[(base + j) * L + base + i] = y[i];
+    }
+    __syncthreads();
+    for (int d = 1; d < 8; ++d) {
+        const int nel = 64 * (8 - d);  // blocks (J + d, J), J < 8 - d: element e = 64 J + 8 j + r
+        for (int e = t; e < nel; e += NTH) {
+            const int J = e / 64, I = J + d, r = e % 8, j = (e / 8) % 8;
+            const int c = o + 8 * J + j, row = o + 8 * I + r;
+            float acc = 0.f;
+            for (int kb = o + 8 * J; kb < o + 8 * I; kb += 8) {
+#pragma unroll
+                for (int k = 0; k < 8; ++k) acc = fmaf(s[(kb + k) * L + row], inv[c * L + kb + k], acc);
+            }
+            tmp[e] = acc;
+        }
+        __syncthreads();
+        for (int e = t; e < nel; e += NTH) {
+            const int J = e / 64, I = J + d, r = e % 8, j = (e / 8) % 8;
+            const int c = o + 8 * J + j, rb = o + 8 * I;
+            float acc = 0.f;
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (q <= r) acc = fmaf(inv[(rb + q) * L + rb + r], tmp[64 * J + 8 * j + q], acc);
+            inv[c * L + rb + r] = -acc;
+        }
+        __syncthreads();
     }
 }
 
@@ -823,7 +845,7 @@ __device__ void factor_block128(float* s, float* inv, float* tmp, int* bad)
     const int t = threadIdx.x;
     const int i0 = 4 * (t % 16), j0 = 4 * ((t / 16) % 16);  // this thread's 4x4 outputs of a 64x64 product
     factor_block64(s, inv, 0, bad);
-    invert_block64(s, inv, 0);
+    invert_block64(s, inv, tmp, 0);
     for (int e = t; e < 64 * 64; e += NTH) inv[(64 + e / 64) * L + e % 64] = 0.f;  // upper-right block
     __syncthreads();
     // L21 = S21 L11^-T: L21[i][j] = sum_{k <= j} S21[i][k] L11^-1[j][k]
@@ -879,7 +901,7 @@ __device__ void factor_block128(float* s, float* inv, float* tmp, int* bad)
     }
     __syncthreads();
     factor_block64(s, inv, 64, bad);
-    invert_block64(s, inv, 64);
+    invert_block64(s, inv, tmp, 64);
     __syncthreads();
     // T = L21 L11^-1 into tmp (tmp[j * 65 + i] = T[i][j]); L11^-1[k][j] = 0 for k < j
     if (t < 256) {
