@@ -701,11 +701,12 @@ __device__ __forceinline__ void store_block(const float (&R)[64], float* base, i
 // part), in place.  The updates from factorised panels are summed in u (the same positions of u's
 // storage) and subtracted from a column once, when its panel is reached: subtracting each term
 // from s directly drops the terms below half an ulp of the diagonal (about 1 after whitening) and
-// biases the log-determinant upwards.  Panels of 8 columns: every thread factors the panel's 8x8
-// diagonal block itself (same operands and operation order in every thread, so the same values) and
-// then its own row's 8 values, so a panel needs no barrier until its columns are written; the
-// trailing sums are then updated four threads per row.  All NTH threads take part (every barrier is
-// reached by all).  Sets *bad on a non-positive pivot.
+// biases the log-determinant upwards.  Panels of 8 columns: each of the 64 threads that own the
+// block's rows factors the panel's 8x8 diagonal block itself (same operands and operation order in
+// every thread, so the same values) and then its own row's 8 values, so a panel needs no barrier
+// until its columns are written; the trailing sums are then updated four threads per row, from the
+// written columns.  All NTH threads take part (every barrier is reached by all).  Sets *bad on a
+// non-positive pivot.
 __device__ void factor_block64(float* s, float* u, int o, int* bad)
 {
     constexpr int L = 129;
@@ -715,7 +716,12 @@ __device__ void factor_block64(float* s, float* u, int o, int* bad)
     const int r = o + t % 64, part = t / 64;  // parts 0-3 share the row's trailing sums; t >= 256 idle
     for (int kb = o; kb < o + 64; kb += 8) {
         float lb[8][8], rv[8], lr[8];
-        // the panel's 8x8 diagonal block, in every thread
+        // the panel's 8x8 diagonal block, in the two warps that own the panel's rows (t < 64;
+        // the same operands and operation order in every thread, so the same values); a
+        // non-positive pivot is recorded in a register and stored after the loop, so no store
+        // to shared memory holds back the block's loads
+        if (t < 64) {
+        bool notpd = false;
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
 #pragma unroll
@@ -729,7 +735,7 @@ __device__ void factor_block64(float* s, float* u, int o, int* bad)
                 } else {
                     float v = a - acc;
                     if (!(v > 0.f)) {  // not positive definite (or NaN): flag, go on with a benign pivot
-                        if (t == 0) *bad = 1;
+                        notpd = true;
                         v = 1.f;
                     }
                     lb[i][i] = sqrtf(v);
@@ -756,6 +762,8 @@ __device__ void factor_block64(float* s, float* u, int o, int* bad)
                     for (int j = 0; j <= i; ++j) lr[j] = lb[i][j];
                 }
         }
+        if (notpd && t == 0) *bad = 1;
+        }
         __syncthreads();  // every read of the panel's columns is done
         if (t < 64) {
 #pragma unroll
@@ -763,9 +771,29 @@ __device__ void factor_block64(float* s, float* u, int o, int* bad)
                 if (r >= kb + j) s[(kb + j) * L + r] = lr[j];
         }
         __syncthreads();
-        // u[q][r] += sum_j L[r][kb+j] L[q][kb+j] for kb + 8 <= q <= r; q = kb + 8 + part (mod 4)
+        // u[q][r] += sum_j L[r][kb+j] L[q][kb+j] for kb + 8 <= q <= r; q = kb + 8 + part (mod 4),
+        // two q at a time so that their loads and sums overlap (each entry's sum in the same order);
+        // the row's panel values come back from shared memory
         if (t < 256 && r >= kb + 8) {
-            for (int q = kb + 8 + part; q <= r; q += 4) {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) lr[j] = s[(kb + j) * L + r];
+            int q = kb + 8 + part;
+            for (; q + 4 <= r; q += 8) {
+                float a0 = u[q * L + r], a1 = u[(q + 4) * L + r], x0[8], x1[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    x0[j] = s[(kb + j) * L + q];
+                    x1[j] = s[(kb + j) * L + q + 4];
+                }
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    a0 = fmaf(lr[j], x0[j], a0);
+                    a1 = fmaf(lr[j], x1[j], a1);
+                }
+                u[q * L + r] = a0;
+                u[(q + 4) * L + r] = a1;
+            }
+            if (q <= r) {
                 float acc = u[q * L + r];
 #pragma unroll
                 for (int j = 0; j < 8; ++j) acc = fmaf(lr[j], s[(kb + j) * L + q], acc);
