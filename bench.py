@@ -55,6 +55,27 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(x, world, device=None):
+    """The largest of every rank's x: the job's time is its slowest rank's (all ranks call it)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(batch_per_rank, world, ms_per_step):
+    """Evaluations/s of the whole job: every rank evaluates its own batch each step (replicas)."""
+    return batch_per_rank * world / (ms_per_step / 1000.0)
+
+
+def rank_batch_seed(rank):
+    """Seed of a rank's C_l batch: each replica evaluates different vectors."""
+    return 7 + rank
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 200 ms during the timed region."""
 
@@ -196,7 +217,7 @@ def run_ours(args):
     torch.cuda.set_device(local)
     import cosmopp_gb300 as cg
     from cosmopp_gb300 import workload as W
-    wl = W.make(args.workload, batch=args.batch, batch_seed=7 + rank)
+    wl = W.make(args.workload, batch=args.batch, batch_seed=rank_batch_seed(rank))
     B = len(wl.cl_batch)
     d = make_inputs(wl, cg)
     path = args.path
@@ -244,11 +265,8 @@ def run_ours(args):
     ms = e0.elapsed_time(e1) / args.steps
     launches = (ctx.launch_count() - launches0) // args.steps
     clk = clocks.stop()
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = B * world / (ms / 1000.0)
+    ms = max_over_ranks(ms, world, dev)
+    value = job_throughput(B, world, ms)
     assert int(st.sum().item()) == 0, "non-OK element status in the timed batch"
 
     # end to end through the host-pointer C ABI from pinned buffers
@@ -276,10 +294,7 @@ def run_ours(args):
     for k in range(args.steps):
         e2e_step(k)
     e2e_ms = (time.perf_counter() - t0) * 1000.0 / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e2e_ms, world, dev)
     h2d = B * L1 * 8 + wl.n * 8
     d2h = B * (3 * 8 + L1 * 8 + 4)
 
@@ -337,7 +352,7 @@ def run_ours(args):
                       "l2": "per-step working set %.1f GB > 129 MB L2" % (B * 3 * (N * N / 2) * 4 / 1e9),
                       "parallelism": "replicas x%d" % world},
            "clocks": clk, "gpu_launches": int(launches),
-           "e2e": {"value": B * world / (e2e_ms / 1000.0), "unit": "evals/s", "ms_per_step": e2e_ms,
+           "e2e": {"value": job_throughput(B, world, e2e_ms), "unit": "evals/s", "ms_per_step": e2e_ms,
                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
            "stages_ms": {k: round(v, 4) for k, v in stages.items() if k != "end"},
            "roofline": roof}
