@@ -119,6 +119,37 @@ public:
         out.write((const char*)&len, sizeof(int));
         if (len) out.write(comment_.data(), len);
     }
+    /// text format of source/c_matrix.cpp:87-107: nPix, the comment, then "i<TAB>j<TAB>value" for
+    /// i <= j, column by column, at the stream's default precision
+    void writeIntoTextFile(const char* fileName) const
+    {
+        std::ofstream out(fileName);
+        if (!out) cosmopp_gb300_detail::raise(std::string("Cannot write into output file ") + fileName + ".");
+        out << nPix_ << std::endl;
+        out << comment_ << std::endl;
+        for (int j = 0; j < nPix_; ++j)
+            for (int i = 0; i <= j; ++i) out << i << '\t' << j << '\t' << element(i, j) << std::endl;
+    }
+    /// reads what writeIntoTextFile writes (source/c_matrix.cpp:109-154 takes the same layout; it
+    /// reads one whitespace-separated token per entry, so here the i, j, value triples are read
+    /// as written); an index outside the matrix raises, as there
+    void readFromTextFile(const char* fileName)
+    {
+        std::ifstream in(fileName);
+        if (!in) cosmopp_gb300_detail::raise(std::string("Cannot read the input file ") + fileName + ".");
+        in >> nPix_;
+        initialize();
+        std::string rest;
+        std::getline(in, rest);
+        std::getline(in, comment_);
+        int i, j;
+        double val;
+        while (in >> i >> j >> val) {
+            if (i < 0 || i >= nPix_) cosmopp_gb300_detail::raise("Invalid index i = " + std::to_string(i) + ".");
+            if (j < 0 || j >= nPix_) cosmopp_gb300_detail::raise("Invalid index j = " + std::to_string(j) + ".");
+            element(i, j) = val;
+        }
+    }
     /// source/c_matrix.cpp:183-201
     void maskMatrix(const std::vector<int>& goodPixels)
     {

@@ -135,6 +135,35 @@ extern "C" int ref_cl_to_cmatrix_lp_file(const double* cl, int lmax, long nside,
     } catch (std::exception& e) { g_err = e.what(); return 1; }
 }
 
+/* clToCMatrix's matrix with a comment, written by CMatrix's own writeIntoFile and
+   writeIntoTextFile (source/c_matrix.cpp:67-107) */
+extern "C" int ref_cmatrix_write_files(const double* cl, int lmax, long nside, double fwhm_deg, const int* good_nest,
+                                       int n, const char* comment, const char* bin_path, const char* txt_path)
+{
+    try {
+        std::vector<double> c(cl, cl + lmax + 1);
+        std::vector<int> good(good_nest, good_nest + n);
+        CMatrix* m = CMatrixGenerator::clToCMatrix(c, nside, fwhm_deg, &good);
+        m->comment() = comment;
+        m->writeIntoFile(bin_path);
+        m->writeIntoTextFile(txt_path);
+        delete m;
+        return 0;
+    } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
+/* Utils::readClFromFile (source/utils.cpp:173-217): up to max values into out, count returned */
+extern "C" int ref_read_cl(const char* path, int has_l, int is_dl, double* out, int max)
+{
+    try {
+        std::vector<double> cl;
+        Utils::readClFromFile(path, cl, has_l != 0, is_dl != 0);
+        const int k = (int)cl.size() < max ? (int)cl.size() : max;
+        for (int i = 0; i < k; ++i) out[i] = cl[i];
+        return (int)cl.size();
+    } catch (std::exception& e) { g_err = e.what(); return -1; }
+}
+
 /* Utils::beamFunction (source/utils.cpp:54-64) and the pixel-window reader
    with the unit window the shim serves (source/utils.cpp:66-170). */
 extern "C" double ref_beam(int l, double fwhm_deg) { return Utils::beamFunction(l, fwhm_deg); }

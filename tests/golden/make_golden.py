@@ -18,10 +18,12 @@ them through ctypes.  Every number stored below comes from the reference:
   source/test_like_low.cpp:181-193 that uses it;
 * a LegendrePolynomialContainer table file written by the reference's own
   writeIntoFile, and the clToCMatrix covariance computed from that file read
-  back by the reference's file constructor.
+  back by the reference's file constructor;
+* CMatrix binary and text files written by the reference's CMatrix, and what
+  its Utils::readClFromFile reads from two C_l text files.
 
 Usage:  python tests/golden/make_golden.py [part ...]   (parts: main, fiducial,
-legendre; default all)
+legendre, files; default all)
 """
 import ctypes
 import hashlib
@@ -124,6 +126,38 @@ def legendre_cases(R):
     print(name, "n", n, "bytes", os.path.getsize(path))
 
 
+def file_cases(R):
+    """CMatrix binary and text files written by the reference's CMatrix, and C_l text files
+    (plain C_l; l-prefixed D_l) with what the reference's Utils::readClFromFile reads from them."""
+    name, nside, lmax, fwhm_am, keep = LEGENDRE_CASE
+    fwhm = fwhm_am / 60.0
+    ring = W.bernoulli_mask(nside, keep, 1234)
+    nest = O.ring2nest(nside, ring)
+    n = len(nest)
+    cl = W.fiducial_cl(lmax)
+    binp, txtp = os.path.join(HERE, "cmatrix_nside2.bin"), os.path.join(HERE, "cmatrix_nside2.txt")
+    rc = R.ref_cmatrix_write_files(cl.ctypes.data_as(dp), lmax, nside, fwhm, nest.ctypes.data_as(ip), n,
+                                   b"covariance from the reference", binp.encode(), txtp.encode())
+    assert rc == 0, R.ref_last_error()
+    plain = os.path.join(HERE, "cl_plain.txt")
+    with open(plain, "w") as f:
+        f.write("".join("%.17g\n" % v for v in cl))
+    ells = np.arange(lmax + 1)
+    dl = np.where(ells > 0, cl * ells * (ells + 1) / (2 * np.pi), 0.0)
+    withl = os.path.join(HERE, "dl_with_l.txt")
+    with open(withl, "w") as f:
+        f.write("".join("%d %.17g\n" % (l, v) for l, v in zip(ells, dl)))
+    out = {}
+    for key, path, has_l, is_dl in (("read_plain", plain, 0, 0), ("read_dl", withl, 1, 1)):
+        buf = np.zeros(4096)
+        k = R.ref_read_cl(path.encode(), has_l, is_dl, buf.ctypes.data_as(dp), len(buf))
+        assert k > 0, R.ref_last_error()
+        out[key] = buf[:k].copy()
+    np.savez_compressed(os.path.join(HERE, "files_nside2.npz"), nest_good=nest, nside=nside, lmax=lmax,
+                        fwhm_deg=fwhm, c_packed=ref_cmatrix(R, cl, nside, fwhm, nest), **out)
+    print("files_nside2 n", n)
+
+
 def ref_cmatrix(R, cl, nside, fwhm, nest):
     n = len(nest)
     out = np.zeros(n * (n + 1) // 2)
@@ -148,8 +182,13 @@ def main(parts):
     R.ref_legendre_table_write.argtypes = [ctypes.c_int, ctypes.c_long, ip, ctypes.c_int, ctypes.c_char_p]
     R.ref_cl_to_cmatrix_lp_file.argtypes = [dp, ctypes.c_int, ctypes.c_long, ctypes.c_double, ip, ctypes.c_int,
                                             ctypes.c_char_p, dp]
+    R.ref_cmatrix_write_files.argtypes = [dp, ctypes.c_int, ctypes.c_long, ctypes.c_double, ip, ctypes.c_int,
+                                          ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]
+    R.ref_read_cl.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, dp, ctypes.c_int]
     if "legendre" in parts:
         legendre_cases(R)
+    if "files" in parts:
+        file_cases(R)
     if "main" not in parts:
         if "fiducial" in parts:
             fiducial_cases(R)
@@ -206,4 +245,4 @@ def main(parts):
 
 
 if __name__ == "__main__":
-    main(set(sys.argv[1:]) or {"main", "fiducial", "legendre"})
+    main(set(sys.argv[1:]) or {"main", "fiducial", "legendre", "files"})
