@@ -22,13 +22,16 @@ import os
 import numpy as np
 
 __all__ = ["Context", "Likelihood", "LikelihoodWithDerivs", "CGError", "library", "DET_OFFSET",
-           "ring2nest", "nest2ring", "pix2vec", "beam", "mh_sample", "LegendrePolynomialContainer"]
+           "ring2nest", "nest2ring", "pix2vec", "beam", "mh_sample", "LegendrePolynomialContainer",
+           "LikelihoodPolarization"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "libcosmopp_gb300.so")
 
 # source/likelihood.cpp:127-128: the reference subtracts detOffset = -29677.0566 from ln det C
 DET_OFFSET = 29677.0566
+# source/likelihood.cpp:400-401: LikelihoodPolarization subtracts detOffset = 16078.083180
+DET_OFFSET_POL = 16078.083180
 
 CG_OK, CG_ERR_BAD_ARG, CG_ERR_NOT_PD, CG_ERR_NONFINITE, CG_ERR_TIMEOUT, CG_ERR_CUDA, CG_ERR_NO_DEVICE, \
     CG_ERR_ALLOC = range(8)
@@ -105,6 +108,9 @@ def library():
     L.cg_stage_times.argtypes = [ctypes.c_void_p, _dp]
     L.cg_likelihood_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_int]
     L.cg_likelihood_calculate.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+    L.cg_likelihood_pol_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _ip, ctypes.c_int, _dp, _dp,
+                                           ctypes.c_int]
+    L.cg_likelihood_pol_calculate.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp]
     L.cg_likelihood_logdet.restype = ctypes.c_double
     L.cg_likelihood_logdet.argtypes = [ctypes.c_void_p]
     L.cg_likelihood_destroy.argtypes = [ctypes.c_void_p]
@@ -499,6 +505,57 @@ class Likelihood:
         if rc:
             raise CGError(rc, self._L.cg_likelihood_last_error(self._h).decode())
         logdet = ld.value - (-DET_OFFSET)  # logDet_ -= detOffset (source/likelihood.cpp:127-128)
+        return chi2.value + logdet, chi2.value, logdet
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.cg_likelihood_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class LikelihoodPolarization:
+    """The pixel-space part of the reference's LikelihoodPolarization
+    (source/likelihood.cpp:341-401,536-612): ``c_packed`` is the packed Q-then-U covariance of
+    all 2 npix pixels, ``ninv`` the dense (2 npix)^2 inverse noise matrix (the contents of the
+    reference's n_inv.txt), ``good_pixels`` the kept pixels.  ``calculate(v, subtract)`` takes
+    v = N^-1 (Q, U) at the kept pixels and the T-correlated Q, U template at the kept pixels
+    (which the reference forms from the TT a_lm by alm2map_pol) and returns (like, chi2, logdet)
+    with the reference's detOffset applied."""
+
+    def __init__(self, c_packed, npix, good_pixels, ninv, device=0):
+        L = library()
+        c = _f64(c_packed)
+        size = 2 * int(npix)
+        if len(c) != size * (size + 1) // 2:
+            raise CGError(CG_ERR_BAD_ARG, "polarization c matrix includes q and u parts: %d pixels expected" % size)
+        nv = _f64(ninv)
+        if nv.size != size * size:
+            raise CGError(CG_ERR_BAD_ARG, "the inverse noise matrix must be %d x %d" % (size, size))
+        good = np.ascontiguousarray(good_pixels, dtype=np.int32)
+        h = ctypes.c_void_p()
+        rc = L.cg_likelihood_pol_create(ctypes.byref(h), int(npix), good.ctypes.data_as(_ip), len(good), _p(c),
+                                        _p(nv), int(device))
+        if rc:
+            raise CGError(rc, L.cg_likelihood_last_error(None).decode())
+        self._h, self._L, self.n = h, L, 2 * len(good)
+        self.logdet_raw = L.cg_likelihood_logdet(h)
+
+    def calculate(self, v, subtract):
+        chi2 = ctypes.c_double()
+        ld = ctypes.c_double()
+        v, sub = _f64(v), _f64(subtract)
+        if len(v) != self.n or len(sub) != self.n:
+            raise CGError(CG_ERR_BAD_ARG, "v and subtract need 2 x (kept pixels) = %d values" % self.n)
+        rc = self._L.cg_likelihood_pol_calculate(self._h, _p(v), _p(sub), ctypes.byref(chi2), ctypes.byref(ld))
+        if rc:
+            raise CGError(rc, self._L.cg_likelihood_last_error(self._h).decode())
+        logdet = ld.value - DET_OFFSET_POL
         return chi2.value + logdet, chi2.value, logdet
 
     def close(self):

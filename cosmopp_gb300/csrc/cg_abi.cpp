@@ -462,6 +462,8 @@ struct cg_lik {
     int* st = nullptr;
     double logdet = 0;
     std::vector<double> fg;
+    double* Ninv = nullptr;      // polarisation likelihood: dense N^-1 (ld x ld, column-major)
+    int ld = 0;
 };
 
 extern "C" void cg_likelihood_destroy(cg_lik* lik)
@@ -470,6 +472,7 @@ extern "C" void cg_likelihood_destroy(cg_lik* lik)
     cudaSetDevice(lik->ctx.device);
     if (lik->ctx.stream) cudaStreamSynchronize(lik->ctx.stream);
     cudaFree(lik->A); cudaFree(lik->M); cudaFree(lik->Dinv); cudaFree(lik->diag); cudaFree(lik->tmp); cudaFree(lik->st);
+    cudaFree(lik->Ninv);
     if (lik->ctx.stream) cudaStreamDestroy(lik->ctx.stream);
     delete lik;
 }
@@ -546,22 +549,17 @@ extern "C" int cg_likelihood_create(cg_lik** out, int n, const double* c_packed,
     return CG_OK;
 }
 
-extern "C" int cg_likelihood_calculate(cg_lik* lik, const double* t, double* chi2, double* logdet)
+// chi2 (and the foreground terms) for the padded vector already in lik->tmp[0 .. N)
+static int lik_finish(cg_lik* lik, double* chi2, double* logdet)
 {
-    if (!lik || !t || !chi2 || !logdet) return CG_ERR_BAD_ARG;
     cg_ctx& ctx = lik->ctx;
     const int n = ctx.n, N = ctx.N;
-    for (int i = 0; i < n; ++i)
-        if (!std::isfinite(t[i])) { ctx.err = "non-finite map value"; return CG_ERR_NONFINITE; }
-    CG_CUDA_TRY(&ctx, cudaSetDevice(ctx.device));
     cudaStream_t s = ctx.stream;
     double* tv = lik->tmp;          // padded t
     double* ta = tv + N;            // C^-1 t
     double* fv = ta + N;            // padded f
     double* fa = fv + N;            // C^-1 f
     double* sc = fa + N;            // scalars
-    cudaMemsetAsync(tv, 0, sizeof(double) * 4 * N, s);
-    cudaMemcpyAsync(tv, t, sizeof(double) * n, cudaMemcpyHostToDevice, s);
     cg::fp64_symv(1, ctx.nt, N, lik->A, tv, ta, s);
     cg::fp64_dot(n, tv, ta, sc + 1, s);  // chi2 = t^T C^-1 t (Likelihood::vmv, source/likelihood.cpp:137-152)
     const bool fgm = !lik->fg.empty();
@@ -583,6 +581,113 @@ extern "C" int cg_likelihood_calculate(cg_lik* lik, const double* t, double* chi
         *chi2 -= tCinvf * tCinvf / fCinvf;
     }
     return CG_OK;
+}
+
+extern "C" int cg_likelihood_calculate(cg_lik* lik, const double* t, double* chi2, double* logdet)
+{
+    if (!lik || !t || !chi2 || !logdet) return CG_ERR_BAD_ARG;
+    cg_ctx& ctx = lik->ctx;
+    const int n = ctx.n, N = ctx.N;
+    if (lik->Ninv) { ctx.err = "a polarisation likelihood takes cg_likelihood_pol_calculate"; return CG_ERR_BAD_ARG; }
+    for (int i = 0; i < n; ++i)
+        if (!std::isfinite(t[i])) { ctx.err = "non-finite map value"; return CG_ERR_NONFINITE; }
+    CG_CUDA_TRY(&ctx, cudaSetDevice(ctx.device));
+    cudaStream_t s = ctx.stream;
+    cudaMemsetAsync(lik->tmp, 0, sizeof(double) * 4 * N, s);
+    cudaMemcpyAsync(lik->tmp, t, sizeof(double) * n, cudaMemcpyHostToDevice, s);
+    return lik_finish(lik, chi2, logdet);
+}
+
+extern "C" int cg_likelihood_pol_create(cg_lik** out, int npix, const int* good, int ngood, const double* c_packed,
+                                        const double* ninv, int device)
+{
+    g_create_error.clear();
+    if (!out || npix <= 0 || !good || ngood <= 0 || ngood > npix || !c_packed || !ninv) {
+        g_create_error = "bad arguments to cg_likelihood_pol_create";
+        return CG_ERR_BAD_ARG;
+    }
+    *out = nullptr;
+    for (int i = 0; i < ngood; ++i)
+        if (good[i] < 0 || good[i] >= npix) { g_create_error = "good pixel index out of range"; return CG_ERR_BAD_ARG; }
+    // source/likelihood.cpp:371-384: the Q and U rows and columns of the kept pixels
+    const int n = 2 * ngood, size = 2 * npix, ld = (n + 63) / 64 * 64;
+    auto full = [&](int k) { return k < ngood ? good[k] : npix + good[k - ngood]; };
+    const size_t np = (size_t)n * (n + 1) / 2;
+    std::vector<double> cg_packed(np), nd((size_t)ld * ld, 0.0);
+    for (int j = 0; j < n; ++j) {
+        const long fj = full(j);
+        for (int i = 0; i <= j; ++i) {
+            const long fi = full(i), a = std::min(fi, fj), b = std::max(fi, fj);
+            cg_packed[(size_t)j * (j + 1) / 2 + i] = c_packed[(size_t)b * (b + 1) / 2 + a];
+        }
+        for (int i = 0; i < n; ++i) nd[(size_t)j * ld + i] = ninv[(size_t)full(i) * size + fj];
+    }
+    for (double v : cg_packed)
+        if (!std::isfinite(v)) { g_create_error = "non-finite matrix entry"; return CG_ERR_NONFINITE; }
+    for (double v : nd)
+        if (!std::isfinite(v)) { g_create_error = "non-finite matrix entry"; return CG_ERR_NONFINITE; }
+    cg_ctx tmpctx;
+    std::string why;
+    if (!device_ok(device, &tmpctx.sm_count, why)) { g_create_error = why; return CG_ERR_NO_DEVICE; }
+    tmpctx.device = device;
+    cudaSetDevice(device);
+    cudaStream_t s = nullptr;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) { g_create_error = "stream"; return CG_ERR_CUDA; }
+    const size_t nel = (size_t)ld * ld;
+    double *d_c = nullptr, *d_n = nullptr, *d_cd = nullptr, *d_t = nullptr, *d_m = nullptr, *d_mp = nullptr;
+    int rc = CG_OK;
+    if (!dalloc(&d_c, np) || !dalloc(&d_n, nel) || !dalloc(&d_cd, nel) || !dalloc(&d_t, nel) || !dalloc(&d_m, nel) ||
+        !dalloc(&d_mp, np)) {
+        g_create_error = "device allocation failed";
+        rc = CG_ERR_ALLOC;
+    }
+    std::vector<double> m_packed(np), zero(np, 0.0);
+    if (rc == CG_OK) {
+        cudaMemcpyAsync(d_c, cg_packed.data(), sizeof(double) * np, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(d_n, nd.data(), sizeof(double) * nel, cudaMemcpyHostToDevice, s);
+        // source/likelihood.cpp:386-387: cInv = N^-1 + N^-1 C N^-1
+        rc = cg::fp64_pol_matrix(&tmpctx, n, ld, d_c, d_n, d_cd, d_t, d_m, d_mp, s);
+        if (rc == CG_OK) {
+            cudaMemcpyAsync(m_packed.data(), d_mp, sizeof(double) * np, cudaMemcpyDeviceToHost, s);
+            if (cudaStreamSynchronize(s) != cudaSuccess) { g_create_error = "polarisation matrix build failed"; rc = CG_ERR_CUDA; }
+        } else {
+            g_create_error = tmpctx.err;
+        }
+    }
+    cudaFree(d_c); cudaFree(d_cd); cudaFree(d_t); cudaFree(d_m); cudaFree(d_mp);
+    cudaStreamDestroy(s);
+    if (rc == CG_OK) rc = cg_likelihood_create(out, n, m_packed.data(), nullptr, zero.data(), nullptr, device);
+    if (rc != CG_OK) {
+        cudaFree(d_n);
+        return rc;
+    }
+    (*out)->Ninv = d_n;
+    (*out)->ld = ld;
+    return CG_OK;
+}
+
+extern "C" int cg_likelihood_pol_calculate(cg_lik* lik, const double* v, const double* subtract, double* chi2,
+                                           double* logdet)
+{
+    if (!lik || !v || !subtract || !chi2 || !logdet) return CG_ERR_BAD_ARG;
+    cg_ctx& ctx = lik->ctx;
+    if (!lik->Ninv) { ctx.err = "not a polarisation likelihood"; return CG_ERR_BAD_ARG; }
+    const int n = ctx.n, N = ctx.N;
+    for (int i = 0; i < n; ++i)
+        if (!std::isfinite(v[i]) || !std::isfinite(subtract[i])) { ctx.err = "non-finite map value"; return CG_ERR_NONFINITE; }
+    CG_CUDA_TRY(&ctx, cudaSetDevice(ctx.device));
+    cudaStream_t s = ctx.stream;
+    double* w = lik->tmp;           // padded w = v - N^-1 s
+    double* vv = w + N;             // v, then s, in the C^-1 slots that lik_finish overwrites
+    double* sv = vv + N;
+    cudaMemsetAsync(lik->tmp, 0, sizeof(double) * 4 * N, s);
+    cudaMemcpyAsync(vv, v, sizeof(double) * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(sv, subtract, sizeof(double) * n, cudaMemcpyHostToDevice, s);
+    // source/likelihood.cpp:595-600: vCopy -= N^-1 subtractMap
+    int rc = cg::fp64_dense_residual(&ctx, n, lik->ld, lik->Ninv, vv, sv, w, s);
+    if (rc) return rc;
+    cudaMemsetAsync(vv, 0, sizeof(double) * 2 * N, s);
+    return lik_finish(lik, chi2, logdet);   // chi2 = w^T cInv w (source/likelihood.cpp:602-609)
 }
 
 extern "C" int cg_selftest_wait_timeout(cg_ctx* ctx, int* status)

@@ -163,6 +163,13 @@ int fp64_ensure(cg_ctx* ctx, int B);
 int fp64_build_tiled(cg_ctx* ctx, int B, const double* d_cl, bool add_noise, cudaStream_t s);
 int fp64_build_tiled_into(cg_ctx* ctx, int B, const double* d_cl, bool add_noise, double* A, cudaStream_t s);
 int fp64_build_packed(cg_ctx* ctx, int B, const double* d_cl, double* d_out, cudaStream_t s);
+// polarisation likelihood set-up: M = N^-1 + N^-1 C N^-1 for packed C and dense N^-1 (ld x ld,
+// column-major, zero padded), packed into d_m_packed; d_cd, d_t, d_m are ld x ld scratch
+int fp64_pol_matrix(cg_ctx* ctx, int n, int ld, const double* d_c_packed, const double* d_ninv, double* d_cd,
+                    double* d_t, double* d_m, double* d_m_packed, cudaStream_t s);
+// w = v - N^-1 s for the dense N^-1 above
+int fp64_dense_residual(cg_ctx* ctx, int n, int ld, const double* d_ninv, const double* d_v, const double* d_s,
+                        double* d_w, cudaStream_t s);
 // P_l(x_ij) for l0 <= l < l1 into d_out [(l1 - l0)][n(n+1)/2]; d_a, d_b = the recurrence
 // coefficients, at least l1 entries each (device pointers)
 int fp64_legendre_table(cg_ctx* ctx, int l0, int l1, const double* d_a, const double* d_b, double* d_out,

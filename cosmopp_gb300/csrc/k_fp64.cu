@@ -412,6 +412,87 @@ __global__ void dot_kernel(int n, const double* __restrict__ a, const double* __
     if (threadIdx.x == 0) *out = red[0];
 }
 
+// Dense FP64 helpers of the polarisation likelihood's set-up (column-major, leading dimension
+// ld, a multiple of 64, zero padding beyond n).
+// out = add + A B: one 64 x 64 output tile per CTA, 16-deep K slices of A and B in shared memory,
+// 4 x 4 outputs per thread at rows tx + 16 p and columns ty + 16 q
+__global__ void __launch_bounds__(kThreads) dense_gemm64(int ld, const double* __restrict__ A,
+                                                         const double* __restrict__ Bm,
+                                                         const double* __restrict__ add, double* __restrict__ out)
+{
+    __shared__ double As[16][65], Bs[16][65];
+    const int bi = blockIdx.x * 64, bj = blockIdx.y * 64;
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    double acc[4][4];
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[p][q] = 0.0;
+    for (int k0 = 0; k0 < ld; k0 += 16) {
+        for (int e = threadIdx.x; e < 1024; e += kThreads) {
+            const int r = e % 64, kk = e / 64;
+            As[kk][r] = A[(size_t)(k0 + kk) * ld + bi + r];
+            const int kb = e % 16, c = e / 16;
+            Bs[kb][c] = Bm[(size_t)(bj + c) * ld + k0 + kb];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < 16; ++kk) {
+            double a[4], b[4];
+#pragma unroll
+            for (int p = 0; p < 4; ++p) a[p] = As[kk][tx + 16 * p];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) b[q] = Bs[kk][ty + 16 * q];
+#pragma unroll
+            for (int p = 0; p < 4; ++p)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[p][q] = fma(a[p], b[q], acc[p][q]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            const size_t o = (size_t)(bj + ty + 16 * q) * ld + bi + tx + 16 * p;
+            out[o] = (add ? add[o] : 0.0) + acc[p][q];
+        }
+}
+
+// packed symmetric (i <= j at j(j+1)/2 + i) to dense, zero outside n x n; grid covers ld x ld
+__global__ void packed_to_dense(int n, int ld, const double* __restrict__ pk, double* __restrict__ d)
+{
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)ld * ld) return;
+    const int r = (int)(e % ld), c = (int)(e / ld);
+    const int i = min(r, c), j = max(r, c);
+    d[e] = (j < n) ? pk[(size_t)j * (j + 1) / 2 + i] : 0.0;
+}
+
+// the upper triangle of a dense symmetric matrix, packed
+__global__ void dense_to_packed(int n, int ld, const double* __restrict__ d, double* __restrict__ pk)
+{
+    const long np = (long)n * (n + 1) / 2;
+    const long k = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= np) return;
+    long j = (long)((sqrt(8.0 * (double)k + 1.0) - 1.0) * 0.5);
+    while (j * (j + 1) / 2 > k) --j;
+    while ((j + 1) * (j + 2) / 2 <= k) ++j;
+    const long i = k - j * (j + 1) / 2;
+    pk[k] = d[(size_t)j * ld + i];
+}
+
+// w = v - N s for a dense symmetric N (row i read as column i, coalesced over i)
+__global__ void dense_residual(int n, int ld, const double* __restrict__ Nm, const double* __restrict__ v,
+                               const double* __restrict__ sv, double* __restrict__ w)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double acc = 0.0;
+    for (int j = 0; j < n; ++j) acc = fma(Nm[(size_t)j * ld + i], sv[j], acc);
+    w[i] = v[i] - acc;
+}
+
 // LegendrePolynomialContainer's table (source/c_matrix_generator.cpp:30-76): P_l(x_ij) for
 // l0 <= l < l1 at out[(l - l0) np + j(j+1)/2 + i], i <= j, by Math::Legendre's recurrence
 // (include/legendre.hpp:26-37: P_0 = 1, P_1 = x, P_l = ((2 - 1/l) x) P_{l-1} - (1 - 1/l) P_{l-2},
@@ -604,6 +685,30 @@ int fp64_build_fiducial(cg_ctx* ctx, int lo, int hi, const double* d_tab, double
         CG_CUDA_TRY(ctx, cudaFuncSetAttribute(build_fid_packed, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     build_fid_packed<<<(unsigned)((np + 4 * kThreads - 1) / (4 * kThreads)), kThreads, smem, s>>>(
         ctx->n, ctx->N, lo, hi, ctx->d_xyz, d_tab, m0, d_out);
+    count_launch(ctx);
+    CG_CUDA_TRY(ctx, cudaGetLastError());
+    return CG_OK;
+}
+
+int fp64_pol_matrix(cg_ctx* ctx, int n, int ld, const double* d_c_packed, const double* d_ninv, double* d_cd,
+                    double* d_t, double* d_m, double* d_m_packed, cudaStream_t s)
+{
+    const size_t nel = (size_t)ld * ld;
+    packed_to_dense<<<(unsigned)((nel + kThreads - 1) / kThreads), kThreads, 0, s>>>(n, ld, d_c_packed, d_cd);
+    const dim3 grid(ld / 64, ld / 64);
+    dense_gemm64<<<grid, kThreads, 0, s>>>(ld, d_cd, d_ninv, nullptr, d_t);   // T = C N^-1
+    dense_gemm64<<<grid, kThreads, 0, s>>>(ld, d_ninv, d_t, d_ninv, d_m);     // M = N^-1 + N^-1 T
+    const long np = (long)n * (n + 1) / 2;
+    dense_to_packed<<<(unsigned)((np + kThreads - 1) / kThreads), kThreads, 0, s>>>(n, ld, d_m, d_m_packed);
+    count_launch(ctx, 4);
+    CG_CUDA_TRY(ctx, cudaGetLastError());
+    return CG_OK;
+}
+
+int fp64_dense_residual(cg_ctx* ctx, int n, int ld, const double* d_ninv, const double* d_v, const double* d_s,
+                        double* d_w, cudaStream_t s)
+{
+    dense_residual<<<(n + kThreads - 1) / kThreads, kThreads, 0, s>>>(n, ld, d_ninv, d_v, d_s, d_w);
     count_launch(ctx);
     CG_CUDA_TRY(ctx, cudaGetLastError());
     return CG_OK;

@@ -204,6 +204,21 @@ double cg_likelihood_logdet(const cg_lik* lik);
 void cg_likelihood_destroy(cg_lik* lik);
 const char* cg_likelihood_last_error(const cg_lik* lik);
 
+/* The pixel-space part of LikelihoodPolarization (include/likelihood.hpp:137-224,
+   source/likelihood.cpp:341-401,536-612).  c_packed: the (2 npix)-pixel Q-then-U covariance,
+   packed; ninv: the (2 npix) x (2 npix) inverse noise matrix, row-major as n_inv.txt holds it,
+   taken symmetric; good[ngood]: the kept pixels.  The construct keeps the Q and U rows and
+   columns of the kept pixels and factors cInv = N^-1 + N^-1 C N^-1 (2 ngood pixels) on the
+   device, FP64; cg_likelihood_logdet gives its raw ln det (the reference subtracts
+   detOffset = 16078.083180 from it).  calculate: v [2 ngood] = N^-1 (Q, U) at the kept pixels,
+   subtract [2 ngood] = the Q, U template correlated with T at the kept pixels (the reference
+   forms it from the TT a_lm with alm2map_pol; that harmonic step is the caller's):
+   chi2 = w^T cInv^-1 w with w = v - N^-1 subtract; logdet = the raw ln det. */
+int cg_likelihood_pol_create(cg_lik** lik, int npix, const int* good, int ngood, const double* c_packed,
+                             const double* ninv, int device);
+int cg_likelihood_pol_calculate(cg_lik* lik, const double* v, const double* subtract, double* chi2,
+                                double* logdet);
+
 /* No counterpart in the reference.  The same construct + calculate as
    cg_likelihood_create / cg_likelihood_calculate, for one map, for callers
    that cannot allocate device memory (code running inside another framework's

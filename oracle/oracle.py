@@ -205,6 +205,26 @@ def read_legendre_file(path):
     return int(lmax), int(npix), data.reshape(int(lmax) + 1, int(npix) * (int(npix) + 1) // 2)
 
 
+def likelihood_pol(c_packed, npix, good, ninv, v, subtract):
+    """LikelihoodPolarization's pixel-space algebra (source/likelihood.cpp:341-401,536-612) in
+    numpy FP64: keep the Q and U rows / columns of the kept pixels, cInv = N^-1 + N^-1 C N^-1,
+    logDet = ln det cInv (raw, without detOffset), w = v - N^-1 subtract, chi2 = w^T cInv^-1 w.
+    Returns (chi2, logdet_raw)."""
+    size = 2 * npix
+    c = np.zeros((size, size))
+    iu = np.triu_indices(size)
+    c[iu[0], iu[1]] = np.asarray(c_packed)[iu[1] * (iu[1] + 1) // 2 + iu[0]]
+    c = c + np.triu(c, 1).T
+    idx = np.concatenate([np.asarray(good), npix + np.asarray(good)])
+    cm = c[np.ix_(idx, idx)]
+    nm = np.asarray(ninv).reshape(size, size)[np.ix_(idx, idx)]
+    m = nm + nm @ (cm @ nm)
+    sign, logdet = np.linalg.slogdet(m)
+    w = np.asarray(v) - nm @ np.asarray(subtract)
+    chi2 = float(w @ np.linalg.solve(m, w))
+    return chi2, float(logdet) if sign > 0 else float("nan")
+
+
 def noise_matrix(sims):
     """Averaging step of calculateNoiseMatrix (source/c_matrix_generator.cpp:887-910) over
     sims [nsims, n]: (packed noise matrix, max |per-pixel mean|)."""
