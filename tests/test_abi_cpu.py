@@ -75,6 +75,37 @@ def test_bad_config_rejected_before_device():
         cg.Context(lmax=8, fwhm_deg=7.0, nside=2, good_pixels=[0, 1, 999])
 
 
+def test_new_entry_points_reject_bad_arguments_before_the_device():
+    """Argument checks of the table, noise-matrix and polarisation entry points run before any
+    device work; with valid arguments and no GPU the polarisation likelihood fails loudly."""
+    import ctypes
+    L = cg.library()
+    assert L.cg_legendre_table(None, 0, 3, None) == cg.CG_ERR_BAD_ARG
+    assert L.cg_noise_matrix_from_sims(None, 10, 4, None, None, None) == cg.CG_ERR_BAD_ARG
+    h = ctypes.c_void_p()
+    good = np.array([0, 1], dtype=np.int32)
+    gp = good.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+    c = np.zeros(8 * 9 // 2)
+    ninv = np.eye(8)
+    assert L.cg_likelihood_pol_create(ctypes.byref(h), 0, gp, 2, cg._p(c), cg._p(ninv), 0) == cg.CG_ERR_BAD_ARG
+    bad = np.array([0, 7], dtype=np.int32)  # pixel 7 of 4
+    assert L.cg_likelihood_pol_create(ctypes.byref(h), 4, bad.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), 2,
+                                      cg._p(c), cg._p(ninv), 0) == cg.CG_ERR_BAD_ARG
+    with pytest.raises(cg.CGError) as ei:
+        cg.LikelihoodPolarization(c[:5], 4, good, ninv)
+    assert ei.value.code == cg.CG_ERR_BAD_ARG
+    nan_c = c.copy()
+    nan_c[0] = np.nan
+    with pytest.raises(cg.CGError) as ei:
+        cg.LikelihoodPolarization(nan_c, 4, good, ninv)
+    assert ei.value.code == cg.CG_ERR_NONFINITE
+    import torch
+    if not torch.cuda.is_available():
+        with pytest.raises(cg.CGError) as ei:
+            cg.LikelihoodPolarization(c + np.concatenate([[1.0] * 36]), 4, good, ninv)
+        assert ei.value.code == cg.CG_ERR_NO_DEVICE
+
+
 def test_legendre_file_reader_and_writer_match_the_reference_format(oracle_mod, tmp_path):
     """The reference's own LegendrePolynomialContainer file reads into the values the oracle
     computes, and writes back byte for byte (no device needed for file I/O)."""
