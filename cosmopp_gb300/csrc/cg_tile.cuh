@@ -87,8 +87,20 @@ __device__ __forceinline__ void df_add(float& hi, float& lo, float v)
     hi = t;
 }
 
+// two double-float partial sums combined (Knuth's TwoSum on the high words, the low words added)
+__device__ __forceinline__ void df_merge(float& hi, float& lo, float h2, float l2)
+{
+    const float t = hi + h2;
+    const float z = t - hi;
+    lo = (lo + l2) + ((hi - (t - z)) + (h2 - z));
+    hi = t;
+}
+
 // One CTA walks SYMV_TPB consecutive tiles of one batch element: 128-bit loads, the next tile
 // prefetched into registers while the current one is reduced.  grid (ceil(tiles / SYMV_TPB), B).
+// The four partial sums of a row are combined in FP32 (double-float for DF) and converted to FP64
+// once: this GPU's FP64 rate is about two operations per clock per SM, and converting every
+// thread's partials cost more than reading the tile.
 constexpr int SYMV_TPB = 8;
 template <bool DF>
 __global__ void __launch_bounds__(256) symv_partials(int nt, const float* __restrict__ V, size_t strideA,
@@ -97,7 +109,7 @@ __global__ void __launch_bounds__(256) symv_partials(int nt, const float* __rest
 {
     __shared__ float s[TS][TS + 1];
     __shared__ float svh[2][TS], svl[2][TS];
-    __shared__ double red[4][2][TS];
+    __shared__ float redh[4][2][TS], redl[4][2][TS];
     const int b = blockIdx.y, ntile = ntiles_lower(nt);
     const int t0 = blockIdx.x * SYMV_TPB;
     const int tn = min(SYMV_TPB, ntile - t0);
@@ -147,13 +159,26 @@ __global__ void __launch_bounds__(256) symv_partials(int nt, const float* __rest
                 th = fmaf(vt, svh[1][c], th);
             }
         }
-        red[q][0][r] = (double)ah + (double)al;
-        red[q][1][r] = (double)th + (double)tl;
+        redh[q][0][r] = ah;
+        redl[q][0][r] = al;
+        redh[q][1][r] = th;
+        redl[q][1][r] = tl;
         __syncthreads();
         if (q == 0) {
             double* p = part + ((size_t)b * ntile + t) * 2 * TS;
-            p[r] = ((red[0][0][r] + red[1][0][r]) + red[2][0][r]) + red[3][0][r];
-            p[TS + r] = (I != J) ? ((red[0][1][r] + red[1][1][r]) + red[2][1][r]) + red[3][1][r] : 0.0;
+            float h0 = redh[0][0][r], l0 = redl[0][0][r], h1 = redh[0][1][r], l1 = redl[0][1][r];
+#pragma unroll
+            for (int k = 1; k < 4; ++k) {
+                if (DF) {
+                    df_merge(h0, l0, redh[k][0][r], redl[k][0][r]);
+                    df_merge(h1, l1, redh[k][1][r], redl[k][1][r]);
+                } else {
+                    h0 += redh[k][0][r];
+                    h1 += redh[k][1][r];
+                }
+            }
+            p[r] = DF ? (double)h0 + (double)l0 : (double)h0;
+            p[TS + r] = (I != J) ? (DF ? (double)h1 + (double)l1 : (double)h1) : 0.0;
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k) cur[k] = nxt[k];
