@@ -93,7 +93,7 @@ struct MixedWork {
     double* y = nullptr;         // [cap][N] L_ref^-1 d
     double* x = nullptr;         // [cap][N] (I+K)^-1 y
     double* r = nullptr;         // [cap][N] refinement residual
-    double* part = nullptr;      // [cap][tiles][2][TS] matvec partials
+    double* part = nullptr;      // [cap][tiles][2][TS] matvec partials (FP64 for trmv, float2 pairs for symv)
     float* gpart = nullptr;      // [tiles][cap][lpad] adjoint partials
     float* proj = nullptr;       // [cap][nharm_pad] Z^T x_b
     double* ld = nullptr;        // [cap] ln det C_b

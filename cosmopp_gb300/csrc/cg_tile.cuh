@@ -72,8 +72,8 @@ namespace tile {
 
 // Symmetric matvec on the tiled lower storage, two deterministic passes:
 // symv_partials: per lower tile (I, J): part[t][0][r] = (V_IJ v_J)[r],
-//                part[t][1][c] = (V_IJ^T v_I)[c] (I != J);
-// symv_reduce:   out_I = sum_J (row-I pieces) in a fixed order, in FP64.
+//                part[t][1][c] = (V_IJ^T v_I)[c] (I != J), each as a double-float pair (hi, lo);
+// symv_reduce:   out_I = sum_J (row-I pieces) in a fixed order, double-float, one FP64 conversion.
 // DF = false: FP32 products and in-tile sums (a solve, whose error is then
 // refined away).  DF = true: the vector is split into two FP32 words
 // (hi + lo) and every product is formed exactly with an FMA, the in-tile sums
@@ -105,7 +105,7 @@ constexpr int SYMV_TPB = 8;
 template <bool DF>
 __global__ void __launch_bounds__(256) symv_partials(int nt, const float* __restrict__ V, size_t strideA,
                                                      const double* __restrict__ v, int vstride,
-                                                     double* __restrict__ part)
+                                                     float2* __restrict__ part)
 {
     __shared__ float s[TS][TS + 1];
     __shared__ float svh[2][TS], svl[2][TS];
@@ -165,7 +165,7 @@ __global__ void __launch_bounds__(256) symv_partials(int nt, const float* __rest
         redl[q][1][r] = tl;
         __syncthreads();
         if (q == 0) {
-            double* p = part + ((size_t)b * ntile + t) * 2 * TS;
+            float2* p = part + ((size_t)b * ntile + t) * 2 * TS;
             float h0 = redh[0][0][r], l0 = redl[0][0][r], h1 = redh[0][1][r], l1 = redl[0][1][r];
 #pragma unroll
             for (int k = 1; k < 4; ++k) {
@@ -177,24 +177,30 @@ __global__ void __launch_bounds__(256) symv_partials(int nt, const float* __rest
                     h1 += redh[k][1][r];
                 }
             }
-            p[r] = DF ? (double)h0 + (double)l0 : (double)h0;
-            p[TS + r] = (I != J) ? (DF ? (double)h1 + (double)l1 : (double)h1) : 0.0;
+            p[r] = make_float2(h0, DF ? l0 : 0.f);
+            p[TS + r] = (I != J) ? make_float2(h1, DF ? l1 : 0.f) : make_float2(0.f, 0.f);
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k) cur[k] = nxt[k];
     }
 }
 
-static __global__ void __launch_bounds__(64) symv_reduce(int nt, const double* __restrict__ part, double* __restrict__ out,
+static __global__ void __launch_bounds__(64) symv_reduce(int nt, const float2* __restrict__ part, double* __restrict__ out,
                                                   int ostride, const double* __restrict__ add, double sign)
 {
     const int I = blockIdx.x, b = blockIdx.y, r = threadIdx.x, ntile = ntiles_lower(nt);
-    const double* pb = part + (size_t)b * ntile * 2 * TS;
-    double s = 0.0;
-    for (int J = 0; J <= I; ++J) s += pb[(size_t)tile_index(I, J) * 2 * TS + r];
-    for (int J = I + 1; J < nt; ++J) s += pb[(size_t)tile_index(J, I) * 2 * TS + TS + r];
+    const float2* pb = part + (size_t)b * ntile * 2 * TS;
+    float h = 0.f, l = 0.f;
+    for (int J = 0; J <= I; ++J) {
+        const float2 x = pb[(size_t)tile_index(I, J) * 2 * TS + r];
+        df_merge(h, l, x.x, x.y);
+    }
+    for (int J = I + 1; J < nt; ++J) {
+        const float2 x = pb[(size_t)tile_index(J, I) * 2 * TS + TS + r];
+        df_merge(h, l, x.x, x.y);
+    }
     const size_t o = (size_t)b * ostride + I * TS + r;
-    out[o] = (add ? add[o] : 0.0) + sign * s;
+    out[o] = (add ? add[o] : 0.0) + sign * ((double)h + (double)l);
 }
 
 }  // namespace tile

@@ -166,26 +166,39 @@ __global__ void __launch_bounds__(256) build_ubar(int N, int lmax, int lp, const
     for (int k = threadIdx.x; k < NE * lp; k += blockDim.x) dst[(size_t)(k / NE) * TILE_ELEMS + k % NE] = out[k];
 }
 
-// y[b][I-block] = sum_{J <= I} Mref_IJ d_b[J-block]; grid (nt, maps), 256 threads
-__global__ void __launch_bounds__(256) trmv_lower(int nt, int n, int N, const double* __restrict__ M,
-                                                  const double* __restrict__ d, int d_stride,
-                                                  double* __restrict__ y)
+// y = M d for the lower-triangular tiled FP64 M, one CTA per tile (I, J <= I) and map:
+// part[t][r] = (M_IJ d_J)[r] (four partial sums per row, fixed order), then trmv_reduce sums the
+// row's tiles in order.  One CTA per tile spreads the FP64 products over every SM (a CTA per row
+// block left 40 SMs to do them at this GPU's FP64 rate).
+__global__ void __launch_bounds__(256) trmv_partials(int nt, int n, const double* __restrict__ M,
+                                                     const double* __restrict__ d, int d_stride,
+                                                     double* __restrict__ part)
 {
-    __shared__ double part[4][TS];
-    const int I = blockIdx.x, b = blockIdx.y;
+    __shared__ double red[4][TS];
+    const int t = blockIdx.x, b = blockIdx.y, ntile = ntiles_lower(nt);
+    int I, J;
+    tile_coords(t, I, J);
     const int r = threadIdx.x % TS, q = threadIdx.x / TS;
+    const double* tl = M + (size_t)t * TILE_ELEMS;
     const double* db = d + (size_t)b * d_stride;
     double s = 0.0;
-    for (int J = 0; J <= I; ++J) {
-        const double* t = M + (size_t)tile_index(I, J) * TILE_ELEMS;
-        for (int c = q; c < TS; c += 4) {
-            const int j = J * TS + c;
-            if (j < n) s += t[r + TS * c] * db[j];
-        }
+    for (int c = q; c < TS; c += 4) {
+        const int j = J * TS + c;
+        if (j < n) s = fma(tl[r + TS * c], db[j], s);
     }
-    part[q][r] = s;
+    red[q][r] = s;
     __syncthreads();
-    if (q == 0) y[(size_t)b * N + I * TS + r] = ((part[0][r] + part[1][r]) + part[2][r]) + part[3][r];
+    if (q == 0) part[((size_t)b * ntile + t) * TS + r] = ((red[0][r] + red[1][r]) + red[2][r]) + red[3][r];
+}
+
+__global__ void __launch_bounds__(64) trmv_reduce(int nt, int N, const double* __restrict__ part,
+                                                  double* __restrict__ y)
+{
+    const int I = blockIdx.x, b = blockIdx.y, r = threadIdx.x, ntile = ntiles_lower(nt);
+    const double* pb = part + (size_t)b * ntile * TS;
+    double s = 0.0;
+    for (int J = 0; J <= I; ++J) s += pb[(size_t)tile_index(I, J) * TS + r];
+    y[(size_t)b * N + I * TS + r] = s;
 }
 
 // eps[l][b] = C_bl / cref_l - 1 (0 for l < 2 and padding)
@@ -487,26 +500,40 @@ __global__ void __launch_bounds__(256) project_x(int B, int N, int nhp, const fl
     }
 }
 
-// grad[b][l] = (sum_t part[t][b][l]) / cref_l - sum_{h in l} proj[b][h]^2, FP64 sums in a fixed
-// order; rows of Z for l are h = l^2 - 4 .. l^2 + 2l - 4; grid B
-__global__ void adj_finish(int B, int ntile, int lmax, int lp, int nhp, const float* __restrict__ part,
-                           const float* __restrict__ proj, const double* __restrict__ cref,
-                           double* __restrict__ grad)
+// grad_bl = (sum over tiles of part) / cref_l - sum_{h in l} proj_bh^2, with the rows of Z for l
+// at h = l^2 - 4 .. l^2 + 2l - 4; grid B.  The tile sums are
+// double-float in FP32, four threads per l over interleaved tiles merged in a fixed order, and
+// converted to FP64 once: summing 820 partials per l in FP64 ran at this GPU's FP64 rate.
+__global__ void __launch_bounds__(256) adj_finish(int B, int ntile, int lmax, int lp, int nhp,
+                                                  const float* __restrict__ part, const float* __restrict__ proj,
+                                                  const double* __restrict__ cref, double* __restrict__ grad)
 {
-    const int b = blockIdx.x;
-    for (int l = threadIdx.x; l <= lmax; l += blockDim.x) {
-        double g = 0.0;
-        if (l >= 2) {
-            double s = 0.0;
-            for (int t = 0; t < ntile; ++t) s += (double)part[((size_t)t * B + b) * lp + l];
-            double xx = 0.0;
-            for (int h = l * l - 4; h < (l + 1) * (l + 1) - 4; ++h) {
-                const double p = (double)proj[(size_t)b * nhp + h];
-                xx += p * p;
+    __shared__ float sh[4][64], sl[4][64];
+    const int b = blockIdx.x, li = threadIdx.x % 64, ch = threadIdx.x / 64;
+    for (int base = 0; base <= lmax; base += 64) {
+        const int l = base + li;
+        float h = 0.f, lo = 0.f;
+        if (l >= 2 && l <= lmax)
+            for (int t = ch; t < ntile; t += 4) df_add(h, lo, part[((size_t)t * B + b) * lp + l]);
+        sh[ch][li] = h;
+        sl[ch][li] = lo;
+        __syncthreads();
+        if (ch == 0 && l <= lmax) {
+            double g = 0.0;
+            if (l >= 2) {
+#pragma unroll
+                for (int k = 1; k < 4; ++k) df_merge(h, lo, sh[k][li], sl[k][li]);
+                const double sum = (double)h + (double)lo;
+                double xx = 0.0;
+                for (int hh = l * l - 4; hh < (l + 1) * (l + 1) - 4; ++hh) {
+                    const double p = (double)proj[(size_t)b * nhp + hh];
+                    xx += p * p;
+                }
+                g = sum / cref[l] - xx;
             }
-            g = s / cref[l] - xx;
+            grad[(size_t)b * (lmax + 1) + l] = g;
         }
-        grad[(size_t)b * (lmax + 1) + l] = g;
+        __syncthreads();
     }
 }
 
@@ -716,13 +743,15 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
     CG_CUDA_TRY(ctx, cudaMemsetAsync(w.tcerr, 0, sizeof(int) * (1 + tc_queue_slots(nt)), s));
     init_status<<<(B + 127) / 128, 128, 0, s>>>(B, d_cl, lmax, w.st);
     make_eps<<<B, 64, 0, s>>>(B, lmax, lp, d_cl, w.cref, w.eps);
-    count_launch(ctx, d_stride == 0 ? 5 : 4);
+    count_launch(ctx, d_stride == 0 ? 6 : 5);
     // y = Mref d: one map (broadcast) or one per element
     if (d_stride == 0) {
-        trmv_lower<<<dim3(nt, 1), 256, 0, s>>>(nt, n, N, w.Mref, d_d, 0, w.r);
+        trmv_partials<<<dim3(ntile, 1), 256, 0, s>>>(nt, n, w.Mref, d_d, 0, w.part);
+        trmv_reduce<<<dim3(nt, 1), 64, 0, s>>>(nt, N, w.part, w.r);
         broadcast_vec<<<dim3((N + 255) / 256, B), 256, 0, s>>>(B, N, w.r, w.y);
     } else {
-        trmv_lower<<<dim3(nt, B), 256, 0, s>>>(nt, n, N, w.Mref, d_d, d_stride, w.y);
+        trmv_partials<<<dim3(ntile, B), 256, 0, s>>>(nt, n, w.Mref, d_d, d_stride, w.part);
+        trmv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, N, w.part, w.y);
     }
     // A_b = I + sum_l eps_bl Ubar_l; small batches use 32-element CTA tiles (more entries per block)
     // when the double-buffered table rows fit in shared memory
@@ -745,13 +774,14 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
     stage_mark(ctx, ST_LAUUM, s);
     if ((rc = tiled_lauum_tc(ctx, B, nt, w.Ms, w.Mc, w.V, w.tcerr, s))) return rc;
     stage_mark(ctx, ST_SOLVE, s);
-    // x = V y; r = y - A x; x += V r
-    symv_partials<false><<<dim3((ntile + SYMV_TPB - 1) / SYMV_TPB, B), 256, 0, s>>>(nt, w.V, tiled, w.y, N, w.part);
-    symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, w.part, w.x, N, nullptr, 1.0);
-    symv_partials<true><<<dim3((ntile + SYMV_TPB - 1) / SYMV_TPB, B), 256, 0, s>>>(nt, w.A, tiled, w.x, N, w.part);
-    symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, w.part, w.r, N, w.y, -1.0);
-    symv_partials<false><<<dim3((ntile + SYMV_TPB - 1) / SYMV_TPB, B), 256, 0, s>>>(nt, w.V, tiled, w.r, N, w.part);
-    symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, w.part, w.x, N, w.x, 1.0);
+    // x = V y; r = y - A x; x += V r  (the partials buffer holds double-float pairs here)
+    float2* pf = reinterpret_cast<float2*>(w.part);
+    symv_partials<false><<<dim3((ntile + SYMV_TPB - 1) / SYMV_TPB, B), 256, 0, s>>>(nt, w.V, tiled, w.y, N, pf);
+    symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, pf, w.x, N, nullptr, 1.0);
+    symv_partials<true><<<dim3((ntile + SYMV_TPB - 1) / SYMV_TPB, B), 256, 0, s>>>(nt, w.A, tiled, w.x, N, pf);
+    symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, pf, w.r, N, w.y, -1.0);
+    symv_partials<false><<<dim3((ntile + SYMV_TPB - 1) / SYMV_TPB, B), 256, 0, s>>>(nt, w.V, tiled, w.r, N, pf);
+    symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, pf, w.x, N, w.x, 1.0);
     chi2_mixed<<<B, 256, 0, s>>>(n, N, N, w.y, w.x, w.ld, d_m2lnl, d_chi2, d_logdet);
     count_launch(ctx, 7);
     stage_mark(ctx, ST_ADJOINT, s);
@@ -771,7 +801,7 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
         }
         const int nhp = nharm_pad(lmax);
         project_x<<<dim3(nhp / 64, (B + 63) / 64), 256, 0, s>>>(B, N, nhp, w.Zf, w.x, w.proj);
-        adj_finish<<<B, 64, 0, s>>>(B, ntile, lmax, lp, nhp, w.gpart, w.proj, w.cref, d_grad);
+        adj_finish<<<B, 256, 0, s>>>(B, ntile, lmax, lp, nhp, w.gpart, w.proj, w.cref, d_grad);
         count_launch(ctx, 2);
     }
     merge_tc_status<<<(B + 127) / 128, 128, 0, s>>>(B, w.tcerr, w.st);
