@@ -48,3 +48,13 @@ def test_file_formats_match_the_reference(exe, tmp_path):
     vals = np.frombuffer(back[4:4 + 8 * n * (n + 1) // 2], dtype=np.float64)
     assert np.allclose(vals, g["c_packed"], rtol=1e-5, atol=1e-9)
     assert open(tmp_path / "lp.bin", "rb").read() == open(os.path.join(G, "legendre_nside2_lmax8.bin"), "rb").read()
+
+
+@pytest.mark.parametrize("src", ["test_dropin.cpp", "test_legendre_lp.cpp", "test_files_cpu.cpp"])
+def test_dropin_header_compiles_as_cxx11_without_warnings(src):
+    """The reference builds with -std=c++11 (CMakeLists.txt:13); code using the drop-in header
+    must compile there too, warning-free under -Wall -Wextra."""
+    p = subprocess.run(["g++", "-std=c++11", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I",
+                        os.path.join(ROOT, "include"), os.path.join(ROOT, "tests", "cxx", src)],
+                       capture_output=True, text=True, timeout=120)
+    assert p.returncode == 0, p.stderr
