@@ -41,7 +41,9 @@ def parse():
     ap.add_argument("--path", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--batch", type=int, default=None)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--fp64-compare-batch", type=int, default=16)
+    ap.add_argument("--fp64-compare-batch", type=int, default=None,
+                    help="elements the plain FP64 path evaluates for the mixed/FP64 ratio and the error bars "
+                         "(default: the whole batch)")
     ap.add_argument("--workload", default=WORKLOAD, help="named workload in cosmopp_gb300.workload.WORKLOADS")
     ap.add_argument("--hmc-iters", type=int, default=12, help="batched-HMC iterations reported beside the line "
                                                               "(64 chains x 20 leapfrog steps of 0.05); 0 = skip")
@@ -158,7 +160,7 @@ def cpu_baseline(wl, d, seconds_budget=20.0):
     O.build()
     cores = os.cpu_count() or 1
     O.set_threads(cores)
-    nest = np.array([int(x) for x in __import__("cosmopp_gb300").ring2nest(wl.nside, wl.ring_kept)], dtype=np.int32)
+    nest = O.ring2nest(wl.nside, wl.ring_kept)
     xyz = O.unit_vectors(wl.nside, nest, "NEST")
     t0 = time.perf_counter()
     done = 0
@@ -177,13 +179,13 @@ def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    import cosmopp_gb300 as cg
+    # the workload module is pure numpy: importing it does not load the product library
     from cosmopp_gb300 import workload as W
     from oracle import oracle as O
     wl = W.make(args.workload, batch=args.batch)
     # data map from the oracle's own FP64 covariance (no GPU on this arm)
     O.build()
-    nest = cg.ring2nest(wl.nside, wl.ring_kept)
+    nest = O.ring2nest(wl.nside, wl.ring_kept)
     xyz = O.unit_vectors(wl.nside, nest, "NEST")
     c = O.cl_to_cmatrix(wl.cl_fid, xyz, wl.fwhm_deg)
     d = W.draw_data(W.packed_to_full(c, wl.n) + wl.sigma ** 2 * np.eye(wl.n), wl.z)
@@ -359,32 +361,54 @@ def run_ours(args):
     if roof_build:
         out["roofline_build"] = roof_build
     out["roofline"]["peak_source"] = peak_kind
-    if rank == 0 and path == "mixed" and args.fp64_compare_batch > 0:
-        # the plain FP64 GPU path on the same workload, for the mixed-vs-FP64 ratio and the error bar
-        Bf = min(args.fp64_compare_batch, B)
+    nfp = B if args.fp64_compare_batch is None else min(args.fp64_compare_batch, B)
+    if rank == 0 and path == "mixed" and nfp > 0:
+        # The plain FP64 GPU path on the same inputs (itself pinned to the reference to <= 1e-6): the
+        # mixed/FP64 throughput ratio, the FP64 stage split (build vs Cholesky), and the error of every
+        # element's -2lnL and of every gradient component of the timed batch against it.
+        Bf = nfp
         c64 = cg.Context(lmax=wl.lmax, fwhm_deg=wl.fwhm_deg, nside=wl.nside, good_pixels=wl.ring_kept,
                          scheme="RING", noise_sigma=wl.sigma, max_batch=Bf, precision="fp64", device=local)
         clsf = cls[0, :Bf].contiguous()
         m64 = torch.empty(Bf, dtype=torch.float64, device=dev)
         g64 = torch.empty(Bf, L1, dtype=torch.float64, device=dev)
-        c64.loglike_device(Bf, clsf.data_ptr(), dd.data_ptr(), 0, m64.data_ptr(), None, None, g64.data_ptr(),
+        t64 = torch.empty(Bf, L1, dtype=torch.float64, device=dev)
+        zero = torch.zeros_like(dd)
+        nw = min(Bf, 8)
+        c64.loglike_device(nw, clsf.data_ptr(), dd.data_ptr(), 0, m64.data_ptr(), None, None, g64.data_ptr(),
                            None, sp)
-        torch.cuda.synchronize()
-        step(0)
         torch.cuda.synchronize()
         f0 = torch.cuda.Event(enable_timing=True)
         f1 = torch.cuda.Event(enable_timing=True)
+        c64.set_profiling(True)
         f0.record(stream)
         c64.loglike_device(Bf, clsf.data_ptr(), dd.data_ptr(), 0, m64.data_ptr(), None, None, g64.data_ptr(),
                            None, sp)
         f1.record(stream)
         torch.cuda.synchronize()
         ms64 = f0.elapsed_time(f1)
-        err = (m2[:Bf] - m64).abs().max().item()
-        gerr = ((grad[:Bf] - g64).abs().max(dim=1).values / g64.abs().max(dim=1).values).max().item()
-        out["plain_fp64_gpu"] = {"value": Bf / (ms64 / 1000.0), "unit": "evals/s", "batch": Bf,
-                                 "mixed_over_fp64": value / world / (Bf / (ms64 / 1000.0)),
-                                 "max_abs_delta_m2lnl": err, "max_rel_delta_grad": gerr}
+        st64 = c64.stage_times()
+        c64.set_profiling(False)
+        # the trace term T_l = tr(C^-1 dC/dC_l) of each element (the gradient of a zero map): the
+        # size of the two terms whose difference is the gradient, the scale of its absolute floor
+        mz = torch.empty(Bf, dtype=torch.float64, device=dev)
+        c64.loglike_device(Bf, clsf.data_ptr(), zero.data_ptr(), 0, mz.data_ptr(), None, None, t64.data_ptr(),
+                           None, sp)
+        step(0)
+        torch.cuda.synchronize()
+        dm = (m2[:Bf] - m64).abs()
+        dg = (grad[:Bf, 2:] - g64[:, 2:]).abs()
+        rel = dg / g64[:, 2:].abs()
+        over_T = dg / t64[:, 2:]
+        out["plain_fp64_gpu"] = {
+            "value": Bf / (ms64 / 1000.0), "unit": "evals/s", "batch": Bf,
+            "mixed_over_fp64": value / world / (Bf / (ms64 / 1000.0)),
+            "stages_ms": {k: round(v, 3) for k, v in st64.items() if k != "end"},
+            "max_abs_delta_m2lnl": dm.max().item(), "elements_compared": Bf,
+            "grad_max_rel_delta": rel.max().item(), "grad_p99_rel_delta": torch.quantile(rel.flatten(), 0.99).item(),
+            "grad_max_delta_over_trace": over_T.max().item(),
+            "grad_components_within_1e-4": int(((dg <= 1e-4 * g64[:, 2:].abs()) | (over_T <= 1e-6)).sum().item()),
+            "grad_components": int(dg.numel())}
         c64.close()
     if rank == 0 and path == "mixed" and args.hmc_iters > 0:
         # gradient + HMC: 64 chains on ln C_l (l = 2..lmax), 20 leapfrog steps of 0.05, unit masses,

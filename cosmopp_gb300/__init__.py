@@ -102,6 +102,7 @@ def library():
     L.cg_legendre_table.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp]
     L.cg_noise_matrix_from_sims.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
     L.cg_selftest_wait_timeout.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
+    L.cg_probe_tf32_rate.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp]
     L.cg_launch_count.restype = ctypes.c_longlong
     L.cg_launch_count.argtypes = [ctypes.c_void_p]
     L.cg_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int]
@@ -365,6 +366,13 @@ class Context:
         st = ctypes.c_int(-1)
         self._check(self._L.cg_selftest_wait_timeout(self._h, ctypes.byref(st)))
         return st.value
+
+    def probe_tf32_rate(self, iters=1 << 16, reps=5):
+        """TF32 tensor-core rate (TFLOP/s) of the MMA form the factorisation kernels issue, and
+        the mean launch time (ms) (cg_probe_tf32_rate)."""
+        tf, ms = ctypes.c_double(0), ctypes.c_double(0)
+        self._check(self._L.cg_probe_tf32_rate(self._h, int(iters), int(reps), ctypes.byref(tf), ctypes.byref(ms)))
+        return tf.value, ms.value
 
     def launch_count(self):
         """Kernels this context has launched so far."""

@@ -207,6 +207,8 @@ bool adjoint_tc_ok(int lp);
 int adjoint_contract_tc(cg_ctx* ctx, int B, int nt, int lp, const float* U, const float* V, size_t strideA,
                         float* part, int* d_err, cudaStream_t s);
 int selftest_wait_timeout(cg_ctx* ctx, int* host_status);
+// achieved rate of the factorisation kernels' MMA form (kind::tf32 M128 N128 K8, A in tensor memory)
+int probe_tf32_rate(cg_ctx* ctx, int iters, int reps, double* tflops, double* ms_per_launch);
 // mixed path (k_mixed.cu)
 int mixed_prepare_reference(cg_ctx* ctx, const double* cl_ref_host);
 int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, const double* d_d, int d_stride,

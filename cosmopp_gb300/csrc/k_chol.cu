@@ -239,11 +239,13 @@ size_t pair_smem() { return 2 * (size_t)TS * SmemLd<T>::v * sizeof(T); }
 template <typename T>
 size_t diag_smem() { return 2 * (size_t)TS * (TS + 1) * sizeof(T); }
 
+// The attribute belongs to the device that is current when it is set, and the FP64 kernels
+// need more than the default 48 KB, so it is set on every call (a few host microseconds):
+// a context on another device, or the allocation-free entry point on another GPU, then
+// launches with it too, and no process-wide flag is shared between threads.
 template <typename T>
 int set_smem_attrs(cg_ctx* ctx)
 {
-    static bool done = false;
-    if (done) return CG_OK;
     const int bytes = (int)pair_smem<T>();
     CG_CUDA_TRY(ctx, cudaFuncSetAttribute(chol_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_smem<T>()));
     CG_CUDA_TRY(ctx, cudaFuncSetAttribute(chol_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
@@ -251,7 +253,6 @@ int set_smem_attrs(cg_ctx* ctx)
     CG_CUDA_TRY(ctx, cudaFuncSetAttribute(trtri_finish<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     CG_CUDA_TRY(ctx, cudaFuncSetAttribute(trtri_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
     CG_CUDA_TRY(ctx, cudaFuncSetAttribute(lauum_tiles<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-    done = true;
     return CG_OK;
 }
 

@@ -14,6 +14,10 @@
 // must start at zero, so the contents a previous call left behind do not
 // matter.
 //
+// The outputs (d_out, d_status) are written by the last kernel the call queues, so
+// they are meaningful only when the call returned CG_OK; a host-side error returns
+// before that kernel is queued and leaves them as they were.
+//
 // The first call on each device resolves the array's device address with
 // cudaGetSymbolAddress (with that device current).  Make that first call
 // before capturing a CUDA graph on the device.

@@ -1468,7 +1468,116 @@ __global__ void wait_timeout_probe(int* status)
     }
 }
 
+// Rate probe for the MMA form the factorisation kernels issue: tcgen05.mma kind::tf32, M128 N128 K8,
+// A from tensor memory, B from shared memory (K-major, no swizzle), one issuing thread per CTA and
+// one CTA per SM.  The operands hold arbitrary finite values; the accumulator is never read.  The
+// issuing thread commits its MMAs to an mbarrier and waits for them with a time limit (2 s of
+// %globaltimer); a wait that gives up sets *err.  Tensor memory is freed after the wait either way.
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__global__ void __launch_bounds__(128) mma_rate_probe(int iters, int* err)
+{
+    constexpr int KC_P = 32;                     // K extent of the B operand in shared memory
+    constexpr uint32_t LBO_P = 128, SBO_P = KC_P / 4 * 128;
+    __shared__ __align__(1024) float sb[128 * KC_P];
+    __shared__ uint64_t done;
+    __shared__ uint32_t tbase;
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    for (int e = threadIdx.x; e < 128 * KC_P; e += blockDim.x) sb[e] = 1.0f + 1e-3f * (float)((e * 37) % 101);
+    if (warp == 0) tmem_alloc(&tbase, 256);  // D: columns 0-127, A: 128-159
+    if (threadIdx.x == 0) {
+        mbar_init(&done, 1);
+        fence_mbar_init();
+    }
+    fence_proxy_async();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tm = tbase;
+    {
+        float v[32];
+#pragma unroll
+        for (int i = 0; i < 32; ++i) v[i] = 0.5f + 1e-3f * (float)((lane * 13 + i * 7 + warp) % 97);
+        tmem_st32(tm + ((uint32_t)(warp * 32) << 16) + 128, v);
+    }
+    fence_before();
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        fence_after();
+        const uint32_t idesc = idesc_tf32(128, 128);
+        const uint32_t b0 = smem_u32(sb);
+        for (int it = 0; it < iters; ++it) {
+#pragma unroll
+            for (int kk = 0; kk < KC_P / 8; ++kk)
+                mma_tf32_ta(tm, tm + 128 + 8 * kk, smem_desc(b0 + kk * 2 * LBO_P, LBO_P, SBO_P), idesc,
+                            (it || kk) ? 1u : 0u);
+        }
+        mma_commit(&done);
+        const uint64_t t0 = global_ns();
+        bool ok = false;
+        while (!ok) {
+            uint32_t d;
+            asm volatile(
+                "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+                : "=r"(d)
+                : "r"(smem_u32(&done)), "r"(0u)
+                : "memory");
+            ok = d != 0;
+            if (!ok && global_ns() - t0 > 2000000000ull) break;
+        }
+        if (!ok) atomicExch(err, 1);
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 0) tmem_dealloc(tm, 256);
+}
+
 }  // namespace
+
+int probe_tf32_rate(cg_ctx* ctx, int iters, int reps, double* tflops, double* ms_per_launch)
+{
+    if (iters <= 0 || reps <= 0) { ctx->err = "probe: iters and reps must be positive"; return CG_ERR_BAD_ARG; }
+    int* d_err = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CG_CUDA_TRY(ctx, cudaMalloc((void**)&d_err, sizeof(int)));
+    int rc = CG_OK;
+    cudaError_t e = cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) {
+        mma_rate_probe<<<ctx->sm_count, 128, 0, ctx->stream>>>(iters, d_err);  // warm-up
+        count_launch(ctx);
+        e = cudaEventRecord(e0, ctx->stream);
+    }
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) {
+        mma_rate_probe<<<ctx->sm_count, 128, 0, ctx->stream>>>(iters, d_err);
+        count_launch(ctx);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    float ms = 0;
+    int herr = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e == cudaSuccess) e = cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = CG_ERR_CUDA; }
+    else if (herr) { ctx->err = "probe: a bounded wait gave up"; rc = CG_ERR_TIMEOUT; }
+    else {
+        const double flops = 2.0 * 128 * 128 * 8 * 4.0 * iters * (double)ctx->sm_count * reps;
+        *tflops = flops / (ms * 1e-3) / 1e12;
+        *ms_per_launch = ms / reps;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(d_err);
+    return rc;
+}
 
 static int tc_smem()
 {

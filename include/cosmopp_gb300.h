@@ -185,6 +185,12 @@ int cg_mh_run(cg_ctx* ctx, const double* map, int nchains, const double* x0, con
    limit, on a barrier that nothing completes; *status receives CG_ERR_TIMEOUT when the wait
    gave up and reported as it should.  Nothing faults or hangs; the context stays usable. */
 int cg_selftest_wait_timeout(cg_ctx* ctx, int* status);
+/* Tensor-core rate probe: one CTA per SM issues iters x 4 tcgen05.mma kind::tf32 M128 N128 K8
+   (A in tensor memory, B in shared memory: the form the factorisation kernels issue), reps
+   timed launches after one warm-up, CUDA events on the context's stream.  *tflops = the TF32
+   rate achieved (2 M N K per MMA), *ms = the mean launch time.  The FP32-accurate (3xTF32)
+   peak of the factorisation kernels is a third of it.  No counterpart in the reference. */
+int cg_probe_tf32_rate(cg_ctx* ctx, int iters, int reps, double* tflops, double* ms);
 /* kernels this context has launched so far */
 long long cg_launch_count(const cg_ctx* ctx);
 /* record CUDA events between the stages of each cg_loglike* call */
@@ -227,7 +233,9 @@ int cg_likelihood_pol_calculate(cg_lik* lik, const double* v, const double* subt
    each) and d_t (n) and outputs d_out[2] = {chi2, raw ln det C} and d_status
    (nullable; CG_OK or CG_ERR_NOT_PD) are all device pointers owned by the
    caller; the call itself allocates nothing and runs asynchronously on
-   `stream`.  Its workspace is one static device array sized for n <= 768
+   `stream`.  d_out and d_status are written by the call's last kernel, so
+   they hold results only when the call returned CG_OK (a host-side error
+   returns before that kernel is queued).  Its workspace is one static device array sized for n <= 768
    (about 5.5 MB, held on every GPU that loads the library until exit); larger
    n is rejected with CG_ERR_BAD_ARG (text in cg_last_error(NULL)).  Every call
    shares that array: calls whose GPU work overlaps race and must be

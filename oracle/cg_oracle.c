@@ -411,3 +411,57 @@ void orc_legendre_table(int lmax, const double* xyz, int n, double* out)
             for (int l = 0; l <= lmax; ++l) out[(long)l * np + (long)j * (j + 1) / 2 + i] = orc_legendre(l, dot);
         }
 }
+
+/* Extended-precision -2lnL pieces (test infrastructure, no reference counterpart).  Dense
+   row-major lower factor; left-looking: l_ij = (a_ij - sum_{k<j} l_ik l_jk) / l_jj, each row's
+   dot products contiguous, rows of one column in parallel. */
+int orc_loglike_extended(int n, const double* c_packed, const double* noise_var, const double* d,
+                         double* chi2, double* logdet_raw)
+{
+    long double* L = (long double*)malloc(sizeof(long double) * (size_t)n * n);
+    if (!L) return -2;
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j <= i; ++j)
+            L[(size_t)i * n + j] = (long double)c_packed[(long)i * (i + 1) / 2 + j] +
+                                   (i == j ? (long double)noise_var[i] : 0.0L);
+    int info = 0;
+    for (int j = 0; j < n && !info; ++j) {
+        long double* rj = L + (size_t)j * n;
+        long double s = rj[j];
+        for (int k = 0; k < j; ++k) s -= rj[k] * rj[k];
+        if (!(s > 0)) { info = j + 1; break; }
+        const long double piv = sqrtl(s);
+        rj[j] = piv;
+#pragma omp parallel for schedule(static)
+        for (int i = j + 1; i < n; ++i) {
+            long double* ri = L + (size_t)i * n;
+            long double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+            int k = 0;
+            for (; k + 4 <= j; k += 4) {
+                a0 += ri[k] * rj[k];
+                a1 += ri[k + 1] * rj[k + 1];
+                a2 += ri[k + 2] * rj[k + 2];
+                a3 += ri[k + 3] * rj[k + 3];
+            }
+            for (; k < j; ++k) a0 += ri[k] * rj[k];
+            ri[j] = (ri[j] - ((a0 + a1) + (a2 + a3))) / piv;
+        }
+    }
+    if (!info) {
+        long double ld = 0, c2 = 0;
+        long double* y = (long double*)malloc(sizeof(long double) * n);
+        for (int i = 0; i < n; ++i) {
+            const long double* ri = L + (size_t)i * n;
+            long double s = d[i];
+            for (int k = 0; k < i; ++k) s -= ri[k] * y[k];
+            y[i] = s / ri[i];
+            c2 += y[i] * y[i];
+            ld += logl(ri[i]);
+        }
+        free(y);
+        *chi2 = (double)c2;
+        *logdet_raw = (double)(2 * ld);
+    }
+    free(L);
+    return info;
+}

@@ -84,6 +84,15 @@ void orc_legendre_table(int lmax, const double* xyz, int n, double* out);
    |mean over simulations| of any pixel. */
 void orc_noise_matrix(int nsims, int n, const double* sims, double* packed, double* max_abs_mean);
 
+/* No reference counterpart: the exact-arithmetic yardstick for the FP64 noise floor.
+   chi2 = d^T A^-1 d and ln det A for A = C (packed FP64) + diag(noise_var), computed in
+   long double (x87 80-bit on x86-64: 64-bit significand, about 2000 times finer than FP64)
+   by a dense Cholesky and a forward solve.  Returns 0, or j + 1 when pivot j is not
+   positive.  On targets whose long double is IEEE quad it is software arithmetic and slow;
+   the fixture script runs it in the x86 build container only. */
+int orc_loglike_extended(int n, const double* c_packed, const double* noise_var, const double* d,
+                         double* chi2, double* logdet_raw);
+
 #ifdef __cplusplus
 }
 #endif

@@ -59,6 +59,7 @@ def lib():
         L.orc_adjoint.argtypes = [_dp, ctypes.c_int, _dp, ctypes.c_int, ctypes.c_double, _dp]
         L.orc_noise_matrix.argtypes = [ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
         L.orc_legendre_table.argtypes = [ctypes.c_int, _dp, ctypes.c_int, _dp]
+        L.orc_loglike_extended.argtypes = [ctypes.c_int, _dp, _dp, _dp, _dp, _dp]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_get_threads.restype = ctypes.c_int
         L.hp_ring2nest.restype = ctypes.c_long
@@ -178,6 +179,18 @@ def evaluate(cl, xyz, fwhm_deg, noise_var, d, grad=True, restart=False):
     return dict(m2lnl=m2.value, chi2=chi2.value, logdet=ld.value, grad=g, status=st)
 
 
+def loglike_extended(c_packed, noise_var, d):
+    """chi2 and raw ln det of C + diag(noise_var) in extended precision (long double): the
+    yardstick the FP64 paths' rounding noise is measured against.  Returns (chi2, logdet, info)."""
+    c = np.ascontiguousarray(c_packed, dtype=np.float64)
+    d = np.ascontiguousarray(d, dtype=np.float64)
+    n = len(d)
+    nv = np.broadcast_to(np.asarray(noise_var, dtype=np.float64), (n,)).copy()
+    chi2, ld = ctypes.c_double(0), ctypes.c_double(0)
+    info = lib().orc_loglike_extended(n, _p(c), _p(nv), _p(d), ctypes.byref(chi2), ctypes.byref(ld))
+    return chi2.value, ld.value, info
+
+
 def adjoint(w_packed, lmax, xyz, fwhm_deg):
     w = np.ascontiguousarray(w_packed, dtype=np.float64)
     xyz = np.ascontiguousarray(xyz, dtype=np.float64)
@@ -239,26 +252,33 @@ def noise_matrix(sims):
 # ---- the reference itself, compiled here by oracle/ref/Makefile (absent on machines
 #      without the reference sources) ----
 
-def ref_available():
-    return os.path.exists(_REF)
+def ref_available(variant=""):
+    return os.path.exists(_REF.replace(".so", variant + ".so"))
 
 
-def ref():
+def ref(variant=""):
+    """The compiled reference: variant "" is the strict -O2 build, "_fastmath" the build with
+    the reference's shipped -ffast-math flags (make -C oracle/ref fastmath)."""
     global _ref
+    if variant:
+        return _bind_ref(ctypes.CDLL(_REF.replace(".so", variant + ".so")))
     if _ref is None:
-        R = ctypes.CDLL(_REF)
-        R.ref_last_error.restype = ctypes.c_char_p
-        R.ref_legendre.restype = ctypes.c_double
-        R.ref_legendre.argtypes = [ctypes.c_int, ctypes.c_double]
-        R.ref_beam.restype = ctypes.c_double
-        R.ref_beam.argtypes = [ctypes.c_int, ctypes.c_double]
-        R.ref_cl_to_cmatrix.argtypes = [_dp, ctypes.c_int, ctypes.c_long, ctypes.c_double, _ip, ctypes.c_int, _dp]
-        R.ref_likelihood.argtypes = [_dp, ctypes.c_int, ctypes.c_long, ctypes.c_double, _ip, ctypes.c_int,
-                                     ctypes.c_double, _dp, _dp, _dp, _dp]
-        R.ref_likelihood_packed.argtypes = [_dp, _dp, _dp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp]
-        R.ref_fiducial_matrix.argtypes = [_dp, ctypes.c_int, ctypes.c_long, ctypes.c_int, ctypes.c_double, _ip,
-                                          ctypes.c_int, _dp]
-        R.ref_pixel_window.argtypes = [ctypes.c_long, ctypes.c_int, ctypes.c_double, _dp]
-        R.ref_run_subtest.argtypes = [ctypes.c_char_p, ctypes.c_int, _dp, _dp]
-        _ref = R
+        _ref = _bind_ref(ctypes.CDLL(_REF))
     return _ref
+
+
+def _bind_ref(R):
+    R.ref_last_error.restype = ctypes.c_char_p
+    R.ref_legendre.restype = ctypes.c_double
+    R.ref_legendre.argtypes = [ctypes.c_int, ctypes.c_double]
+    R.ref_beam.restype = ctypes.c_double
+    R.ref_beam.argtypes = [ctypes.c_int, ctypes.c_double]
+    R.ref_cl_to_cmatrix.argtypes = [_dp, ctypes.c_int, ctypes.c_long, ctypes.c_double, _ip, ctypes.c_int, _dp]
+    R.ref_likelihood.argtypes = [_dp, ctypes.c_int, ctypes.c_long, ctypes.c_double, _ip, ctypes.c_int,
+                                 ctypes.c_double, _dp, _dp, _dp, _dp]
+    R.ref_likelihood_packed.argtypes = [_dp, _dp, _dp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp]
+    R.ref_fiducial_matrix.argtypes = [_dp, ctypes.c_int, ctypes.c_long, ctypes.c_int, ctypes.c_double, _ip,
+                                      ctypes.c_int, _dp]
+    R.ref_pixel_window.argtypes = [ctypes.c_long, ctypes.c_int, ctypes.c_double, _dp]
+    R.ref_run_subtest.argtypes = [ctypes.c_char_p, ctypes.c_int, _dp, _dp]
+    return R

@@ -22,8 +22,15 @@ them through ctypes.  Every number stored below comes from the reference:
 * CMatrix binary and text files written by the reference's CMatrix, and what
   its Utils::readClFromFile reads from two C_l text files.
 
+* the FP64 noise floor at nside 16: for 100 lognormal C_l vectors (the plain
+  FP64 workload), the reference's Likelihood chi2 / logDet from its strict
+  build, the same for the first 10 from its -ffast-math build and from the
+  oracle's restated LAPACK loops, and an extended-precision (long double)
+  evaluation of the same FP64 covariance, the yardstick all of them are
+  measured against.
+
 Usage:  python tests/golden/make_golden.py [part ...]   (parts: main, fiducial,
-legendre, files; default all)
+legendre, files, config2; default all)
 """
 import ctypes
 import hashlib
@@ -175,6 +182,54 @@ def ref_like(R, cl, nside, fwhm, nest, sigma, d):
     return chi2.value, ld.value, lk.value
 
 
+def _config2_worker(args):
+    """One strict-build reference evaluation in a worker process (the reference's pair loop
+    is serial, so the 100 evaluations run side by side)."""
+    k, cl, nside, fwhm, nest, sigma, d = args
+    R = O.ref()
+    return k, ref_like(R, cl, nside, fwhm, nest, sigma, d)
+
+
+def config2_cases():
+    """The plain FP64 workload at nside 16 (100 lognormal C_l vectors) and its noise floor."""
+    import multiprocessing as mp
+    g = dict(np.load(os.path.join(HERE, "nside16_lmax47.npz")))
+    wl = W.make("nside16_lmax47")
+    nside, fwhm, sigma = wl.nside, wl.fwhm_deg, wl.sigma
+    nest = O.ring2nest(nside, wl.ring_kept)
+    assert np.array_equal(nest, g["nest_good"]) and np.array_equal(wl.cl_batch[:2], g["cls"][1:3])
+    d = g["d"]
+    cls = wl.cl_batch
+    os.environ["OMP_NUM_THREADS"] = "2"
+    os.environ["OPENBLAS_NUM_THREADS"] = "2"
+    with mp.get_context("spawn").Pool(4) as pool:
+        rows = dict(pool.map(_config2_worker, [(k, cls[k], nside, fwhm, nest, sigma, d) for k in range(len(cls))]))
+    rows = np.array([rows[k] for k in range(len(cls))])
+    O.set_threads(os.cpu_count() or 1)
+    xyz = O.unit_vectors(nside, nest, "NEST")
+    ext = []
+    for cl in cls:
+        c = O.cl_to_cmatrix(cl, xyz, fwhm)
+        chi2, ld, info = O.loglike_extended(c, sigma ** 2, d)
+        assert info == 0
+        ext.append((chi2, ld))
+    ext = np.array(ext)
+    nsub = 10
+    Rf = O.ref("_fastmath")
+    fast = np.array([ref_like(Rf, cls[k], nside, fwhm, nest, sigma, d) for k in range(nsub)])
+    restated = np.array([O.evaluate(cls[k], xyz, fwhm, sigma ** 2, d, grad=False)["m2lnl"] for k in range(nsub)])
+    m2 = rows[:, 0] + (rows[:, 1] - DET_OFFSET)
+    m2_ext = ext[:, 0] + ext[:, 1]
+    np.savez_compressed(os.path.join(HERE, "config2_nside16.npz"), nside=nside, lmax=wl.lmax, fwhm_deg=fwhm,
+                        sigma=sigma, nest_good=nest, cls=cls, d=d, chi2=rows[:, 0], logdet_raw=rows[:, 1] - DET_OFFSET,
+                        m2lnl=m2, chi2_ext=ext[:, 0], logdet_ext=ext[:, 1], m2lnl_ext=m2_ext,
+                        m2lnl_fastmath=fast[:, 0] + (fast[:, 1] - DET_OFFSET), m2lnl_restated=restated)
+    print("config2 nside16: %d vectors; |reference - extended| max %.3e; |fastmath - extended| max %.3e; "
+          "|restated - extended| max %.3e" % (len(cls), np.abs(m2 - m2_ext).max(),
+                                              np.abs(fast[:, 0] + fast[:, 1] - DET_OFFSET - m2_ext[:nsub]).max(),
+                                              np.abs(restated - m2_ext[:nsub]).max()))
+
+
 def main(parts):
     if not O.ref_available():
         raise SystemExit("build the reference first: make -C oracle/ref")
@@ -185,6 +240,8 @@ def main(parts):
     R.ref_cmatrix_write_files.argtypes = [dp, ctypes.c_int, ctypes.c_long, ctypes.c_double, ip, ctypes.c_int,
                                           ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]
     R.ref_read_cl.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, dp, ctypes.c_int]
+    if "config2" in parts:
+        config2_cases()
     if "legendre" in parts:
         legendre_cases(R)
     if "files" in parts:
@@ -245,4 +302,4 @@ def main(parts):
 
 
 if __name__ == "__main__":
-    main(set(sys.argv[1:]) or {"main", "fiducial", "legendre", "files"})
+    main(set(sys.argv[1:]) or {"main", "fiducial", "legendre", "files", "config2"})

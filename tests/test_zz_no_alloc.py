@@ -66,6 +66,47 @@ def test_noalloc_matches_allocating_entry_point_twice(oracle_mod):
         lik.close()
 
 
+def test_noalloc_matches_reference_golden_and_allocates_nothing(oracle_mod):
+    """Straight against the reference's own chi2 and ln det (golden fixture), and the property
+    the entry point exists for: after a first call on the device, a call leaves the device's
+    free memory unchanged."""
+    import torch
+    L = _lib()
+    g = load_golden("nside8_lmax24")
+    n, c, noise, t = _case("nside8_lmax24", oracle_mod, 0)
+    rc, out, st = _noalloc(L, n, c, noise, t)
+    assert rc == 0 and st == 0
+    assert abs(out[0] - float(g["chi2"][0])) <= TOL, (out[0], g["chi2"][0])
+    assert abs(out[1] - float(g["logdet_raw"][0])) <= TOL, (out[1], g["logdet_raw"][0])
+    dev = torch.device("cuda", 0)
+    dc = torch.tensor(c, dtype=torch.float64, device=dev)
+    dn = torch.tensor(noise, dtype=torch.float64, device=dev)
+    dt = torch.tensor(t, dtype=torch.float64, device=dev)
+    res = torch.zeros(2, dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info(dev)
+    rc = L.cg_likelihood_noalloc(n, ctypes.c_void_p(dc.data_ptr()), None, ctypes.c_void_p(dn.data_ptr()),
+                                 ctypes.c_void_p(dt.data_ptr()), ctypes.c_void_p(res.data_ptr()), None, None)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info(dev)
+    assert rc == 0
+    assert free1 == free0, (free0, free1)
+    assert np.array_equal(res.cpu().numpy(), out)
+
+
+def test_noalloc_reports_not_positive_definite(oracle_mod):
+    """An indefinite covariance: the call runs (CG_OK) and the device status word says
+    CG_ERR_NOT_PD, as chol_diag set it."""
+    L = _lib()
+    n, c, noise, t = _case("nside4", oracle_mod, 0)
+    rc, out, st = _noalloc(L, n, -c, noise, t)
+    assert rc == 0, L.cg_last_error(None)
+    assert st == cg.CG_ERR_NOT_PD
+    # and the shared workspace serves a good matrix again on the next call
+    rc, out, st = _noalloc(L, n, c, noise, t)
+    assert rc == 0 and st == 0
+
+
 def test_noalloc_rejects_sizes_beyond_its_workspace():
     L = _lib()
     dummy = ctypes.c_void_p(16)  # never dereferenced: the size check comes first
