@@ -227,6 +227,27 @@ def run_ours(args):
                      noise_sigma=wl.sigma, max_batch=B, precision=path, device=local,
                      cl_ref=wl.cl_fid if path == "mixed" else None, recenter="fixed")
     L1 = wl.lmax + 1
+    tuning = None
+    if path == "mixed":
+        # launch shapes: the tuning file's entry for this device and shape, else an autotune run
+        # (one coordinate pass, CUDA-event timed) appended to the file
+        tune_file = os.environ.get("COSMOPP_GB300_TUNE_FILE") or os.path.join(ROOT, "cosmopp_gb300", "_lib",
+                                                                               "tune.txt")
+        t0 = time.perf_counter()
+        found = ctx.tune_load(tune_file)
+        tune_ms = None if found else ctx.autotune(B, tune_file)
+        tuning = {"knobs": ctx.tuning(), "source": "tuning file" if found else "autotuned in this run",
+                  "file": os.path.relpath(tune_file, ROOT), "autotune_ms_per_call": tune_ms,
+                  "seconds": round(time.perf_counter() - t0, 2)}
+    plan = ctx.memory_plan()
+    plan180 = cg.plan_memory(180 * 10 ** 9, lmax=wl.lmax, fwhm_deg=wl.fwhm_deg, nside=wl.nside,
+                             good_pixels=wl.ring_kept, scheme="RING", noise_sigma=wl.sigma, max_batch=B,
+                             precision=path)
+    admission = {"bytes_fixed_gb": round(plan["bytes_fixed"] / 1e9, 3),
+                 "bytes_per_element_gb": round(plan["bytes_per_element"] / 1e9, 4),
+                 "free_gb_at_create": round(plan["bytes_budget"] / 1e9, 1), "chunk": plan["chunk"],
+                 "batch_total_gb": round((plan["bytes_fixed"] + B * plan["bytes_per_element"]) / 1e9, 2),
+                 "max_batch_in_180gb": plan180["max_batch_fit"]}
     dev = torch.device("cuda", local)
     # a few distinct batches, cycled so that no two consecutive steps see the same inputs
     nb = 4
@@ -311,20 +332,30 @@ def run_ours(args):
     ctx.set_profiling(False)
     torch.cuda.synchronize()
     peaks, peak_kind = load_peaks()
+    tf32 = None
+    if path == "mixed":
+        # the tensor-core peak of the factorisation kernels' own MMA form, measured now, with the clocks
+        pc = ClockSampler(local)
+        pc.start()
+        rates = [ctx.probe_tf32_rate(1 << 16, 10)[0] for _ in range(4)]
+        tf32 = {"tflops": max(rates), "clocks": pc.stop(), "form": "tcgen05.mma kind::tf32 M128 N128 K8, A in "
+                "tensor memory, B in shared memory, one issuing thread per SM (cg_probe_tf32_rate)"}
     n, N = wl.n, ((wl.n + 127) // 128) * 128  # the library pads to an even number of 64-tiles
     pairs = n * (n + 1) // 2
     roof_build = None
     if path == "mixed":
         # The dominant kernel: the tensor-core Cholesky (chol_tc_update + chol_tc_panel).  Algorithmic
-        # work n^3/3 flops per evaluation.  Its peak: tcgen05 kind::tf32 runs at half the bf16 rate and
-        # 3xTF32 spends three MMAs per product for FP32 accuracy, so the FP32-accurate peak is
-        # bf16 / 6; the kernel sits inside a long step, so the sustained bf16 figure is used.
-        peak3 = peaks["bf16_tflops_sustained"] / 6.0
+        # work n^3/3 flops per evaluation.  Its peak: the TF32 rate of its own MMA form, measured live
+        # by the library's probe at this run's clocks, divided by the three MMAs per product of the
+        # FP32-accurate 3xTF32 split.  (The bf16-derived figure, measured bf16 sustained / 6, is
+        # reported beside it; it assumes TF32 = bf16 / 2 at the power-capped bf16 clock.)
+        peak3 = tf32["tflops"] / 3.0
         chol_flops = B * n ** 3 / 3.0
         roof = {"kernel": "tensor-core Cholesky (chol_tc_update + chol_tc_panel, 3xTF32 tcgen05)",
                 "bound": "tensor", "achieved": chol_flops / (stages["cholesky"] * 1e-3) / 1e12, "peak": peak3,
                 "unit": "TFLOP/s", "algorithmic_flops": chol_flops,
-                "peak_note": "measured bf16 sustained / 6 (TF32 = bf16 / 2, three MMAs per product)",
+                "peak_note": "measured TF32 rate of the kernel's MMA form / 3 (three MMAs per FP32-accurate "
+                             "product); bf16-derived alternative %.1f" % (peaks["bf16_tflops_sustained"] / 6.0),
                 # ncu dram__bytes_read + dram__bytes_write of all 39 Cholesky launches of one batch-32
                 # step, x B / 32 (traffic grows with the batch): profiles/tc_kernels_nside16_b32.md
                 "traffic": 4.891e9 * B / 32.0 if args.workload == WORKLOAD else None,
@@ -336,7 +367,10 @@ def run_ours(args):
         tiled = nt * (nt + 1) // 2 * 4096
         lpad = ((L1 + 15) // 16) * 16
         build_bytes = tiled * lpad * 4 + B * tiled * 4
-        roof_build = {"kernel": "contraction (build stage, K_b = sum_l eps_bl Ubar_l, FP32 out)", "bound": "hbm",
+        fwd_tc = bool(tuning and tuning["knobs"].get("fwd") == 1)
+        roof_build = {"kernel": "build stage: A_b = I + sum_l eps_bl Ubar_l, FP32 out (%s)" %
+                                ("contract_fwd_tc, tcgen05 3xTF32" if fwd_tc else "contract_fwd, FP32 FMA"),
+                      "bound": "hbm",
                       "achieved": build_bytes / (stages["build"] * 1e-3) / 1e9, "peak": peaks["hbm_gbs"],
                       "unit": "GB/s", "algorithmic_bytes": build_bytes}
         roof_build["frac"] = roof_build["achieved"] / roof_build["peak"]
@@ -357,7 +391,11 @@ def run_ours(args):
            "e2e": {"value": job_throughput(B, world, e2e_ms), "unit": "evals/s", "ms_per_step": e2e_ms,
                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
            "stages_ms": {k: round(v, 4) for k, v in stages.items() if k != "end"},
-           "roofline": roof}
+           "roofline": roof, "admission": admission}
+    if tuning:
+        out["config"]["tuning"] = tuning
+    if tf32:
+        out["tf32_probe"] = tf32
     if roof_build:
         out["roofline_build"] = roof_build
     out["roofline"]["peak_source"] = peak_kind

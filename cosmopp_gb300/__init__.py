@@ -103,6 +103,13 @@ def library():
     L.cg_noise_matrix_from_sims.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
     L.cg_selftest_wait_timeout.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
     L.cg_probe_tf32_rate.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp]
+    L.cg_plan_memory.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    L.cg_get_memory_plan.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    L.cg_tune_set.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]
+    L.cg_tune_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, _ip]
+    L.cg_tune_describe.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]
+    L.cg_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_char_p, _dp]
+    L.cg_tune_load.argtypes = [ctypes.c_void_p, ctypes.c_char_p, _ip]
     L.cg_launch_count.restype = ctypes.c_longlong
     L.cg_launch_count.argtypes = [ctypes.c_void_p]
     L.cg_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int]
@@ -168,6 +175,74 @@ def beam(l, fwhm_deg):
     return library().cg_beam(int(l), float(fwhm_deg))
 
 
+def _make_config(L, lmax, fwhm_deg, nside, good_pixels, scheme, dirs, beam, noise_sigma, noise_var, max_batch,
+                 precision, device, cl_ref, recenter, recenter_radius):
+    """A cg_config for these arguments and the arrays its pointers refer to (keep them alive)."""
+    cfg = _Config()
+    L.cg_config_init(ctypes.byref(cfg))
+    keep = []
+    if dirs is not None:
+        d = _f64(dirs).reshape(-1, 3)
+        keep.append(d)
+        cfg.dirs = _p(d)
+        cfg.n = d.shape[0]
+    else:
+        cfg.nside = int(nside)
+        cfg.scheme = SCHEME[scheme.upper()]
+        if good_pixels is not None:
+            g = np.ascontiguousarray(good_pixels, dtype=np.int32)
+            keep.append(g)
+            cfg.good_pixels = g.ctypes.data_as(_ip)
+            cfg.n = len(g)
+    cfg.lmax = int(lmax)
+    cfg.fwhm_deg = float(fwhm_deg)
+    if beam is not None:
+        b = _f64(beam)
+        keep.append(b)
+        cfg.beam = _p(b)
+    cfg.noise_sigma = float(noise_sigma)
+    if noise_var is not None:
+        nv = _f64(noise_var)
+        keep.append(nv)
+        cfg.noise_var = _p(nv)
+    cfg.max_batch = int(max_batch)
+    cfg.precision = PRECISION[precision]
+    cfg.device = int(device)
+    if cl_ref is not None:
+        cr = _f64(cl_ref)
+        keep.append(cr)
+        cfg.cl_ref = _p(cr)
+    cfg.recenter = RECENTER[recenter]
+    cfg.recenter_radius = float(recenter_radius)
+    return cfg, keep
+
+
+class _MemPlan(ctypes.Structure):
+    _fields_ = [("bytes_fixed", ctypes.c_size_t), ("bytes_per_element", ctypes.c_size_t),
+                ("bytes_budget", ctypes.c_size_t), ("bytes_reserve", ctypes.c_size_t),
+                ("max_batch_fit", ctypes.c_int), ("chunk", ctypes.c_int)]
+
+
+def _plan_dict(p):
+    return {k: getattr(p, k) for k, _ in _MemPlan._fields_}
+
+
+def plan_memory(budget_bytes=0, lmax=2, fwhm_deg=1.0, nside=None, good_pixels=None, scheme="NEST", dirs=None,
+                beam=None, noise_sigma=1e-3, noise_var=None, max_batch=1, precision="fp64", device=0, cl_ref=None,
+                recenter="auto", recenter_radius=1.0):
+    """Memory admission of a context with these arguments, before creating it (cg_plan_memory):
+    dict(bytes_fixed, bytes_per_element, bytes_budget, bytes_reserve, max_batch_fit, chunk).
+    budget_bytes = 0 plans against the device's free memory, otherwise needs no device."""
+    L = library()
+    cfg, keep = _make_config(L, lmax, fwhm_deg, nside, good_pixels, scheme, dirs, beam, noise_sigma, noise_var,
+                             max_batch, precision, device, cl_ref, recenter, recenter_radius)
+    p = _MemPlan()
+    rc = L.cg_plan_memory(ctypes.byref(cfg), ctypes.c_size_t(int(budget_bytes)), ctypes.byref(p))
+    if rc:
+        raise CGError(rc, L.cg_last_error(None).decode())
+    return _plan_dict(p)
+
+
 # ---- context ------------------------------------------------------------------
 
 class Context:
@@ -182,42 +257,8 @@ class Context:
                  noise_sigma=1e-3, noise_var=None, max_batch=1, precision="fp64", device=0, cl_ref=None,
                  recenter="auto", recenter_radius=1.0):
         L = library()
-        cfg = _Config()
-        L.cg_config_init(ctypes.byref(cfg))
-        keep = []
-        if dirs is not None:
-            d = _f64(dirs).reshape(-1, 3)
-            keep.append(d)
-            cfg.dirs = _p(d)
-            cfg.n = d.shape[0]
-        else:
-            cfg.nside = int(nside)
-            cfg.scheme = SCHEME[scheme.upper()]
-            if good_pixels is not None:
-                g = np.ascontiguousarray(good_pixels, dtype=np.int32)
-                keep.append(g)
-                cfg.good_pixels = g.ctypes.data_as(_ip)
-                cfg.n = len(g)
-        cfg.lmax = int(lmax)
-        cfg.fwhm_deg = float(fwhm_deg)
-        if beam is not None:
-            b = _f64(beam)
-            keep.append(b)
-            cfg.beam = _p(b)
-        cfg.noise_sigma = float(noise_sigma)
-        if noise_var is not None:
-            nv = _f64(noise_var)
-            keep.append(nv)
-            cfg.noise_var = _p(nv)
-        cfg.max_batch = int(max_batch)
-        cfg.precision = PRECISION[precision]
-        cfg.device = int(device)
-        if cl_ref is not None:
-            cr = _f64(cl_ref)
-            keep.append(cr)
-            cfg.cl_ref = _p(cr)
-        cfg.recenter = RECENTER[recenter]
-        cfg.recenter_radius = float(recenter_radius)
+        cfg, keep = _make_config(L, lmax, fwhm_deg, nside, good_pixels, scheme, dirs, beam, noise_sigma, noise_var,
+                                 max_batch, precision, device, cl_ref, recenter, recenter_radius)
         h = ctypes.c_void_p()
         rc = L.cg_create(ctypes.byref(h), ctypes.byref(cfg))
         if rc:
@@ -228,6 +269,12 @@ class Context:
         self.n = L.cg_get_n(h)
         self.max_batch = int(max_batch)
         self.precision = precision
+
+    def memory_plan(self):
+        """The memory admission this context was created under (cg_get_memory_plan)."""
+        p = _MemPlan()
+        self._check(self._L.cg_get_memory_plan(self._h, ctypes.byref(p)))
+        return _plan_dict(p)
 
     def close(self):
         if getattr(self, "_h", None):
@@ -366,6 +413,37 @@ class Context:
         st = ctypes.c_int(-1)
         self._check(self._L.cg_selftest_wait_timeout(self._h, ctypes.byref(st)))
         return st.value
+
+    TUNE_KNOBS = ("fwd", "fwd_ctas", "chol_ctas", "panel_ctas", "adj")
+
+    def tune_set(self, knob, value):
+        self._check(self._L.cg_tune_set(self._h, knob.encode(), int(value)))
+
+    def tune_get(self, knob):
+        v = ctypes.c_int(0)
+        self._check(self._L.cg_tune_get(self._h, knob.encode(), ctypes.byref(v)))
+        return v.value
+
+    def tuning(self):
+        """The launch-shape knobs in effect, as a dict (cg_tune_describe)."""
+        buf = ctypes.create_string_buffer(512)
+        self._check(self._L.cg_tune_describe(self._h, buf, 512))
+        return {k: int(v) for k, v in (t.split("=") for t in buf.value.decode().split())}
+
+    def autotune(self, B=None, path=None):
+        """Coordinate search over the launch-shape knobs at batch B (default max_batch), applied
+        and appended to the tuning file `path` if given (cg_autotune).  Returns the chosen
+        shape's median ms per call."""
+        ms = ctypes.c_double(0)
+        self._check(self._L.cg_autotune(self._h, int(B or self.max_batch),
+                                        None if path is None else str(path).encode(), ctypes.byref(ms)))
+        return ms.value
+
+    def tune_load(self, path):
+        """Apply a tuning file's entry for this shape; True if one was found (cg_tune_load)."""
+        f = ctypes.c_int(0)
+        self._check(self._L.cg_tune_load(self._h, str(path).encode(), ctypes.byref(f)))
+        return bool(f.value)
 
     def probe_tf32_rate(self, iters=1 << 16, reps=5):
         """TF32 tensor-core rate (TFLOP/s) of the MMA form the factorisation kernels issue, and

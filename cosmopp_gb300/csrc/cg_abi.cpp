@@ -9,6 +9,8 @@
 #include <memory>
 #include <new>
 
+#include <cstdlib>
+
 #include "cg_internal.h"
 
 namespace {
@@ -96,6 +98,88 @@ extern "C" void cg_destroy(cg_ctx* ctx)
     delete ctx;
 }
 
+// ---- memory admission ----------------------------------------------------------
+
+namespace {
+
+// the context's own allocations of cg_create: geometry, beam tables, staging for max_batch elements
+size_t staging_bytes(int N, int lmax, int max_batch)
+{
+    const size_t L1 = (size_t)lmax + 1, Bm = (size_t)max_batch;
+    return sizeof(double) * (3 * (size_t)N + N + 3 * L1 + Bm * L1) + sizeof(double) * (Bm * (3 + L1) + Bm * N) +
+           sizeof(int) * Bm;
+}
+
+void fill_plan(const cg_ctx* shape, size_t budget, cg_memory_plan* p)
+{
+    size_t fixed = staging_bytes(shape->N, shape->lmax, shape->max_batch), per = 0;
+    if (shape->precision == CG_PREC_MIXED) {
+        size_t f = 0;
+        cg::mixed_bytes(shape, &f, &per);
+        fixed += f;
+    } else {
+        per = cg::fp64_bytes_per_element(shape);
+    }
+    p->bytes_fixed = fixed;
+    p->bytes_per_element = per;
+    p->bytes_budget = budget;
+    p->bytes_reserve = ((size_t)256 << 20) + budget / 100;
+    const size_t avail = budget > p->bytes_reserve + fixed ? budget - p->bytes_reserve - fixed : 0;
+    const size_t fit = per ? avail / per : 0;
+    p->max_batch_fit = (int)std::min<size_t>(fit, (size_t)1 << 30);
+    p->chunk = std::min(shape->max_batch, p->max_batch_fit);
+}
+
+// pixel count, padded size and l range of a configuration (the checks cg_create repeats)
+int shape_of(const cg_config* cfg, cg_ctx* shape)
+{
+    if (!cfg || cfg->struct_size != (int)sizeof(cg_config)) return CG_ERR_BAD_ARG;
+    if (cfg->lmax < 2 || cfg->lmax > 255 || cfg->max_batch < 1) return CG_ERR_BAD_ARG;
+    if (cfg->precision != CG_PREC_FP64 && cfg->precision != CG_PREC_MIXED) return CG_ERR_BAD_ARG;
+    int n;
+    if (cfg->dirs) {
+        n = cfg->n;
+    } else {
+        if (cfg->nside <= 0 || cfg->nside > 8192) return CG_ERR_BAD_ARG;
+        const long npix = cg_nside2npix(cfg->nside);
+        n = cfg->good_pixels ? cfg->n : (int)npix;
+        if (n > npix) return CG_ERR_BAD_ARG;
+    }
+    if (n <= 0) return CG_ERR_BAD_ARG;
+    shape->n = n;
+    shape->nt = 2 * ((n + 2 * cg::TS - 1) / (2 * cg::TS));
+    shape->N = shape->nt * cg::TS;
+    shape->lmax = cfg->lmax;
+    shape->max_batch = cfg->max_batch;
+    shape->precision = cfg->precision;
+    return CG_OK;
+}
+
+}  // namespace
+
+extern "C" int cg_plan_memory(const cg_config* cfg, size_t budget_bytes, cg_memory_plan* plan)
+{
+    if (!plan) return CG_ERR_BAD_ARG;
+    cg_ctx shape;
+    int rc = shape_of(cfg, &shape);
+    if (rc) { g_create_error = "cg_plan_memory: invalid configuration"; return rc; }
+    if (budget_bytes == 0) {
+        if (cudaSetDevice(cfg->device) != cudaSuccess) { g_create_error = "cg_plan_memory: no such device"; return CG_ERR_NO_DEVICE; }
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { g_create_error = "cg_plan_memory: cudaMemGetInfo failed"; return CG_ERR_CUDA; }
+        budget_bytes = fr;
+    }
+    fill_plan(&shape, budget_bytes, plan);
+    return CG_OK;
+}
+
+extern "C" int cg_get_memory_plan(const cg_ctx* ctx, cg_memory_plan* plan)
+{
+    if (!ctx || !plan) return CG_ERR_BAD_ARG;
+    *plan = ctx->plan;
+    return CG_OK;
+}
+
 extern "C" int cg_create(cg_ctx** out, const cg_config* cfg)
 {
     g_create_error.clear();
@@ -168,6 +252,24 @@ extern "C" int cg_create(cg_ctx** out, const cg_config* cfg)
         g_create_error = "cudaStreamCreate failed";
         return CG_ERR_CUDA;
     }
+    // admission: plan the device bytes against the free memory before allocating anything
+    {
+        size_t fr = 0, tot = 0;
+        if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) { g_create_error = "cudaMemGetInfo failed"; cg_destroy(ctx.release()); return CG_ERR_CUDA; }
+        fill_plan(ctx.get(), fr, &ctx->plan);
+        if (ctx->plan.max_batch_fit < 1) {
+            char msg[256];
+            std::snprintf(msg, sizeof msg,
+                          "admission: %.2f GB fixed + %.2f GB per batch element do not fit in %.2f GB free "
+                          "(reserve %.2f GB)",
+                          ctx->plan.bytes_fixed / 1e9, ctx->plan.bytes_per_element / 1e9, fr / 1e9,
+                          ctx->plan.bytes_reserve / 1e9);
+            g_create_error = msg;
+            cg_destroy(ctx.release());
+            return CG_ERR_ALLOC;
+        }
+        ctx->chunk = ctx->plan.chunk;
+    }
     const int N = ctx->N, L1 = ctx->lmax + 1, Bm = ctx->max_batch;
     std::vector<double> soa(3 * (size_t)N, 0.0), nz(N, 0.0);
     for (int i = 0; i < ctx->n; ++i) {
@@ -192,6 +294,11 @@ extern "C" int cg_create(cg_ctx** out, const cg_config* cfg)
     if (ctx->precision == CG_PREC_MIXED && cfg->cl_ref) {
         const int rc = cg::mixed_prepare_reference(ctx.get(), cfg->cl_ref);
         if (rc) { g_create_error = ctx->err; cg_destroy(ctx.release()); return rc; }
+    }
+    // launch shapes tuned earlier for this device, pixel count, l range and batch size
+    if (ctx->precision == CG_PREC_MIXED) {
+        const char* tf = std::getenv("COSMOPP_GB300_TUNE_FILE");
+        if (tf && *tf) cg_tune_load(ctx.get(), tf, nullptr);
     }
     *out = ctx.release();
     return CG_OK;
@@ -375,9 +482,24 @@ extern "C" int cg_loglike_device(cg_ctx* ctx, int B, const double* d_cl, const d
     CG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
     ctx->nmarks = 0;
-    if (ctx->precision == CG_PREC_MIXED)
-        return cg::mixed_loglike(ctx, B, d_cl, nullptr, d_d, d_stride, d_m2lnl, d_chi2, d_logdet, d_grad, d_status, s);
-    return cg::fp64_loglike(ctx, B, d_cl, d_d, d_stride, d_m2lnl, d_chi2, d_logdet, d_grad, d_status, s);
+    // the batch in pieces of the admitted chunk (one piece when the whole batch fits)
+    const int chunk = ctx->chunk > 0 ? ctx->chunk : B;
+    const size_t L1 = (size_t)ctx->lmax + 1;
+    for (int b0 = 0; b0 < B; b0 += chunk) {
+        const int nb = std::min(chunk, B - b0);
+        const double* cl = d_cl + b0 * L1;
+        const double* dd = d_d + (d_stride ? (size_t)b0 * d_stride : 0);
+        double* m2 = d_m2lnl + b0;
+        double* c2 = d_chi2 ? d_chi2 + b0 : nullptr;
+        double* ld = d_logdet ? d_logdet + b0 : nullptr;
+        double* gr = d_grad ? d_grad + b0 * L1 : nullptr;
+        int* st = d_status ? d_status + b0 : nullptr;
+        const int rc = ctx->precision == CG_PREC_MIXED
+                           ? cg::mixed_loglike(ctx, nb, cl, nullptr, dd, d_stride, m2, c2, ld, gr, st, s)
+                           : cg::fp64_loglike(ctx, nb, cl, dd, d_stride, m2, c2, ld, gr, st, s);
+        if (rc) return rc;
+    }
+    return CG_OK;
 }
 
 extern "C" int cg_loglike(cg_ctx* ctx, int B, const double* cl, const double* d, int d_stride, double* m2lnl,

@@ -101,6 +101,15 @@ struct MixedWork {
     int* tcerr = nullptr;        // [1 + tc_queue_slots] tensor-core error flag and work-queue counters
 };
 
+// ---- launch-shape knobs of the mixed path (set by cg_tune_set / cg_autotune / a tuning file) ----
+struct Tune {
+    int fwd = 1;          // forward contraction: 0 = FP32 FMA (contract_fwd), 1 = tensor cores (contract_fwd_tc)
+    int fwd_ctas = 0;     // persistent CTAs of the tensor-core contraction (0 = one per SM)
+    int chol_ctas = 0;    // persistent CTAs of the Cholesky's off-diagonal work queue, column blocks J > 0 (0 = one per SM)
+    int panel_ctas = 0;   // persistent CTAs of the Cholesky's panel solve (0 = one per SM)
+    int adj = 0;          // tensor-core adjoint variant (fetch groups / buffers), 0 .. 2
+};
+
 }  // namespace cg
 
 struct cg_ctx {
@@ -127,6 +136,10 @@ struct cg_ctx {
     size_t d_out_bytes = 0;
     cg::Fp64Work w64;
     cg::MixedWork wmx;
+    cg::Tune tune;
+    // memory admission (cg_plan_memory): a call's batch runs in pieces of `chunk` elements
+    int chunk = 0;
+    cg_memory_plan plan = {};
     std::string err;
     // instrumentation: kernel launch counter and optional per-stage CUDA events
     long long launches = 0;
@@ -160,6 +173,9 @@ inline void stage_mark(cg_ctx* ctx, int stage, cudaStream_t s)
 inline void count_launch(cg_ctx* ctx, long long k = 1) { ctx->launches += k; }
 // plain FP64 path (k_fp64.cu)
 int fp64_ensure(cg_ctx* ctx, int B);
+size_t fp64_bytes_per_element(const cg_ctx* ctx);
+// mixed path device bytes: reference point + table, and one batch element's workspace
+void mixed_bytes(const cg_ctx* ctx, size_t* fixed, size_t* per_element);
 int fp64_build_tiled(cg_ctx* ctx, int B, const double* d_cl, bool add_noise, cudaStream_t s);
 int fp64_build_tiled_into(cg_ctx* ctx, int B, const double* d_cl, bool add_noise, double* A, cudaStream_t s);
 int fp64_build_packed(cg_ctx* ctx, int B, const double* d_cl, double* d_out, cudaStream_t s);
@@ -206,6 +222,11 @@ int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, const float* Mc,
 bool adjoint_tc_ok(int lp);
 int adjoint_contract_tc(cg_ctx* ctx, int B, int nt, int lp, const float* U, const float* V, size_t strideA,
                         float* part, int* d_err, cudaStream_t s);
+// A_b = I + sum_l eps_bl Ubar_l on the tensor cores (k_tc.cu), for lp % 16 == 0, lp <= 64; ctas = the
+// persistent grid (0 = one CTA per SM)
+bool contract_fwd_tc_ok(int lp);
+int contract_fwd_tc_launch(cg_ctx* ctx, int B, int nt, int lp, const float* U, const float* eps, float* A,
+                           size_t strideA, int* d_err, int ctas, cudaStream_t s);
 int selftest_wait_timeout(cg_ctx* ctx, int* host_status);
 // achieved rate of the factorisation kernels' MMA form (kind::tf32 M128 N128 K8, A in tensor memory)
 int probe_tf32_rate(cg_ctx* ctx, int iters, int reps, double* tflops, double* ms_per_launch);

@@ -624,6 +624,16 @@ void fp64_free(cg_ctx* ctx)
     w = Fp64Work();
 }
 
+// Device bytes of one batch element's FP64 workspace: the allocations of fp64_ensure, in its order
+size_t fp64_bytes_per_element(const cg_ctx* ctx)
+{
+    const size_t tiled = tiled_elems(ctx->nt);
+    const int ntile = ntiles_lower(ctx->nt);
+    return sizeof(double) * tiled * 2 + sizeof(double) * (size_t)ctx->nt * TILE_ELEMS +
+           sizeof(double) * (size_t)ctx->N * 3 + sizeof(double) * (size_t)ntile * (ctx->lmax + 1) + sizeof(int) +
+           sizeof(double);
+}
+
 int fp64_ensure(cg_ctx* ctx, int B)
 {
     Fp64Work& w = ctx->w64;

@@ -569,6 +569,20 @@ void mixed_free(cg_ctx* ctx)
     w = MixedWork();
 }
 
+// Device bytes of the mixed path: *fixed = the reference point's buffers and the whitened table
+// (ensure_ref_bufs), *per_element = one batch element's workspace (ensure_batch_bufs), in their order
+void mixed_bytes(const cg_ctx* ctx, size_t* fixed, size_t* per_element)
+{
+    const size_t tiled = tiled_elems(ctx->nt);
+    const size_t N = (size_t)ctx->N, nt = (size_t)ctx->nt, lp = (size_t)lpad_of(ctx->lmax);
+    const size_t nhp = (size_t)nharm_pad(ctx->lmax), ntile = (size_t)ntiles_lower(ctx->nt);
+    *fixed = sizeof(double) * (2 * tiled + nt * TILE_ELEMS + N + 2 * nhp * N) + sizeof(float) * (tiled * lp + nhp * N) +
+             sizeof(double) * ((size_t)ctx->lmax + 2) + sizeof(int) * (1 + (size_t)tc_queue_slots(ctx->nt));
+    *per_element = sizeof(float) * (2 * tiled + 2 * tc_split_elems(ctx->nt) + tc_linv_elems(ctx->nt) +
+                                    2 * tc_c1_elems(ctx->nt) + N + lp + ntile * lp + nhp) +
+                   sizeof(double) * (3 * N + ntile * 2 * TS + 1) + sizeof(int);
+}
+
 static int ensure_ref_bufs(cg_ctx* ctx)
 {
     MixedWork& w = ctx->wmx;
@@ -756,7 +770,10 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
     // A_b = I + sum_l eps_bl Ubar_l; small batches use 32-element CTA tiles (more entries per block)
     // when the double-buffered table rows fit in shared memory
     const size_t smem32 = sizeof(float) * lp * (32 + 2 * 512), smem128 = sizeof(float) * lp * (128 + 2 * 128);
-    if (B <= 48 && smem32 <= 200 * 1024) {
+    if (ctx->tune.fwd == 1 && contract_fwd_tc_ok(lp)) {
+        if ((rc = contract_fwd_tc_launch(ctx, B, nt, lp, w.U, w.eps, w.A, tiled, w.tcerr, ctx->tune.fwd_ctas, s)))
+            return rc;
+    } else if (B <= 48 && smem32 <= 200 * 1024) {
         CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_fwd<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32));
         contract_fwd<32><<<dim3((unsigned)(tiled / (512 * FWD_NBLK)), (B + 31) / 32), 256, smem32, s>>>(
             B, lp, w.U, w.eps, w.A, tiled, w.tcerr);

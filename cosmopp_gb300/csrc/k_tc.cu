@@ -57,6 +57,8 @@
 // solve) in C1 only; M in SC and C1 tiles of M^T (tile (I, J) holds (M_IJ)^T:
 // rows = M's columns in tile J, K = M's rows in tile I); Linv_J as a 128x128 SC
 // block [K chunk][plane][128 x 32].
+#include <algorithm>
+
 #include "cg_internal.h"
 #include "cg_tc.cuh"
 
@@ -1456,6 +1458,172 @@ __global__ void __launch_bounds__(ADJ_NTH, 1) contract_adj_tc(int B, int lp, con
     if (warp == 0) tmem_dealloc(tm, TMEM_COLS);
 }
 
+// ---- forward contraction on the tensor cores ---------------------------------------------------
+// A_b = I + sum_l eps_bl Ubar_l for every entry e of every lower tile and every batch element b:
+// D[e][b] = sum_l Ubar[e][l] E[b][l] with M = 128 entries (a row block of a tile), N = the batch
+// chunk (16 .. 256, zero-padded), K = lp.  3xTF32 as everywhere here; the two cross products go
+// into the accumulator first, while it is still small, and the hi*hi products last, so the tensor
+// core's one-way accumulation drift acts on the main term over only lp / 8 instructions.  The
+// identity is added in FP32 by the epilogue.  Persistent CTAs (one per SM) walk the row blocks in
+// steps of the grid; per CTA the batch chunk's E (hi and lo planes) stays in shared memory:
+//   warps 0-3 (producers): load a row block's table rows (lane = entry, coalesced per l), split them
+//              and write the K-major canonical A operand into one of two shared-memory stages;
+//   warp 8    (MMA issue): one thread issues the block's 3 lp / 8 MMAs (A and B from shared memory)
+//              into one of two tensor-memory accumulators and commits them;
+//   warps 4-7 (epilogue): drain the accumulator (lane = entry, 32 batch columns per load), add the
+//              identity on the diagonal and store A[b][e] (each warp store 128 contiguous bytes).
+constexpr int FWD_PROD = 128;
+constexpr int FWD_NTH = 2 * FWD_PROD + 32;
+constexpr int FWD_NBMAX = 256;
+
+struct FwdCtl {
+    uint64_t a_full[2];   // A stage written (one arrival per producer warp)
+    uint64_t a_empty[2];  // A stage's MMAs completed
+    uint64_t d_full[2];   // accumulator's MMAs completed
+    uint64_t d_empty[2];  // accumulator drained (one arrival per epilogue warp)
+    uint64_t fin;         // the issuer's last commit
+    uint32_t tbase;
+};
+
+template <int LP>
+__global__ void __launch_bounds__(FWD_NTH) contract_fwd_tc(int B, int nblk, int nb, const float* __restrict__ U,
+                                                           const float* __restrict__ eps, float* __restrict__ A,
+                                                           size_t strideA, int* err)
+{
+    static_assert(LP % 16 == 0 && LP <= 64, "lp");
+    constexpr uint32_t SBO_A = LP / 4 * 128;                 // row-group stride of the K-major operands
+    constexpr uint32_t A_PLANE = 128u * LP * 4;              // one plane of an A stage
+    extern __shared__ __align__(1024) unsigned char fsm_raw[];
+    unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(fsm_raw) + 1023) & ~uintptr_t(1023));
+    const uint32_t b_plane = (uint32_t)nb * LP * 4;
+    unsigned char* sB = sm;                                   // [hi, lo][nb x LP]
+    unsigned char* sA = sm + 2 * b_plane;                     // [stage][hi, lo][128 x LP]
+    __shared__ FwdCtl ctl;
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int b_begin = blockIdx.y * nb;
+    bool ok = true;
+    auto wait = [&](uint64_t* bar, uint32_t parity) {
+        if (!ok) return;
+        ok = mbar_wait(bar, parity, kMaxIter, err);
+        if (!ok) atomicExch(err, 1);
+    };
+    // E's split planes, K-major canonical (row = batch element of the chunk, K = l)
+    for (int k = threadIdx.x; k < nb * LP; k += blockDim.x) {
+        const int r = k / LP, l = k % LP, b = b_begin + r;
+        const float v = (b < B) ? eps[(size_t)l * B + b] : 0.f;
+        const float hi = tf32_rn(v), lo = tf32_rn(v - hi);
+        const uint32_t off = (uint32_t)((r >> 3) * SBO_A + (l >> 2) * 128 + (r & 7) * 16 + (l & 3) * 4);
+        *reinterpret_cast<float*>(sB + off) = hi;
+        *reinterpret_cast<float*>(sB + b_plane + off) = lo;
+    }
+    // two accumulators of nb <= 256 columns, acc apart (a power of two >= 32): 2 acc <= 512 columns
+    uint32_t acc = 32;
+    while (acc < (uint32_t)nb) acc *= 2;
+    if (warp == 8) tmem_alloc(&ctl.tbase, 2 * acc);
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&ctl.a_full[i], FWD_PROD / 32);
+            mbar_init(&ctl.a_empty[i], 1);
+            mbar_init(&ctl.d_full[i], 1);
+            mbar_init(&ctl.d_empty[i], FWD_PROD / 32);
+        }
+        mbar_init(&ctl.fin, 1);
+        fence_mbar_init();
+    }
+    fence_proxy_async();
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tm = ctl.tbase;
+    if (warp < 4) {
+        // producers: row p of every row block this CTA takes
+        const int p = threadIdx.x;
+        int i = 0;
+        for (int m = blockIdx.x; m < nblk && ok; m += gridDim.x, ++i) {
+            const int t = m / (TILE_ELEMS / 128), e = (m % (TILE_ELEMS / 128)) * 128 + p;
+            const float* src = U + (size_t)t * TILE_ELEMS * LP + e;
+            float v[LP];
+#pragma unroll
+            for (int l = 0; l < LP; ++l) v[l] = __ldg(src + (size_t)l * TILE_ELEMS);
+            const int st = i & 1;
+            wait(&ctl.a_empty[st], ((i >> 1) & 1) ^ 1);
+            if (!ok) break;
+            unsigned char* hi = sA + st * 2 * A_PLANE;
+            const uint32_t row = (uint32_t)((p >> 3) * SBO_A + (p & 7) * 16);
+#pragma unroll
+            for (int k4 = 0; k4 < LP / 4; ++k4) {
+                float4 h, lo;
+                split1(make_float4(v[4 * k4], v[4 * k4 + 1], v[4 * k4 + 2], v[4 * k4 + 3]), h, lo);
+                *reinterpret_cast<float4*>(hi + row + k4 * 128) = h;
+                *reinterpret_cast<float4*>(hi + A_PLANE + row + k4 * 128) = lo;
+            }
+            fence_proxy_async();  // the MMA reads the stage through the async proxy
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&ctl.a_full[st]);
+        }
+    } else if (warp < 8) {
+        // epilogue: row (entry) 32 (warp % 4) + lane of every row block
+        const int p = (warp - 4) * 32 + lane;
+        int i = 0;
+        for (int m = blockIdx.x; m < nblk; m += gridDim.x, ++i) {
+            const int dsel = i & 1;
+            wait(&ctl.d_full[dsel], (i >> 1) & 1);
+            if (!ok) break;
+            fence_after();
+            const int t = m / (TILE_ELEMS / 128), e = (m % (TILE_ELEMS / 128)) * 128 + p;
+            int I, J;
+            tile_coords(t, I, J);
+            const float one = (I == J && (e % TS) == (e / TS)) ? 1.f : 0.f;
+            float* dst = A + (size_t)t * TILE_ELEMS + e;
+            for (int c0 = 0; c0 < nb; c0 += 32) {
+                float v[32];
+                tmem_ld32w(tm + lane_base() + acc * dsel + c0, v);  // columns past nb: unused
+#pragma unroll
+                for (int j = 0; j < 32; ++j) {
+                    const int b = b_begin + c0 + j;
+                    if (c0 + j < nb && b < B) dst[(size_t)b * strideA] = v[j] + one;
+                }
+            }
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&ctl.d_empty[dsel]);
+        }
+    } else if (lane == 0) {
+        // the MMA issuer
+        const uint32_t idesc = idesc_tf32(128, nb);
+        const uint32_t a0 = smem_u32(sA), bh = smem_u32(sB), bl = bh + b_plane;
+        int i = 0;
+        for (int m = blockIdx.x; m < nblk; m += gridDim.x, ++i) {
+            const int st = i & 1, dsel = i & 1;
+            wait(&ctl.a_full[st], (i >> 1) & 1);
+            wait(&ctl.d_empty[dsel], ((i >> 1) & 1) ^ 1);
+            if (!ok) break;
+            fence_after();
+            const uint32_t ah = a0 + st * 2 * A_PLANE, al = ah + A_PLANE, d = tm + acc * dsel;
+#pragma unroll
+            for (int kk = 0; kk < LP / 8; ++kk) {
+                const uint32_t off = kk * 2 * LBO;
+                mma_tf32(d, smem_desc(al + off, LBO, SBO_A), smem_desc(bh + off, LBO, SBO_A), idesc, kk ? 1u : 0u);
+                mma_tf32(d, smem_desc(ah + off, LBO, SBO_A), smem_desc(bl + off, LBO, SBO_A), idesc, 1u);
+            }
+#pragma unroll
+            for (int kk = 0; kk < LP / 8; ++kk) {
+                const uint32_t off = kk * 2 * LBO;
+                mma_tf32(d, smem_desc(ah + off, LBO, SBO_A), smem_desc(bh + off, LBO, SBO_A), idesc, 1u);
+            }
+            mma_commit(&ctl.a_empty[st]);
+            mma_commit(&ctl.d_full[dsel]);
+        }
+        // every MMA issued so far completes before tensor memory is freed (bounded, ignores the abort flag)
+        mma_commit(&ctl.fin);
+        if (!mbar_wait(&ctl.fin, 0, kMaxIter)) atomicExch(err, 1);
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    if (warp == 8) tmem_dealloc(tm, 2 * acc);
+}
+
 // Self-test of the bounded-wait path: one thread waits, with a short limit, on an mbarrier
 // that nothing arrives on; the wait must give up and report CG_ERR_TIMEOUT.
 __global__ void wait_timeout_probe(int* status)
@@ -1609,14 +1777,15 @@ int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, flo
     for (int J2 = 0; J2 < nt2; ++J2) {
         // diagonal CTAs, then one CTA per off-diagonal block (J2 = 0) or persistent CTAs
         const int noff = (nt2 - J2 - 1) * B;
-        const int cap = (J2 == 0 ? 4 : 1) * ctx->sm_count;
+        const int cap = J2 == 0 ? 4 * ctx->sm_count : (ctx->tune.chol_ctas > 0 ? ctx->tune.chol_ctas : ctx->sm_count);
         const int grid = B + (noff < cap ? noff : cap);
         chol_tc_update<<<grid, NTH, tc_smem(), s>>>(J2, nt, B, A, Ls, Lc, Linv, Ms, Mc, diag, status,
                                                     d_err + 1 + nt2 + J2, d_err);
         count_launch(ctx);
         if (J2 + 1 < nt2) {
             const int items = (nt2 - J2 - 1) * B;
-            chol_tc_panel<<<items < ctx->sm_count ? items : ctx->sm_count, NTH, tc_smem(), s>>>(
+            const int pc = ctx->tune.panel_ctas > 0 ? ctx->tune.panel_ctas : ctx->sm_count;
+            chol_tc_panel<<<items < pc ? items : pc, NTH, tc_smem(), s>>>(
                 J2, nt, B, Ls, Lc, Linv, d_err + 1 + J2, d_err);
             count_launch(ctx);
         }
@@ -1673,10 +1842,54 @@ int adjoint_contract_tc(cg_ctx* ctx, int B, int nt, int lp, const float* U, cons
 {
     if (!adjoint_tc_ok(lp)) { ctx->err = "tensor-core adjoint contraction needs lp % 16 == 0, lp <= 96"; return CG_ERR_BAD_ARG; }
     const dim3 grid(ntiles_lower(nt), (B + 127) / 128);
-    int rc = (lp <= 48)   ? launch_adj_tc<24, 2, 4>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)
-             : (lp <= 64) ? launch_adj_tc<32, 2, 3>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)
-                          : launch_adj_tc<48, 2, 2>(ctx, grid, B, lp, U, V, strideA, part, d_err, s);
+    // tuning variants: fetch groups G of two chunks with NB group buffers (default), or shallower rings
+    const int v = ctx->tune.adj;
+    int rc;
+    if (lp <= 48)
+        rc = v == 1   ? launch_adj_tc<24, 2, 3>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)
+             : v == 2 ? launch_adj_tc<24, 1, 4>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)
+                      : launch_adj_tc<24, 2, 4>(ctx, grid, B, lp, U, V, strideA, part, d_err, s);
+    else if (lp <= 64)
+        rc = v == 2 ? launch_adj_tc<32, 1, 4>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)
+                    : launch_adj_tc<32, 2, 3>(ctx, grid, B, lp, U, V, strideA, part, d_err, s);
+    else
+        rc = v == 2 ? launch_adj_tc<48, 1, 3>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)
+                    : launch_adj_tc<48, 2, 2>(ctx, grid, B, lp, U, V, strideA, part, d_err, s);
     if (rc) return rc;
+    count_launch(ctx);
+    CG_CUDA_TRY(ctx, cudaGetLastError());
+    return CG_OK;
+}
+
+bool contract_fwd_tc_ok(int lp) { return lp % 16 == 0 && lp >= 16 && lp <= 64; }
+
+static size_t fwd_tc_smem(int lp, int nb) { return (size_t)2 * nb * lp * 4 + (size_t)2 * 2 * 128 * lp * 4 + 1024; }
+
+int contract_fwd_tc_launch(cg_ctx* ctx, int B, int nt, int lp, const float* U, const float* eps, float* A,
+                           size_t strideA, int* d_err, int ctas, cudaStream_t s)
+{
+    if (!contract_fwd_tc_ok(lp)) { ctx->err = "tensor-core forward contraction needs lp % 16 == 0, lp <= 64"; return CG_ERR_BAD_ARG; }
+    // batch chunk: the whole batch up to 256 (rounded up to the MMA's N step of 16), smaller where
+    // E's two planes and two A stages would not fit in shared memory
+    int nb = ((std::min(B, FWD_NBMAX) + 15) / 16) * 16;
+    while (nb > 16 && fwd_tc_smem(lp, nb) > 227 * 1024) nb -= 16;
+    const size_t smem = fwd_tc_smem(lp, nb);
+    const int nblk = ntiles_lower(nt) * (TILE_ELEMS / 128);
+    const int grid_x = std::max(1, std::min(nblk, ctas > 0 ? ctas : ctx->sm_count));
+    const dim3 grid(grid_x, (B + nb - 1) / nb);
+    switch (lp) {
+#define CG_FWD_CASE(LPV)                                                                                          \
+    case LPV:                                                                                                      \
+        CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_fwd_tc<LPV>, cudaFuncAttributeMaxDynamicSharedMemorySize,   \
+                                              (int)smem));                                                          \
+        contract_fwd_tc<LPV><<<grid, FWD_NTH, smem, s>>>(B, nblk, nb, U, eps, A, strideA, d_err);                   \
+        break;
+        CG_FWD_CASE(16)
+        CG_FWD_CASE(32)
+        CG_FWD_CASE(48)
+        CG_FWD_CASE(64)
+#undef CG_FWD_CASE
+    }
     count_launch(ctx);
     CG_CUDA_TRY(ctx, cudaGetLastError());
     return CG_OK;

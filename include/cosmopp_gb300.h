@@ -69,8 +69,31 @@ typedef struct cg_config {
     double recenter_radius;    /* max |ln(C_l / Cref_l)| before an automatic re-centre (0 = 1.0) */
 } cg_config;
 
+/* Memory admission (no counterpart in the reference, whose covariance lives in host memory).
+   The device bytes a context needs: bytes_fixed (the pixel geometry, the staging buffers of
+   max_batch elements and, for the mixed path, the FP64 reference factor and the whitened
+   Legendre table) plus bytes_per_element for every batch element in flight.  Planned against
+   bytes_budget less a reserve of 256 MB + 1% (the CUDA context, allocator rounding):
+   max_batch_fit elements fit; chunk = min(max_batch, max_batch_fit) is the piece a call's batch
+   is evaluated in (one piece after another, each its own batch; with CG_RECENTER_BATCH each
+   piece is re-centred on its own mean).  max_batch_fit = 0: nothing fits. */
+typedef struct cg_memory_plan {
+    size_t bytes_fixed;
+    size_t bytes_per_element;
+    size_t bytes_budget;
+    size_t bytes_reserve;
+    int max_batch_fit;
+    int chunk;
+} cg_memory_plan;
+
 /* ---- context ----------------------------------------------------------- */
 void cg_config_init(cg_config* cfg);
+/* The plan for a configuration before any allocation: budget_bytes = 0 plans against the free
+   memory of cfg->device (needs the device), otherwise against budget_bytes (no device needed). */
+int cg_plan_memory(const cg_config* cfg, size_t budget_bytes, cg_memory_plan* plan);
+/* The plan cg_create admitted this context with (against the device's free memory then).
+   cg_create fails with CG_ERR_ALLOC, before allocating anything, when not one element fits. */
+int cg_get_memory_plan(const cg_ctx* ctx, cg_memory_plan* plan);
 int cg_create(cg_ctx** ctx, const cg_config* cfg);
 void cg_destroy(cg_ctx* ctx);
 const char* cg_last_error(const cg_ctx* ctx);   /* ctx may be NULL: last create error */
@@ -198,6 +221,26 @@ int cg_set_profiling(cg_ctx* ctx, int enable);
 /* per-stage device milliseconds of the last profiled call: ms[7] =
    {build/contraction, cholesky, trtri, lauum, solve+refine, adjoint, 0} */
 int cg_stage_times(cg_ctx* ctx, double* ms);
+
+/* ---- launch-shape tuning of the mixed path (no counterpart in the reference) ---- */
+/* Knobs, by name: "fwd" (forward contraction: 1 = tensor cores, 0 = FP32 FMA), "fwd_ctas",
+   "chol_ctas", "panel_ctas" (persistent CTA counts of the tensor-core contraction, the Cholesky's
+   off-diagonal work queue and its panel solve; 0 = one per SM), "adj" (tensor-core adjoint
+   variant 0..2).  Values only change launch shapes, never results beyond rounding order. */
+int cg_tune_set(cg_ctx* ctx, const char* knob, int value);
+int cg_tune_get(const cg_ctx* ctx, const char* knob, int* value);
+/* "fwd=1 fwd_ctas=0 ..." of the knobs in effect */
+int cg_tune_describe(const cg_ctx* ctx, char* buf, int len);
+/* One coordinate pass over the knobs' candidate values on this context's shape at batch B
+   (median of 3 timed calls per candidate, CUDA events), keeping a change only when it is
+   faster by more than 0.5%; the result is applied and, if path is non-NULL, appended to that
+   tuning file under "<device>|n=..|lmax=..|B=..|".  *best_ms = the chosen shape's time.
+   Overwrites the context's staging buffers. */
+int cg_autotune(cg_ctx* ctx, int B, const char* path, double* best_ms);
+/* Apply the last entry of a tuning file for this device, n, lmax and B = max_batch (*found = 1),
+   or keep the current knobs (*found = 0, also when the file does not exist).  cg_create does
+   this for mixed contexts when the environment variable COSMOPP_GB300_TUNE_FILE names a file. */
+int cg_tune_load(cg_ctx* ctx, const char* path, int* found);
 
 /* ---- Likelihood drop-in (source/likelihood.cpp:38-41,69-180) ------------- */
 /* construct from packed C, fiducial (nullable = 0) and noise, with optional

@@ -127,3 +127,24 @@ def test_legendre_file_reader_and_writer_match_the_reference_format(oracle_mod, 
     short.write_bytes(open(path, "rb").read()[:100])
     with pytest.raises(cg.CGError):
         cg.LegendrePolynomialContainer(file_name=str(short))
+
+
+def test_memory_plan_without_a_device():
+    """Admission sizing against an explicit budget needs no device: the nside-32 batch of 32 fits in
+    180 GB, a budget below the fixed part admits nothing, and chunks never exceed max_batch."""
+    from cosmopp_gb300 import workload as W
+    wl = W.make("nside32_lmax95_b32")
+    kw = dict(lmax=wl.lmax, fwhm_deg=wl.fwhm_deg, nside=wl.nside, good_pixels=wl.ring_kept, scheme="RING",
+              noise_sigma=wl.sigma)
+    p = cg.plan_memory(180 * 10 ** 9, precision="mixed", max_batch=32, **kw)
+    assert p["chunk"] == 32 and p["max_batch_fit"] >= 32
+    # the whitened table alone: tiles x 4096 entries x lpad (96) x 4 bytes
+    nt = 2 * ((wl.n + 127) // 128)
+    assert p["bytes_fixed"] > nt * (nt + 1) // 2 * 4096 * 96 * 4
+    small = cg.plan_memory(p["bytes_fixed"], precision="mixed", max_batch=32, **kw)
+    assert small["max_batch_fit"] == 0 and small["chunk"] == 0
+    mid = cg.plan_memory(p["bytes_fixed"] + p["bytes_reserve"] + 5 * p["bytes_per_element"] + 10 ** 9,
+                         precision="mixed", max_batch=32, **kw)
+    assert 1 <= mid["chunk"] < 32
+    with pytest.raises(cg.CGError):
+        cg.plan_memory(10 ** 9, precision="mixed", max_batch=0, **kw)

@@ -2,16 +2,21 @@
 from the reference's own code) and with the oracle restatement.
 
 Bars: the covariance matrix is bit-identical (integer-exact comparison of
-the FP64 words); -2lnL within |delta| <= 1e-6 at nside <= 8 (FP64 Cholesky
-ordering noise is ~1e-9 there) and within 1e-6 relative at nside 16; the
-adjoint gradient within 1e-4 relative of the reference's central finite
-differences and 1e-8 relative of the oracle's FP64 adjoint."""
+the FP64 words); -2lnL, chi2 and ln det within 1e-6 absolute of the
+reference at every nside.  The FP64 rounding noise of the reference itself,
+measured against an extended-precision (long double) evaluation of the same
+covariance, is at most 2.4e-10 over 100 nside-16 vectors
+(tests/golden/config2_nside16.npz), so 1e-6 is not below the noise floor.
+The adjoint gradient is checked per component: within 1e-4 relative of the
+reference's central finite differences, and within 1e-8 of the oracle's FP64
+adjoint relative to max(|g_l|, s_l), s_l the gradient's minimum statistical
+scatter (conftest.grad_scale)."""
 import hashlib
 
 import numpy as np
 import pytest
 
-from conftest import load_golden
+from conftest import assert_grad_close, grad_scale, load_golden
 
 import cosmopp_gb300 as cg
 
@@ -63,7 +68,7 @@ def test_fiducial_matrix_bit_identical_and_low_l_flow(name):
     noise[idx * (idx + 1) // 2 + idx] = float(g["sigma"]) ** 2
     like, chi2, logdet = cg.Likelihood(c, fid, noise, good_pixels=g["nest_good"]).calculate(g["d"])
     assert abs(chi2 - float(g["chi2"])) <= 1e-6
-    assert abs(like - float(g["like_ref"])) <= 2e-6
+    assert abs(like - float(g["like_ref"])) <= 1e-6
 
 
 def test_cmatrix_batched_matches_single(oracle_mod):
@@ -83,10 +88,31 @@ def test_loglike_matches_reference(name):
     with _ctx(g, max_batch=B) as ctx:
         r = ctx.loglike(g["cls"], g["d"], grad=False)
     assert np.all(r["status"] == 0)
-    tol = 1e-6 if int(g["nside"]) <= 8 else 1e-6 * np.abs(g["m2lnl"]).max()
+    tol = 1e-6
     assert np.abs(r["logdet"] - g["logdet_raw"]).max() <= tol
     assert np.abs(r["chi2"] - g["chi2"]).max() <= tol
     assert np.abs(r["m2lnl"] - g["m2lnl"]).max() <= tol
+
+
+def test_plain_fp64_workload_100_vectors_against_reference_and_extended_precision():
+    """The plain FP64 workload at nside 16 (100 lognormal C_l vectors): every -2lnL within 1e-6 of
+    the reference's, and of the extended-precision value of the same covariance; the fixture's own
+    record of the reference's FP64 noise (strict and -ffast-math builds, restated LAPACK loops)
+    against extended precision stays below 1e-8."""
+    g = load_golden("config2_nside16")
+    B = len(g["cls"])
+    with _ctx(g, max_batch=B) as ctx:
+        r = ctx.loglike(g["cls"], g["d"], grad=False)
+    assert np.all(r["status"] == 0)
+    d_ref = np.abs(r["m2lnl"] - g["m2lnl"]).max()
+    d_ext = np.abs(r["m2lnl"] - g["m2lnl_ext"]).max()
+    print("FP64 GPU, 100 vectors: max |d(-2lnL)| vs reference %.3e, vs extended %.3e" % (d_ref, d_ext))
+    assert d_ref <= 1e-6 and d_ext <= 1e-6
+    assert np.abs(r["chi2"] - g["chi2_ext"]).max() <= 1e-6
+    assert np.abs(r["logdet"] - g["logdet_ext"]).max() <= 1e-6
+    n10 = len(g["m2lnl_fastmath"])
+    for key in ("m2lnl", "m2lnl_fastmath", "m2lnl_restated"):
+        assert np.abs(g[key][:n10] - g["m2lnl_ext"][:n10]).max() <= 1e-8, key
 
 
 @pytest.mark.parametrize("name", ["nside2", "nside4", "nside8_lmax24", "nside16_lmax47"])
@@ -94,14 +120,16 @@ def test_gradient_matches_reference_fd_and_oracle(name, oracle_mod):
     g = load_golden(name)
     with _ctx(g, max_batch=1) as ctx:
         r = ctx.loglike(g["cls"][0], g["d"], grad=True)
+        s = grad_scale(ctx, g["cls"][0], len(g["nest_good"]), int(g["lmax"]))
     grad = r["grad"]
-    scale = np.abs(g["fd_grad"]).max()
+    # the reference's central differences (step 1e-4 C_l) carry its -2lnL rounding noise (< 1e-9)
+    # over 2h and an O(h^2) truncation: both far below 1e-4 of every component here
     for ell, fd in zip(g["fd_ells"], g["fd_grad"]):
-        assert abs(grad[ell] - fd) <= 1e-4 * abs(fd) + 1e-6 * scale, (ell, grad[ell], fd)
+        assert abs(grad[ell] - fd) <= 1e-4 * abs(fd), (ell, grad[ell], fd)
     if int(g["nside"]) <= 8:
         xyz = oracle_mod.unit_vectors(int(g["nside"]), g["nest_good"], "NEST")
         e = oracle_mod.evaluate(g["cls"][0], xyz, float(g["fwhm_deg"]), float(g["sigma"]) ** 2, g["d"], grad=True)
-        assert np.abs(grad - e["grad"]).max() <= 1e-8 * np.abs(e["grad"]).max()
+        assert_grad_close(grad, e["grad"], s, 1e-8, name)
 
 
 def test_batch_elements_independent_and_per_map_data():
@@ -150,15 +178,15 @@ def test_likelihood_dropin_matches_reference(name, oracle_mod):
     like, chi2, logdet = lik.calculate(g["d"])
     assert abs(logdet - g["logdet_ref"][0]) <= 1e-6
     assert abs(chi2 - g["chi2"][0]) <= 1e-6
-    assert abs(like - g["like_ref"][0]) <= 2e-6
+    assert abs(like - g["like_ref"][0]) <= 1e-6
     # foreground marginalisation (source/likelihood.cpp:171-177) against the oracle
     fg = np.cos(3 * xyz[:, 2]) + 0.3 * xyz[:, 0]
     lik_f = cg.Likelihood(c, None, noise, foreground=fg)
     like_f, chi2_f, logdet_f = lik_f.calculate(g["d"])
     like_o, chi2_o, logdet_o, _, st = oracle_mod.likelihood(c, noise, g["d"], foreground=fg)
     assert st == 0
-    assert abs(chi2_f - chi2_o) <= 1e-6 * max(1.0, abs(chi2_o))
-    assert abs((logdet_f - cg.DET_OFFSET) - logdet_o) <= 1e-6 * max(1.0, abs(logdet_o))
+    assert abs(chi2_f - chi2_o) <= 1e-6
+    assert abs((logdet_f - cg.DET_OFFSET) - logdet_o) <= 1e-6
 
 
 def test_likelihood_dropin_rejects_indefinite():
