@@ -63,6 +63,8 @@ class _Config(ctypes.Structure):
 # int (*)(void* user, int nchains, const double* x, double* m2lnl)
 _BATCH_LIKE = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                ctypes.POINTER(ctypes.c_double))
+_BATCH_LIKE_GRAD = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                    ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double))
 
 PRIOR = {"uniform": 0, "gauss": 1}
 
@@ -98,6 +100,8 @@ def library():
                              ctypes.c_double, _dp, ctypes.c_int, ctypes.c_ulonglong, _dp, _dp]
     _mh_tail = [_dp, _ip, _dp, _dp, ctypes.c_int, _ip, ctypes.c_int, ctypes.c_ulonglong, _dp, _dp, _dp]
     L.cg_mh_sample.argtypes = [ctypes.c_int, ctypes.c_int, _BATCH_LIKE, ctypes.c_void_p, _dp, ctypes.c_int] + _mh_tail
+    L.cg_hmc_sample.argtypes = [ctypes.c_int, ctypes.c_int, _BATCH_LIKE_GRAD, ctypes.c_void_p, _dp, ctypes.c_int,
+                                ctypes.c_int, ctypes.c_double, _dp, ctypes.c_int, ctypes.c_ulonglong, _dp, _dp]
     L.cg_mh_run.argtypes = [ctypes.c_void_p, _dp, ctypes.c_int, _dp, _dp, ctypes.c_int] + _mh_tail
     L.cg_legendre_table.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp]
     L.cg_noise_matrix_from_sims.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
@@ -414,7 +418,7 @@ class Context:
         self._check(self._L.cg_selftest_wait_timeout(self._h, ctypes.byref(st)))
         return st.value
 
-    TUNE_KNOBS = ("fwd", "fwd_ctas", "chol_ctas", "panel_ctas", "adj")
+    TUNE_KNOBS = ("fwd", "fwd_ctas", "chol_ctas", "panel_ctas", "adj", "diag_sq")
 
     def tune_set(self, knob, value):
         self._check(self._L.cg_tune_set(self._h, knob.encode(), int(value)))
@@ -520,6 +524,41 @@ def mh_sample(like, x0, niter, sampling_width, priors=None, blocks=None, adapt=T
     if rc:
         raise CGError(rc, "cg_mh_sample")
     return out
+
+
+def hmc_sample(like_grad, x0, niter, nleap, tau, mass=None, jitter=False, seed=0):
+    """Batched HMC (cg_hmc_sample) over a host likelihood with gradient:
+    ``like_grad(x [nchains, npar]) -> (-2lnL [nchains], d(-2lnL)/dx [nchains, npar])``, called once
+    per leapfrog step for all chains.  Math::HMC::run's rules and random-number order
+    (source/hmc.cpp:31-126); no device is used.  Returns (chain [niter+1, nchains, npar+1]:
+    -2lnL then x, accept_rate [nchains])."""
+    L = library()
+    x0 = _f64(x0)
+    nchains, npar = x0.shape
+    failure = []
+
+    def _cb(_user, nc, xp, outp, gp):
+        try:
+            x = np.ctypeslib.as_array(xp, shape=(nc, npar))
+            m2, g = like_grad(x.copy())
+            np.ctypeslib.as_array(outp, shape=(nc,))[:] = m2
+            np.ctypeslib.as_array(gp, shape=(nc, npar))[:] = g
+            return 0
+        except Exception as e:  # surfaced after the call returns
+            failure.append(e)
+            return CG_ERR_BAD_ARG
+
+    cb = _BATCH_LIKE_GRAD(_cb)
+    chain = np.zeros((niter + 1, nchains, npar + 1))
+    acc = np.zeros(nchains)
+    m = None if mass is None else _f64(mass)
+    rc = L.cg_hmc_sample(nchains, npar, cb, None, _p(x0), int(niter), int(nleap), float(tau), _p(m),
+                         int(bool(jitter)), int(seed), _p(chain), _p(acc))
+    if failure:
+        raise failure[0]
+    if rc:
+        raise CGError(rc, "cg_hmc_sample")
+    return chain, acc
 
 
 class LegendrePolynomialContainer:

@@ -108,6 +108,7 @@ struct Tune {
     int chol_ctas = 0;    // persistent CTAs of the Cholesky's off-diagonal work queue, column blocks J > 0 (0 = one per SM)
     int panel_ctas = 0;   // persistent CTAs of the Cholesky's panel solve (0 = one per SM)
     int adj = 0;          // tensor-core adjoint variant (fetch groups / buffers), 0 .. 2
+    int diag_sq = 1;      // Cholesky diagonal blocks: row sums of squares on the CUDA cores (accuracy, not speed)
 };
 
 }  // namespace cg

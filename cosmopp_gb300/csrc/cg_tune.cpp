@@ -29,6 +29,7 @@ const Knob kKnobs[] = {
     {"chol_ctas", &cg::Tune::chol_ctas},
     {"panel_ctas", &cg::Tune::panel_ctas},
     {"adj", &cg::Tune::adj},
+    {"diag_sq", &cg::Tune::diag_sq},
 };
 
 const Knob* find_knob(const char* name)
@@ -49,13 +50,14 @@ std::vector<int> candidates(const cg_ctx* ctx, const Knob& k)
     if (k.field == &cg::Tune::chol_ctas) return {0, sm / 2, 2 * sm};
     if (k.field == &cg::Tune::panel_ctas) return {0, sm / 2, 2 * sm};
     if (k.field == &cg::Tune::adj) return {0, 1, 2};
-    return {0};
+    return {ctx->tune.*(k.field)};  // accuracy knobs are not searched
 }
 
 bool valid_value(const cg_ctx* ctx, const Knob& k, int v)
 {
     if (k.field == &cg::Tune::fwd) return v == 0 || v == 1;
     if (k.field == &cg::Tune::adj) return v >= 0 && v <= 2;
+    if (k.field == &cg::Tune::diag_sq) return v == 0 || v == 1;
     return v >= 0 && v <= 64 * std::max(1, ctx->sm_count);  // CTA counts; 0 = one per SM
 }
 

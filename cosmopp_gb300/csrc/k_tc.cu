@@ -328,8 +328,11 @@ constexpr uint32_t kMaxIter = 1u << 22;  // try_wait attempts before a wait give
 
 // chunk g's A (row r, K half h: from qx, or for A_SMEM_C1 from the shared-memory ring) into
 // tensor-memory stage g % NAST, then one arrival per warp on the stage's a_full barrier
+// ssq (nullable, B_FROM_A only): the chunk's sum of squares of this thread's 16 values, summed in
+// FP32 (round to nearest) and added to the double-float (ssq->x, ssq->y) by an exact two-sum
 template <int AMODE, int BMODE = B_COPY, int NX, class W>
-__device__ __forceinline__ void put_a(int g, float4 (&qx)[NX], W& wait, const float* sa_f, TcCtl& ctl, uint32_t tm)
+__device__ __forceinline__ void put_a(int g, float4 (&qx)[NX], W& wait, const float* sa_f, TcCtl& ctl, uint32_t tm,
+                                      float2* ssq = nullptr)
 {
     const int r = threadIdx.x % 128, h = threadIdx.x / 128, lane = threadIdx.x % 32, st = g % NAST;
     if constexpr (AMODE == A_SMEM_C1 || AMODE == A_SMEM_PRE) {
@@ -342,6 +345,22 @@ __device__ __forceinline__ void put_a(int g, float4 (&qx)[NX], W& wait, const fl
         if constexpr (AMODE == A_SMEM_C1) {
             __syncwarp();
             if (lane == 0) mbar_arrive(&ctl.as_empty[si]);
+        }
+        if constexpr (BMODE == B_FROM_A) {
+            if (ssq) {
+                float p = 0.f;
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    p = fmaf(qx[i].x, qx[i].x, p);
+                    p = fmaf(qx[i].y, qx[i].y, p);
+                    p = fmaf(qx[i].z, qx[i].z, p);
+                    p = fmaf(qx[i].w, qx[i].w, p);
+                }
+                const float t = __fadd_rn(ssq->x, p), bp = __fsub_rn(t, ssq->x);
+                const float e = __fadd_rn(__fsub_rn(ssq->x, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+                ssq->x = t;
+                ssq->y = __fadd_rn(ssq->y, e);
+            }
         }
     }
     float4 qh[4], ql[4];
@@ -453,7 +472,7 @@ __device__ __forceinline__ void copy_b(int g, W& wait, TcCtl& ctl, uint32_t sb, 
 // thread whose wait gave up skips its later waits, so a failure ends the launch quickly.
 template <int AMODE, int BMODE = B_COPY, class FA, class FB>
 __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& ctl, uint32_t tm, float (&R)[64],
-                         int* err)
+                         int* err, float2* ssq = nullptr)
 {
     static_assert(BMODE == B_COPY || AMODE == A_SMEM_C1, "B_FROM_A needs the A chunk staged in shared memory");
     bool ok = true;
@@ -479,18 +498,18 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
             if (nchunks > 1) fa(1, r, h, a1);
         }
         if (nchunks > 0) {
-            put_a<AMODE, BMODE>(0, a0, wait, sa_f, ctl, tm);
+            put_a<AMODE, BMODE>(0, a0, wait, sa_f, ctl, tm, ssq);
             if constexpr (REG) { if (nchunks > 2) fa(2, r, h, a0); }
         }
         if (nchunks > 1) {
-            put_a<AMODE, BMODE>(1, a1, wait, sa_f, ctl, tm);
+            put_a<AMODE, BMODE>(1, a1, wait, sa_f, ctl, tm, ssq);
             if constexpr (REG) { if (nchunks > 3) fa(3, r, h, a1); }
         }
         // step c: chunk c - 2 is retired and its A stage takes chunk c + 2 (held in slot qx = c & 1)
         auto step = [&](int c, float4 (&qx)[NX]) {
             if (c >= 2) retire_acc(c - 2, false, (c & 1) != 0, wait, ok, err, ctl, tm, R);
             if (c + 2 < nchunks) {
-                put_a<AMODE, BMODE>(c + 2, qx, wait, sa_f, ctl, tm);
+                put_a<AMODE, BMODE>(c + 2, qx, wait, sa_f, ctl, tm, ssq);
                 if constexpr (REG) { if (c + 4 < nchunks) fa(c + 4, r, h, qx); }
             }
         };
@@ -996,10 +1015,11 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
                                                          float* __restrict__ Linv, float* __restrict__ Ms,
                                                          float* __restrict__ Mc, float* __restrict__ diag,
                                                          int* __restrict__ status, int* __restrict__ queue,
-                                                         int* __restrict__ err)
+                                                         int* __restrict__ err, int diag_sq)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ TcCtl ctl;
+    __shared__ float2 sq[2][128];   // diagonal blocks: sum over K of L_rk^2, per row and K half
     const int nt2 = nt / 2, noff = nt2 - J2 - 1;
     const size_t ntile = (size_t)ntiles_lower(nt);
     const int row = threadIdx.x % 128, h = threadIdx.x / 128;
@@ -1056,9 +1076,16 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
         bot = Lcb + (size_t)tile_index(2 * I2 + 1, c / 2) * C1_TILE;
         kc = c % 2;
     };
-    // B = A (S_JJ = A_JJ - L_J L_J^T): the producers copy the split A chunk into the B stage
+    // B = A (S_JJ = A_JJ - L_J L_J^T): the producers copy the split A chunk into the B stage.  The
+    // tensor core's FP32 accumulation rounds one way, so its sums of squares on the diagonal of
+    // L_J L_J^T come out low by a fraction of an ulp per MMA, every one in the same direction; over
+    // the n pivots that biases ln det upwards, by up to ~1e-3 at nside 16 for C_l far from the
+    // reference point.  With diag_sq the producers also sum each row's squares on the CUDA cores
+    // (round to nearest, double-float across chunks) and those sums replace the diagonal.
     auto fb = [](int, uint32_t, uint64_t*) {};
-    tc_kloop<A_SMEM_C1, B_FROM_A>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
+    float2 ssq = make_float2(0.f, 0.f);
+    tc_kloop<A_SMEM_C1, B_FROM_A>(nchunks, fa, fb, smem_raw, ctl, tm, R, err, diag_sq ? &ssq : nullptr);
+    if (prod) sq[h][row] = ssq;
     // diagonal block: S = A_JJ - P into shared memory (column-major, ld 129), lower part
     float* s = reinterpret_cast<float*>(smem_raw);
     float* inv = s + 128 * 129;
@@ -1070,6 +1097,11 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
             const float* t = Ab + (size_t)tile_index(ti, tj) * TILE_ELEMS;
 #pragma unroll
             for (int j = 0; j < 64; ++j) s[(64 * h + j) * 129 + row] = t[(row % 64) + TS * j] - R[j];
+            if (diag_sq && h == row / 64) {
+                const double p = ((double)sq[0][row].x + (double)sq[1][row].x) +
+                                 ((double)sq[0][row].y + (double)sq[1][row].y);
+                s[row * 129 + row] = (float)((double)t[(row % 64) + TS * (row % 64)] - p);
+            }
         }
     }
     __syncthreads();
@@ -1780,7 +1812,7 @@ int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, flo
         const int cap = J2 == 0 ? 4 * ctx->sm_count : (ctx->tune.chol_ctas > 0 ? ctx->tune.chol_ctas : ctx->sm_count);
         const int grid = B + (noff < cap ? noff : cap);
         chol_tc_update<<<grid, NTH, tc_smem(), s>>>(J2, nt, B, A, Ls, Lc, Linv, Ms, Mc, diag, status,
-                                                    d_err + 1 + nt2 + J2, d_err);
+                                                    d_err + 1 + nt2 + J2, d_err, ctx->tune.diag_sq);
         count_launch(ctx);
         if (J2 + 1 < nt2) {
             const int items = (nt2 - J2 - 1) * B;

@@ -170,6 +170,18 @@ int cg_reference_count(const cg_ctx* ctx);
 int cg_hmc_run(cg_ctx* ctx, const double* map, int nchains, const double* x0, const double* cl_template,
                int niter, int nleap, double tau, const double* mass, int jitter, unsigned long long seed,
                double* chain, double* accept_rate);
+/* A batched likelihood with gradient: -2lnL of nchains parameter vectors x [nchains][npar] into
+   m2lnl [nchains] and d(-2lnL)/dx into grad [nchains][npar]; returns CG_OK or an error code that
+   ends the run.  The batched form of LikelihoodWithDerivs (include/likelihood_function.hpp:30-47). */
+typedef int (*cg_batch_like_grad_fn)(void* user, int nchains, const double* x, double* m2lnl, double* grad);
+/* The sampler of cg_hmc_run over any batched likelihood with gradient (Math::HMC::run,
+   source/hmc.cpp:31-126, over many chains): chain [niter+1][nchains][npar+1] holds -2lnL then x.
+   Random numbers: std::mt19937(seed) through uniform_real_distribution(0, 1) and
+   normal_distribution(0, 1) in the reference's order, so nchains = 1 with jitter != 0 reproduces
+   Math::HMC(npar, like, root, tau, nleap, seed) with unit masses and the same start.  Needs no device. */
+int cg_hmc_sample(int nchains, int npar, cg_batch_like_grad_fn like, void* user, const double* x0, int niter,
+                  int nleap, double tau, const double* mass, int jitter, unsigned long long seed, double* chain,
+                  double* accept_rate);
 
 /* ---- batched Metropolis-Hastings (MetropolisHastings::run, source/mcmc.cpp:455-700) ---- */
 #define CG_PRIOR_UNIFORM 0    /* 1/(max - min) on [p1 = min, p2 = max] (include/mcmc.hpp:350-357) */

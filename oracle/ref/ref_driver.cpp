@@ -15,6 +15,7 @@
 #include <utils.hpp>
 #include <test_legendre.hpp>
 #include <test_matrix.hpp>
+#include <hmc.hpp>
 
 static std::string g_err;
 
@@ -194,4 +195,56 @@ extern "C" int ref_run_subtest(const char* which, int i, double* res, double* ex
         else return 2;
         return 0;
     } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
+/* Math::HMC::run (source/hmc.cpp:31-126), unmodified, on an analytic Gaussian
+   -2lnL = sum_i ((x_i - mu_i) / sig_i)^2 with unit masses and starting point `start`.  Records,
+   at full precision, every point where the reference evaluated the derivative, except the
+   re-evaluation at the current point that opens each iteration (the batched sampler keeps
+   that gradient from the previous step instead): the leapfrog positions in order, into
+   pts [max_pts][n].  Returns their count (or -1); the chain file the reference writes is
+   root + ".txt". */
+namespace {
+class RefGauss : public Math::LikelihoodWithDerivs {
+public:
+    RefGauss(int n, const double* mu, const double* sig) : mu_(mu, mu + n), sig_(sig, sig + n) {}
+    double calculate(double* p, int n) override
+    {
+        after_calc_ = true;
+        double s = 0;
+        for (int i = 0; i < n; ++i) {
+            const double d = (p[i] - mu_[i]) / sig_[i];
+            s += d * d;
+        }
+        return s;
+    }
+    double calculateDeriv(double* p, int n, int i) override
+    {
+        if (i == 0) {
+            if (!after_calc_) pts.insert(pts.end(), p, p + n);
+            after_calc_ = false;
+        }
+        return 2 * (p[i] - mu_[i]) / (sig_[i] * sig_[i]);
+    }
+    std::vector<double> pts;
+
+private:
+    std::vector<double> mu_, sig_;
+    bool after_calc_ = true;  // the first derivative call (at the start) follows the first calculate
+};
+}  // namespace
+
+extern "C" int ref_hmc_gaussian(int n, const double* mu, const double* sig, const double* start, double tau_max,
+                                int n_max, unsigned int seed, int iters, const char* root, double* pts, int max_pts)
+{
+    try {
+        RefGauss like(n, mu, sig);
+        Math::HMC hmc(n, like, root, tau_max, n_max, (time_t)seed);
+        for (int i = 0; i < n; ++i) hmc.setParam(i, "x" + std::to_string(i), 1.0, start[i]);
+        hmc.run(iters);
+        const int cnt = (int)(like.pts.size() / n);
+        for (int k = 0; k < cnt && k < max_pts; ++k)
+            for (int i = 0; i < n; ++i) pts[(size_t)k * n + i] = like.pts[(size_t)k * n + i];
+        return cnt;
+    } catch (std::exception& e) { g_err = e.what(); return -1; }
 }

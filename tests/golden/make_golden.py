@@ -29,8 +29,11 @@ them through ctypes.  Every number stored below comes from the reference:
   evaluation of the same FP64 covariance, the yardstick all of them are
   measured against.
 
+* Math::HMC's chain on an analytic Gaussian (the reference's sampler, driven by
+  the reference's own code), with every leapfrog position at full precision.
+
 Usage:  python tests/golden/make_golden.py [part ...]   (parts: main, fiducial,
-legendre, files, config2; default all)
+legendre, files, config2, hmc; default all)
 """
 import ctypes
 import hashlib
@@ -230,6 +233,33 @@ def config2_cases():
                                               np.abs(restated - m2_ext[:nsub]).max()))
 
 
+def hmc_cases():
+    """Math::HMC::run (source/hmc.cpp:31-126), the reference's own code, on an analytic Gaussian:
+    the leapfrog positions at full precision and the chain file it writes (6 significant digits)."""
+    import tempfile
+    R = O.ref()
+    dp_ = ctypes.POINTER(ctypes.c_double)
+    R.ref_hmc_gaussian.argtypes = [ctypes.c_int, dp_, dp_, dp_, ctypes.c_double, ctypes.c_int, ctypes.c_uint,
+                                   ctypes.c_int, ctypes.c_char_p, dp_, ctypes.c_int]
+    n = 5
+    mu = np.array([0.3, -1.0, 2.0, 0.0, 0.5])
+    sig = np.array([1.0, 0.5, 2.0, 0.3, 1.5])
+    start = mu + np.array([0.5, -0.2, 1.0, 0.1, -0.7])
+    out = {}
+    for tag, tau, nmax, seed, iters in (("a", 0.3, 10, 12345, 50), ("b", 0.58, 12, 777, 60)):
+        pts = np.zeros((20000, n))
+        root = os.path.join(tempfile.mkdtemp(), "hmc")
+        cnt = R.ref_hmc_gaussian(n, mu.ctypes.data_as(dp_), sig.ctypes.data_as(dp_), start.ctypes.data_as(dp_), tau,
+                                 nmax, seed, iters, root.encode(), pts.ctypes.data_as(dp_), len(pts))
+        assert 0 < cnt <= len(pts), R.ref_last_error()
+        ch = np.loadtxt(root + ".txt")
+        out.update({tag + "_tau": tau, tag + "_nmax": nmax, tag + "_seed": seed, tag + "_iters": iters,
+                    tag + "_points": pts[:cnt].copy(), tag + "_chain_file": ch})
+        acc = np.mean(np.any(np.diff(ch[:, 2:], axis=0) != 0, axis=1))
+        print("hmc %s: %d leapfrog points, acceptance %.2f" % (tag, cnt, acc))
+    np.savez_compressed(os.path.join(HERE, "hmc_gaussian_reference.npz"), mu=mu, sig=sig, start=start, **out)
+
+
 def main(parts):
     if not O.ref_available():
         raise SystemExit("build the reference first: make -C oracle/ref")
@@ -242,6 +272,8 @@ def main(parts):
     R.ref_read_cl.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_int, dp, ctypes.c_int]
     if "config2" in parts:
         config2_cases()
+    if "hmc" in parts:
+        hmc_cases()
     if "legendre" in parts:
         legendre_cases(R)
     if "files" in parts:
@@ -302,4 +334,4 @@ def main(parts):
 
 
 if __name__ == "__main__":
-    main(set(sys.argv[1:]) or {"main", "fiducial", "legendre", "files", "config2"})
+    main(set(sys.argv[1:]) or {"main", "fiducial", "legendre", "files", "config2", "hmc"})
