@@ -45,6 +45,8 @@ def parse():
                     help="elements the plain FP64 path evaluates for the mixed/FP64 ratio and the error bars "
                          "(default: the whole batch)")
     ap.add_argument("--workload", default=WORKLOAD, help="named workload in cosmopp_gb300.workload.WORKLOADS")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the library's default launch shapes (or the tuning file's) instead of autotuning")
     ap.add_argument("--hmc-iters", type=int, default=12, help="batched-HMC iterations reported beside the line "
                                                               "(64 chains x 20 leapfrog steps of 0.05); 0 = skip")
     return ap.parse_args()
@@ -235,8 +237,9 @@ def run_ours(args):
                                                                                "tune.txt")
         t0 = time.perf_counter()
         found = ctx.tune_load(tune_file)
-        tune_ms = None if found else ctx.autotune(B, tune_file)
-        tuning = {"knobs": ctx.tuning(), "source": "tuning file" if found else "autotuned in this run",
+        tune_ms = None if (found or args.no_autotune) else ctx.autotune(B, tune_file)
+        tuning = {"knobs": ctx.tuning(),
+                  "source": "tuning file" if found else ("defaults" if args.no_autotune else "autotuned in this run"),
                   "file": os.path.relpath(tune_file, ROOT), "autotune_ms_per_call": tune_ms,
                   "seconds": round(time.perf_counter() - t0, 2)}
     plan = ctx.memory_plan()

@@ -16,6 +16,9 @@
 #include <test_legendre.hpp>
 #include <test_matrix.hpp>
 #include <hmc.hpp>
+#include <whole_matrix.hpp>
+#include <fstream>
+#include <unistd.h>
 
 static std::string g_err;
 
@@ -247,4 +250,44 @@ extern "C" int ref_hmc_gaussian(int n, const double* mu, const double* sig, cons
             for (int i = 0; i < n; ++i) pts[(size_t)k * n + i] = like.pts[(size_t)k * n + i];
         return cnt;
     } catch (std::exception& e) { g_err = e.what(); return -1; }
+}
+
+/* LikelihoodPolarization (source/likelihood.cpp:341-401, 536-612), unmodified: the constructor
+   reads n_inv.txt (written here, in directory `dir`, from ninv [size][size] row-major) and
+   factors cInv = N^-1 + N^-1 C N^-1 over the Q and U rows of the kept pixels; calculate() is
+   then run with all-zero TT a_lm, so its E-mode template is zero (the shim's rotation and
+   synthesis map zero coefficients to zero maps and refuse anything else): chi2 = v^T cInv^-1 v,
+   logdet = the reference's (with its detOffset).  size = 2 npix; lmax >= 2 sizes the unused
+   ET(TT)^-1 matrix. */
+extern "C" int ref_likelihood_pol(int size, const double* c_packed, const double* ninv, const int* good, int ngood,
+                                  long nside, int lmax, const double* v, const char* dir, double* chi2, double* logdet)
+{
+    try {
+        const std::string path = std::string(dir) + "/n_inv.txt";
+        {
+            std::ofstream out(path.c_str());
+            out.precision(17);
+            for (int i = 0; i < size; ++i) {
+                for (int j = 0; j < size; ++j) out << ninv[(size_t)i * size + j] << (j + 1 < size ? " " : "\n");
+            }
+        }
+        char cwd[4096];
+        if (!getcwd(cwd, sizeof cwd)) { g_err = "getcwd"; return 1; }
+        if (chdir(dir) != 0) { g_err = "chdir"; return 1; }
+        CMatrix c(size);
+        for (int j = 0; j < size; ++j)
+            for (int i = 0; i <= j; ++i) c.element(i, j) = c_packed[(long)j * (j + 1) / 2 + i];
+        std::vector<int> g(good, good + ngood);
+        WholeMatrix ettt(2, lmax);
+        int rc = 0;
+        try {
+            LikelihoodPolarization like(c, nside, g, lmax, ettt);
+            LikelihoodPolarization::AlmType alm(lmax, lmax);
+            alm.SetToZero();
+            std::vector<double> vv(v, v + 2 * ngood);
+            like.calculate(vv, alm, *chi2, *logdet);
+        } catch (std::exception& e) { g_err = e.what(); rc = 1; }
+        if (chdir(cwd) != 0) { g_err = "chdir back"; return 1; }
+        return rc;
+    } catch (std::exception& e) { g_err = e.what(); return 1; }
 }

@@ -9,6 +9,8 @@
 #include <stdexcept>
 #include <cstddef>
 
+#include "../../healpix_pix.h"
+
 typedef std::size_t tsize;
 enum Healpix_Ordering_Scheme { RING, NEST };
 enum nside_dummy { SET_NSIDE };
@@ -78,7 +80,15 @@ public:
     const T& operator[](long i) const { return map_[i]; }
     const std::vector<T>& Map() const { return map_; }
     void Import(const Healpix_Map<T>&) { cg_shim_unavailable("Healpix_Map::Import"); }
-    void swap_scheme() { cg_shim_unavailable("Healpix_Map::swap_scheme"); }
+    // RING <-> NEST permutation with the shim's pixel functions (Gorski et al. 2005)
+    void swap_scheme()
+    {
+        std::vector<T> out(map_.size());
+        for (long i = 0; i < (long)map_.size(); ++i)
+            out[scheme_ == RING ? hp_ring2nest(nside_, i) : hp_nest2ring(nside_, i)] = map_[i];
+        map_.swap(out);
+        scheme_ = scheme_ == RING ? NEST : RING;
+    }
     long ang2pix(const struct pointing&) const { cg_shim_unavailable("ang2pix"); return 0; }
     struct pointing pix2ang(long) const;
     T interpolated_value(const struct pointing&) const { cg_shim_unavailable("interpolated_value"); return T(); }
@@ -96,6 +106,7 @@ public:
     T& operator()(int l, int m) { return a_[(tsize)l * (lmax_ + 1) + m]; }
     const T& operator()(int l, int m) const { return a_[(tsize)l * (lmax_ + 1) + m]; }
     void SetToZero() { for (auto& x : a_) x = T(); }
+    bool all_zero() const { for (const auto& x : a_) if (x != T()) return false; return true; }
     template<typename S> void ScaleL(const arr<S>&) { cg_shim_unavailable("Alm::ScaleL"); }
     template<typename S> void Scale(const S& f) { for (auto& x : a_) x *= f; }
 private:

@@ -30,10 +30,12 @@ them through ctypes.  Every number stored below comes from the reference:
   measured against.
 
 * Math::HMC's chain on an analytic Gaussian (the reference's sampler, driven by
-  the reference's own code), with every leapfrog position at full precision.
+  the reference's own code), with every leapfrog position at full precision;
+* LikelihoodPolarization's chi2 and logDet for random Q/U inputs with a zero TT
+  template (the shim maps zero harmonic coefficients to zero maps only).
 
 Usage:  python tests/golden/make_golden.py [part ...]   (parts: main, fiducial,
-legendre, files, config2, hmc; default all)
+legendre, files, config2, hmc, pol; default all)
 """
 import ctypes
 import hashlib
@@ -260,6 +262,48 @@ def hmc_cases():
     np.savez_compressed(os.path.join(HERE, "hmc_gaussian_reference.npz"), mu=mu, sig=sig, start=start, **out)
 
 
+def pol_case_inputs(seed, npix=192, keep=0.8):
+    """The Q/U test inputs (tests/test_gpu_pol.py): a random positive-definite (2 npix)-pixel
+    covariance, a random positive-definite inverse noise matrix, a Bernoulli mask."""
+    rng = np.random.default_rng(seed)
+    size = 2 * npix
+    a = rng.standard_normal((size, size)) / np.sqrt(size)
+    c = a @ a.T + 0.5 * np.eye(size)
+    b = rng.standard_normal((size, size)) / np.sqrt(size)
+    ninv = b @ b.T + 2.0 * np.eye(size)
+    good = np.flatnonzero(rng.uniform(size=npix) < keep).astype(np.int32)
+    c_packed = np.concatenate([c[:j + 1, j] for j in range(size)])
+    return rng, npix, good, c_packed, ninv
+
+
+def pol_cases():
+    """LikelihoodPolarization's constructor and calculate (source/likelihood.cpp:341-401,536-612), the
+    reference's own code, with a zero TT a_lm (zero E-mode template): chi2 and logDet of three maps."""
+    import tempfile
+    R = O.ref()
+    dp_, ip_ = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int)
+    R.ref_likelihood_pol.argtypes = [ctypes.c_int, dp_, dp_, ip_, ctypes.c_int, ctypes.c_long, ctypes.c_int, dp_,
+                                     ctypes.c_char_p, dp_, dp_]
+    rng, npix, good, c_packed, ninv = pol_case_inputs(3)
+    ninv = np.ascontiguousarray(ninv)
+    vs, chi2s, lds = [], [], []
+    for k in range(3):
+        v = rng.standard_normal(2 * len(good))
+        chi2, ld = ctypes.c_double(), ctypes.c_double()
+        rc = R.ref_likelihood_pol(2 * npix, c_packed.ctypes.data_as(dp_), ninv.ctypes.data_as(dp_),
+                                  good.ctypes.data_as(ip_), len(good), 4, 4, v.ctypes.data_as(dp_),
+                                  tempfile.mkdtemp().encode(), ctypes.byref(chi2), ctypes.byref(ld))
+        assert rc == 0, R.ref_last_error()
+        vs.append(v)
+        chi2s.append(chi2.value)
+        lds.append(ld.value)
+    digest = hashlib.sha256(c_packed.tobytes() + ninv.tobytes() + good.tobytes()).hexdigest()
+    np.savez_compressed(os.path.join(HERE, "pol_nside4_reference.npz"), seed=3, npix=npix, good=good, v=np.array(vs),
+                        chi2=np.array(chi2s), logdet_ref=np.array(lds), det_offset=16078.083180,
+                        inputs_sha256=np.array(digest))
+    print("pol: chi2", chi2s, "logDet", lds)
+
+
 def main(parts):
     if not O.ref_available():
         raise SystemExit("build the reference first: make -C oracle/ref")
@@ -274,6 +318,8 @@ def main(parts):
         config2_cases()
     if "hmc" in parts:
         hmc_cases()
+    if "pol" in parts:
+        pol_cases()
     if "legendre" in parts:
         legendre_cases(R)
     if "files" in parts:
@@ -334,4 +380,4 @@ def main(parts):
 
 
 if __name__ == "__main__":
-    main(set(sys.argv[1:]) or {"main", "fiducial", "legendre", "files", "config2", "hmc"})
+    main(set(sys.argv[1:]) or {"main", "fiducial", "legendre", "files", "config2", "hmc", "pol"})

@@ -37,6 +37,24 @@ def test_pol_likelihood_matches_oracle(oracle_mod):
     lik.close()
 
 
+def test_pol_likelihood_matches_the_reference_itself():
+    """Against the reference's own compiled LikelihoodPolarization (fixture from make_golden.py,
+    part pol: its constructor fed n_inv.txt, calculate run with a zero TT a_lm, so the E-mode
+    template is zero): chi2 and the raw ln det of three maps."""
+    import hashlib
+    from conftest import load_golden
+    g = load_golden("pol_nside4_reference")
+    _, npix, good, c_packed, ninv = _case(int(g["seed"]))
+    ninv = np.ascontiguousarray(ninv)
+    assert hashlib.sha256(c_packed.tobytes() + ninv.tobytes() + good.tobytes()).hexdigest() == str(g["inputs_sha256"])
+    lik = cg.LikelihoodPolarization(c_packed, npix, good, ninv)
+    for v, chi2_r, ld_r in zip(g["v"], g["chi2"], g["logdet_ref"]):
+        like, chi2, logdet = lik.calculate(v, np.zeros_like(v))
+        assert abs(chi2 - chi2_r) <= 1e-9 * max(1.0, abs(chi2_r)), (chi2, chi2_r)
+        assert abs(logdet - ld_r) <= 1e-9 * max(1.0, abs(ld_r)), (logdet, ld_r)
+    lik.close()
+
+
 def test_pol_likelihood_rejects_indefinite():
     _, npix, good, c_packed, ninv = _case(5, npix=48)
     with pytest.raises(cg.CGError) as e:

@@ -154,3 +154,24 @@ def test_oracle_legendre_table_matches_reference_file(oracle_mod):
     xyz = oracle_mod.unit_vectors(int(g["nside"]), g["nest_good"], "NEST")
     assert np.array_equal(oracle_mod.legendre_table(lmax, xyz), tab)
     assert np.array_equal(g["c_lp"], g["c_plain"])
+
+
+def test_oracle_pol_algebra_matches_the_reference_itself(oracle_mod):
+    """The oracle's numpy restatement of LikelihoodPolarization's pixel algebra against the
+    reference's own compiled class (fixture: make_golden.py, part pol; zero E-mode template)."""
+    import hashlib
+    g = load_golden("pol_nside4_reference")
+    rng = np.random.default_rng(int(g["seed"]))
+    npix = int(g["npix"])
+    size = 2 * npix
+    a = rng.standard_normal((size, size)) / np.sqrt(size)
+    c = a @ a.T + 0.5 * np.eye(size)
+    b = rng.standard_normal((size, size)) / np.sqrt(size)
+    ninv = np.ascontiguousarray(b @ b.T + 2.0 * np.eye(size))
+    good = np.flatnonzero(rng.uniform(size=npix) < 0.8).astype(np.int32)
+    c_packed = np.concatenate([c[:j + 1, j] for j in range(size)])
+    assert hashlib.sha256(c_packed.tobytes() + ninv.tobytes() + good.tobytes()).hexdigest() == str(g["inputs_sha256"])
+    for v, chi2_r, ld_r in zip(g["v"], g["chi2"], g["logdet_ref"]):
+        chi2, ld = oracle_mod.likelihood_pol(c_packed, npix, good, ninv, v, np.zeros_like(v))
+        assert abs(chi2 - chi2_r) <= 1e-9 * abs(chi2_r)
+        assert abs((ld - float(g["det_offset"])) - ld_r) <= 1e-9 * abs(ld_r)
