@@ -419,6 +419,7 @@ class Context:
         return st.value
 
     TUNE_KNOBS = ("fwd", "fwd_ctas", "chol_ctas", "panel_ctas", "adj", "diag_sq")
+    ACCURACY_KNOBS = ("fwd", "diag_sq")   # never changed by autotune
 
     def tune_set(self, knob, value):
         self._check(self._L.cg_tune_set(self._h, knob.encode(), int(value)))

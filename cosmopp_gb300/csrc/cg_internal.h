@@ -103,7 +103,11 @@ struct MixedWork {
 
 // ---- launch-shape knobs of the mixed path (set by cg_tune_set / cg_autotune / a tuning file) ----
 struct Tune {
-    int fwd = 1;          // forward contraction: 0 = FP32 FMA (contract_fwd), 1 = tensor cores (contract_fwd_tc)
+    // forward contraction: 0 = FP32 FMA (contract_fwd, round to nearest), 1 = tensor cores
+    // (contract_fwd_tc): faster, but the tensor core's one-way FP32 accumulation biases A's entries
+    // by a few ulp of |A - I|, which grows with |C_l / C_ref,l - 1| (1.3e-3 in -2lnL at nside 16
+    // for C_l = C_ref / e); an accuracy choice, not searched by the autotuner
+    int fwd = 0;
     int fwd_ctas = 0;     // persistent CTAs of the tensor-core contraction (0 = one per SM)
     int chol_ctas = 0;    // persistent CTAs of the Cholesky's off-diagonal work queue, column blocks J > 0 (0 = one per SM)
     int panel_ctas = 0;   // persistent CTAs of the Cholesky's panel solve (0 = one per SM)

@@ -5,7 +5,9 @@
 // covariance and likelihood run on the CPU with no launch shapes to choose.
 //
 // File format, one entry per line (later lines for the same key win):
-//   <device name>|n=<n>|lmax=<lmax>|B=<B>| fwd=1 fwd_ctas=0 chol_ctas=0 panel_ctas=0 adj=0 ms=31.5
+//   <device name>|n=<n>|lmax=<lmax>|B=<B>| fwd=0 fwd_ctas=0 chol_ctas=0 panel_ctas=0 adj=0 diag_sq=1 ms=31.5
+// The search covers the launch-shape knobs only (CTA counts, the adjoint's fetch variant); the
+// knobs that change rounding (fwd, diag_sq) keep the values they have.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -45,12 +47,12 @@ std::vector<int> candidates(const cg_ctx* ctx, const Knob& k)
 {
     const int sm = ctx->sm_count;
     const int lp = ((ctx->lmax + 1 + 15) / 16) * 16;
-    if (k.field == &cg::Tune::fwd) return cg::contract_fwd_tc_ok(lp) ? std::vector<int>{1, 0} : std::vector<int>{0};
+    (void)lp;
     if (k.field == &cg::Tune::fwd_ctas) return {0, sm * 3 / 4, sm / 2};
     if (k.field == &cg::Tune::chol_ctas) return {0, sm / 2, 2 * sm};
     if (k.field == &cg::Tune::panel_ctas) return {0, sm / 2, 2 * sm};
     if (k.field == &cg::Tune::adj) return {0, 1, 2};
-    return {ctx->tune.*(k.field)};  // accuracy knobs are not searched
+    return {ctx->tune.*(k.field)};  // accuracy knobs (fwd, diag_sq) are not searched
 }
 
 bool valid_value(const cg_ctx* ctx, const Knob& k, int v)

@@ -235,15 +235,19 @@ int cg_set_profiling(cg_ctx* ctx, int enable);
 int cg_stage_times(cg_ctx* ctx, double* ms);
 
 /* ---- launch-shape tuning of the mixed path (no counterpart in the reference) ---- */
-/* Knobs, by name: "fwd" (forward contraction: 1 = tensor cores, 0 = FP32 FMA), "fwd_ctas",
+/* Knobs, by name.  Launch shapes (results change only in rounding order): "fwd_ctas",
    "chol_ctas", "panel_ctas" (persistent CTA counts of the tensor-core contraction, the Cholesky's
    off-diagonal work queue and its panel solve; 0 = one per SM), "adj" (tensor-core adjoint
-   variant 0..2).  Values only change launch shapes, never results beyond rounding order. */
+   variant 0..2).  Accuracy choices, never changed by cg_autotune: "fwd" (forward contraction:
+   0 = FP32 FMA, the default; 1 = tensor cores, faster, but its one-way accumulation rounding
+   biases the whitened matrix by a few ulp of |A - I|, about 1e-3 in -2lnL at nside 16 for C_l
+   a factor e from the reference point), "diag_sq" (1, the default: the Cholesky's diagonal
+   blocks take their row sums of squares from the CUDA cores rather than the tensor core). */
 int cg_tune_set(cg_ctx* ctx, const char* knob, int value);
 int cg_tune_get(const cg_ctx* ctx, const char* knob, int* value);
 /* "fwd=1 fwd_ctas=0 ..." of the knobs in effect */
 int cg_tune_describe(const cg_ctx* ctx, char* buf, int len);
-/* One coordinate pass over the knobs' candidate values on this context's shape at batch B
+/* One coordinate pass over the launch-shape knobs' candidate values on this context's shape at batch B
    (median of 3 timed calls per candidate, CUDA events), keeping a change only when it is
    faster by more than 0.5%; the result is applied and, if path is non-NULL, appended to that
    tuning file under "<device>|n=..|lmax=..|B=..|".  *best_ms = the chosen shape's time.

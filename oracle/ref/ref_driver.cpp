@@ -16,6 +16,7 @@
 #include <test_legendre.hpp>
 #include <test_matrix.hpp>
 #include <hmc.hpp>
+#include <alm_healpix_tools.h>
 #include <whole_matrix.hpp>
 #include <fstream>
 #include <unistd.h>
@@ -290,4 +291,36 @@ extern "C" int ref_likelihood_pol(int size, const double* c_packed, const double
         if (chdir(cwd) != 0) { g_err = "chdir back"; return 1; }
         return rc;
     } catch (std::exception& e) { g_err = e.what(); return 1; }
+}
+
+/* CMatrixGenerator::calculateNoiseMatrix (source/c_matrix_generator.cpp:789-929), unmodified, at
+   one resolution and beam (nSideOriginal = nSide, fwhmOriginal = fwhm), where the shim's harmonic
+   round trip hands each simulated map on unchanged and records it.  mask [12 nside^2] (NEST,
+   kept where > 0.5) and nobs [12 nside^2] go into the text files the reference reads (in `dir`);
+   out_packed receives the reference's noise matrix over the kept pixels, sims [nsims][12 nside^2]
+   (RING order, as synthesised) the maps it averaged; returns the number of maps (or -1). */
+extern "C" int ref_noise_matrix(long nside, const double* mask, const double* nobs, double sigma0, double fwhm_deg,
+                                const char* dir, double* out_packed, double* sims, int max_sims)
+{
+    try {
+        const long npix = 12 * nside * nside;
+        const std::string mpath = std::string(dir) + "/mask.txt", npath = std::string(dir) + "/noise.txt";
+        {
+            std::ofstream m(mpath.c_str());
+            m.precision(17);
+            m << nside << " 1\n";
+            for (long i = 0; i < npix; ++i) m << mask[i] << "\n";
+            std::ofstream nf(npath.c_str());
+            nf.precision(17);
+            for (long i = 0; i < npix; ++i) nf << i << " 0 " << nobs[i] << "\n";
+        }
+        cg_shim_synthesised_maps().clear();
+        CMatrix* nm = CMatrixGenerator::calculateNoiseMatrix(mpath.c_str(), npath.c_str(), sigma0, fwhm_deg, nside, fwhm_deg);
+        copy_packed(*nm, out_packed);
+        delete nm;
+        const std::vector<std::vector<double> >& rec = cg_shim_synthesised_maps();
+        for (size_t k = 0; k < rec.size() && (int)k < max_sims; ++k)
+            for (long i = 0; i < npix; ++i) sims[k * npix + i] = rec[k][i];
+        return (int)rec.size();
+    } catch (std::exception& e) { g_err = e.what(); return -1; }
 }

@@ -32,10 +32,13 @@ them through ctypes.  Every number stored below comes from the reference:
 * Math::HMC's chain on an analytic Gaussian (the reference's sampler, driven by
   the reference's own code), with every leapfrog position at full precision;
 * LikelihoodPolarization's chi2 and logDet for random Q/U inputs with a zero TT
-  template (the shim maps zero harmonic coefficients to zero maps only).
+  template (the shim maps zero harmonic coefficients to zero maps only);
+* calculateNoiseMatrix's noise matrix and the 1000 simulated maps it averaged
+  (the shim passes each map through the harmonic round trip unchanged, at one
+  resolution and beam, and records it).
 
 Usage:  python tests/golden/make_golden.py [part ...]   (parts: main, fiducial,
-legendre, files, config2, hmc, pol; default all)
+legendre, files, config2, hmc, pol, noise; default all)
 """
 import ctypes
 import hashlib
@@ -304,6 +307,35 @@ def pol_cases():
     print("pol: chi2", chi2s, "logDet", lds)
 
 
+def noise_cases():
+    """CMatrixGenerator::calculateNoiseMatrix (source/c_matrix_generator.cpp:789-929), the reference's
+    own code, at nside 2 with equal input and output resolution and beam: the shim's harmonic
+    round trip hands each of the 1000 simulated maps on unchanged and records it.  Stores the kept
+    pixels, the maps at those pixels (NEST order) and the reference's noise matrix."""
+    import tempfile
+    R = O.ref()
+    dp_ = ctypes.POINTER(ctypes.c_double)
+    R.ref_noise_matrix.argtypes = [ctypes.c_long, dp_, dp_, ctypes.c_double, ctypes.c_double, ctypes.c_char_p, dp_,
+                                   dp_, ctypes.c_int]
+    nside, npix = 2, 48
+    rng = np.random.default_rng(4)
+    mask = (rng.uniform(size=npix) < 0.8).astype(float)
+    nobs = rng.integers(50, 200, npix).astype(float)
+    good = np.flatnonzero(mask > 0.5).astype(np.int32)
+    ng = len(good)
+    out = np.zeros(ng * (ng + 1) // 2)
+    sims = np.zeros((1000, npix))
+    k = R.ref_noise_matrix(nside, mask.ctypes.data_as(dp_), nobs.ctypes.data_as(dp_), 10.0, 7.0,
+                           tempfile.mkdtemp().encode(), out.ctypes.data_as(dp_), sims.ctypes.data_as(dp_), 1000)
+    assert k == 1000, R.ref_last_error()
+    nest_of_ring = O.ring2nest(nside, np.arange(npix))
+    sims_nest = np.zeros_like(sims)
+    sims_nest[:, nest_of_ring] = sims
+    np.savez_compressed(os.path.join(HERE, "noise_nside2_reference.npz"), nside=nside, good=good,
+                        sims=np.ascontiguousarray(sims_nest[:, good]), noise_packed=out)
+    print("noise: %d simulations x %d kept pixels" % (k, ng))
+
+
 def main(parts):
     if not O.ref_available():
         raise SystemExit("build the reference first: make -C oracle/ref")
@@ -320,6 +352,8 @@ def main(parts):
         hmc_cases()
     if "pol" in parts:
         pol_cases()
+    if "noise" in parts:
+        noise_cases()
     if "legendre" in parts:
         legendre_cases(R)
     if "files" in parts:
@@ -380,4 +414,4 @@ def main(parts):
 
 
 if __name__ == "__main__":
-    main(set(sys.argv[1:]) or {"main", "fiducial", "legendre", "files", "config2", "hmc", "pol"})
+    main(set(sys.argv[1:]) or {"main", "fiducial", "legendre", "files", "config2", "hmc", "pol", "noise"})

@@ -1,8 +1,9 @@
 """The noise matrix from simulations (cg_noise_matrix_from_sims) is bit-identical to the
-oracle's restatement of calculateNoiseMatrix's averaging loop
-(source/c_matrix_generator.cpp:887-910): ragged sizes that leave partial 64-pixel tiles and
-partial 16-deep simulation slices, one simulation, and the reference's 1000 simulations at
-the nside 16 pixel count."""
+reference's own calculateNoiseMatrix on the 1000 simulations it averaged (fixture
+noise_nside2_reference.npz), and to the oracle's restatement of its averaging loop
+(source/c_matrix_generator.cpp:887-910) on ragged sizes that leave partial 64-pixel tiles and
+partial 16-deep simulation slices, one simulation, and 1000 simulations at the nside 16 pixel
+count."""
 import numpy as np
 import pytest
 
@@ -35,3 +36,9 @@ def test_noise_matrix_bit_identical(ctx, oracle_mod, nsims, n):
 def test_noise_matrix_rejects_bad_sizes(ctx):
     with pytest.raises(cg.CGError):
         ctx._check(ctx._L.cg_noise_matrix_from_sims(ctx._h, 0, 4, None, None, None))
+
+
+def test_noise_matrix_bit_identical_to_the_reference_itself(ctx):
+    g = load_golden("noise_nside2_reference")
+    got, _ = ctx.noise_matrix_from_sims(g["sims"])
+    assert np.array_equal(got, g["noise_packed"])

@@ -175,3 +175,11 @@ def test_oracle_pol_algebra_matches_the_reference_itself(oracle_mod):
         chi2, ld = oracle_mod.likelihood_pol(c_packed, npix, good, ninv, v, np.zeros_like(v))
         assert abs(chi2 - chi2_r) <= 1e-9 * abs(chi2_r)
         assert abs((ld - float(g["det_offset"])) - ld_r) <= 1e-9 * abs(ld_r)
+
+
+def test_oracle_noise_matrix_bit_identical_to_the_reference_itself(oracle_mod):
+    """The oracle's averaging loop against the reference's own calculateNoiseMatrix on the 1000
+    simulated maps it averaged (fixture: make_golden.py, part noise): bit-identical."""
+    g = load_golden("noise_nside2_reference")
+    packed, _ = oracle_mod.noise_matrix(g["sims"])
+    assert np.array_equal(packed, g["noise_packed"])
