@@ -418,8 +418,8 @@ class Context:
         self._check(self._L.cg_selftest_wait_timeout(self._h, ctypes.byref(st)))
         return st.value
 
-    TUNE_KNOBS = ("fwd", "fwd_ctas", "chol_ctas", "panel_ctas", "adj", "diag_sq")
-    ACCURACY_KNOBS = ("fwd", "diag_sq")   # never changed by autotune
+    TUNE_KNOBS = ("fwd", "fwd_ctas", "chol_ctas", "panel_ctas", "adj", "diag_sq", "table_bf16")
+    ACCURACY_KNOBS = ("fwd", "diag_sq", "table_bf16")   # never changed by autotune
 
     def tune_set(self, knob, value):
         self._check(self._L.cg_tune_set(self._h, knob.encode(), int(value)))

@@ -7,7 +7,7 @@
 // File format, one entry per line (later lines for the same key win):
 //   <device name>|n=<n>|lmax=<lmax>|B=<B>| fwd=0 fwd_ctas=0 chol_ctas=0 panel_ctas=0 adj=0 diag_sq=1 ms=31.5
 // The search covers the launch-shape knobs only (CTA counts, the adjoint's fetch variant); the
-// knobs that change rounding (fwd, diag_sq) keep the values they have.
+// knobs that change rounding (fwd, diag_sq, table_bf16) keep the values they have.
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -32,6 +32,7 @@ const Knob kKnobs[] = {
     {"panel_ctas", &cg::Tune::panel_ctas},
     {"adj", &cg::Tune::adj},
     {"diag_sq", &cg::Tune::diag_sq},
+    {"table_bf16", &cg::Tune::table_bf16},
 };
 
 const Knob* find_knob(const char* name)
@@ -52,14 +53,14 @@ std::vector<int> candidates(const cg_ctx* ctx, const Knob& k)
     if (k.field == &cg::Tune::chol_ctas) return {0, sm / 2, 2 * sm};
     if (k.field == &cg::Tune::panel_ctas) return {0, sm / 2, 2 * sm};
     if (k.field == &cg::Tune::adj) return {0, 1, 2};
-    return {ctx->tune.*(k.field)};  // accuracy knobs (fwd, diag_sq) are not searched
+    return {ctx->tune.*(k.field)};  // accuracy knobs (fwd, diag_sq, table_bf16) are not searched
 }
 
 bool valid_value(const cg_ctx* ctx, const Knob& k, int v)
 {
     if (k.field == &cg::Tune::fwd) return v == 0 || v == 1;
     if (k.field == &cg::Tune::adj) return v >= 0 && v <= 2;
-    if (k.field == &cg::Tune::diag_sq) return v == 0 || v == 1;
+    if (k.field == &cg::Tune::diag_sq || k.field == &cg::Tune::table_bf16) return v == 0 || v == 1;
     return v >= 0 && v <= 64 * std::max(1, ctx->sm_count);  // CTA counts; 0 = one per SM
 }
 
@@ -150,7 +151,14 @@ extern "C" int cg_tune_set(cg_ctx* ctx, const char* knob, int value)
     if (!ctx) return CG_ERR_BAD_ARG;
     const Knob* k = find_knob(knob);
     if (!k || !valid_value(ctx, *k, value)) { ctx->err = std::string("cg_tune_set: bad knob or value: ") + (knob ? knob : "NULL"); return CG_ERR_BAD_ARG; }
+    const int old = ctx->tune.*(k->field);
     ctx->tune.*(k->field) = value;
+    // the table is built at the reference point: rebuild it in the new precision
+    if (k->field == &cg::Tune::table_bf16 && old != value && ctx->precision == CG_PREC_MIXED && ctx->wmx.have_ref) {
+        CG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+        const std::vector<double> ref = ctx->wmx.cl_ref;
+        return cg::mixed_prepare_reference(ctx, ref.data());
+    }
     return CG_OK;
 }
 

@@ -28,6 +28,8 @@
 #include <cmath>
 #include <vector>
 
+#include <cuda_bf16.h>
+
 #include "cg_internal.h"
 #include "cg_tc.cuh"
 #include "cg_tile.cuh"
@@ -537,6 +539,13 @@ __global__ void __launch_bounds__(256) adj_finish(int B, int ntile, int lmax, in
     }
 }
 
+// the table's values rounded to the nearest BF16 (round to nearest even), kept in FP32
+__global__ void round_to_bf16(size_t n, float* __restrict__ u)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        u[i] = __bfloat162float(__float2bfloat16_rn(u[i]));
+}
+
 // Z in FP32
 __global__ void to_f32(size_t n, const double* __restrict__ src, float* __restrict__ dst)
 {
@@ -688,6 +697,7 @@ int mixed_prepare_reference(cg_ctx* ctx, const double* cl_ref_host)
             CG_CUDA_TRY(ctx, cudaFuncSetAttribute(build_ubar<CC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smu));
             build_ubar<CC><<<dim3(ntiles_lower(nt), TS / CC), 256, smu, s>>>(N, lmax, lp, w.Z, w.cref, w.U);
         }
+        if (ctx->tune.table_bf16) round_to_bf16<<<1024, 256, 0, s>>>(tiled * lp, w.U);
         CG_CUDA_TRY(ctx, cudaGetLastError());
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = CG_ERR_CUDA; }

@@ -242,7 +242,9 @@ int cg_stage_times(cg_ctx* ctx, double* ms);
    0 = FP32 FMA, the default; 1 = tensor cores, faster, but its one-way accumulation rounding
    biases the whitened matrix by a few ulp of |A - I|, about 1e-3 in -2lnL at nside 16 for C_l
    a factor e from the reference point), "diag_sq" (1, the default: the Cholesky's diagonal
-   blocks take their row sums of squares from the CUDA cores rather than the tensor core). */
+   blocks take their row sums of squares from the CUDA cores rather than the tensor core),
+   "table_bf16" (0, the default; 1 rounds the whitened Legendre table to BF16 and rebuilds it at
+   the current reference point: the BF16 table variant, whose error is measured, not a fast path). */
 int cg_tune_set(cg_ctx* ctx, const char* knob, int value);
 int cg_tune_get(const cg_ctx* ctx, const char* knob, int* value);
 /* "fwd=1 fwd_ctas=0 ..." of the knobs in effect */

@@ -250,3 +250,29 @@ def test_tuning_knobs_autotune_and_file(tmp_path):
         assert fresh.tuning() == chosen
     with _ctx(g, "mixed", B + 1, cl_ref=g["cls"][0], recenter="fixed") as other:
         assert not other.tune_load(path)   # another batch size: no entry
+
+
+def test_bf16_table_variant_error_is_measured():
+    """The BF16 table variant (the whitened Legendre table rounded to BF16, an 8-bit significand):
+    runs, reports its error against the FP64 path (printed; the mixed path's 1e-3 bar is not
+    expected to hold, the variant exists to measure that), and switching back rebuilds the FP32
+    table, which reproduces the default results exactly."""
+    g = load_golden("nside16_lmax47")
+    B = 32
+    cls = W.lognormal_batch(g["cls"][0], B, 23)
+    with _ctx(g, "fp64", B) as c64:
+        r64 = c64.loglike(cls, g["d"], grad=True)
+    with _ctx(g, "mixed", B, cl_ref=g["cls"][0], recenter="fixed") as cmx:
+        r32 = cmx.loglike(cls, g["d"], grad=True)
+        cmx.tune_set("table_bf16", 1)
+        assert cmx.reference_count() == 2
+        r16 = cmx.loglike(cls, g["d"], grad=True)
+        cmx.tune_set("table_bf16", 0)
+        back = cmx.loglike(cls, g["d"], grad=True)
+    assert np.all(r16["status"] == 0) and np.all(np.isfinite(r16["m2lnl"]))
+    e16 = np.abs(r16["m2lnl"] - r64["m2lnl"]).max()
+    e32 = np.abs(r32["m2lnl"] - r64["m2lnl"]).max()
+    g16 = (np.abs(r16["grad"][:, 2:] - r64["grad"][:, 2:]) / np.abs(r64["grad"][:, 2:]).max(axis=1, keepdims=True)).max()
+    print("BF16 table: max |d(-2lnL)| %.3e (FP32 table %.3e), gradient error / max|g| %.2e" % (e16, e32, g16))
+    assert e32 <= TOL_M2LNL
+    assert np.array_equal(back["m2lnl"], r32["m2lnl"]) and np.array_equal(back["grad"], r32["grad"])
