@@ -341,8 +341,10 @@ def run_ours(args):
         pc = ClockSampler(local)
         pc.start()
         rates = [ctx.probe_tf32_rate(1 << 16, 10)[0] for _ in range(4)]
-        tf32 = {"tflops": max(rates), "clocks": pc.stop(), "form": "tcgen05.mma kind::tf32 M128 N128 K8, A in "
-                "tensor memory, B in shared memory, one issuing thread per SM (cg_probe_tf32_rate)"}
+        f32 = [ctx.probe_fp32_rate(1 << 14, 10)[0] for _ in range(4)]
+        tf32 = {"tflops": max(rates), "fp32_fma2_tflops": max(f32), "clocks": pc.stop(),
+                "form": "tcgen05.mma kind::tf32 M128 N128 K8, A in tensor memory, B in shared memory, one issuing "
+                        "thread per SM (cg_probe_tf32_rate); FP32: packed fma.rn.f32x2 chains (cg_probe_fp32_rate)"}
     n, N = wl.n, ((wl.n + 127) // 128) * 128  # the library pads to an even number of 64-tiles
     pairs = n * (n + 1) // 2
     roof_build = None
@@ -371,11 +373,21 @@ def run_ours(args):
         lpad = ((L1 + 15) // 16) * 16
         build_bytes = tiled * lpad * 4 + B * tiled * 4
         fwd_tc = bool(tuning and tuning["knobs"].get("fwd") == 1)
-        roof_build = {"kernel": "build stage: A_b = I + sum_l eps_bl Ubar_l, FP32 out (%s)" %
-                                ("contract_fwd_tc, tcgen05 3xTF32" if fwd_tc else "contract_fwd, FP32 FMA"),
-                      "bound": "hbm",
-                      "achieved": build_bytes / (stages["build"] * 1e-3) / 1e9, "peak": peaks["hbm_gbs"],
-                      "unit": "GB/s", "algorithmic_bytes": build_bytes}
+        if fwd_tc:
+            roof_build = {"kernel": "build stage: A_b = I + sum_l eps_bl Ubar_l, FP32 out (contract_fwd_tc, tcgen05 "
+                                    "3xTF32)", "bound": "hbm",
+                          "achieved": build_bytes / (stages["build"] * 1e-3) / 1e9, "peak": peaks["hbm_gbs"],
+                          "unit": "GB/s", "algorithmic_bytes": build_bytes}
+        else:
+            # the FP32 contraction does 2 lp flops per entry and element (20 flops per byte moved, above the
+            # FP32 pipe's ridge of ~12): its roofline is the FP32 pipe, measured live by the FMA probe
+            build_flops = 2.0 * B * tiled * lpad
+            roof_build = {"kernel": "build stage: A_b = I + sum_l eps_bl Ubar_l, FP32 out (contract_fwd, packed "
+                                    "FP32 FMA)", "bound": "fp32",
+                          "achieved": build_flops / (stages["build"] * 1e-3) / 1e12, "peak": tf32["fp32_fma2_tflops"],
+                          "unit": "TFLOP/s", "algorithmic_flops": build_flops,
+                          "hbm_gbs": build_bytes / (stages["build"] * 1e-3) / 1e9,
+                          "hbm_frac": build_bytes / (stages["build"] * 1e-3) / 1e9 / peaks["hbm_gbs"]}
         roof_build["frac"] = roof_build["achieved"] / roof_build["peak"]
     else:
         roof = {"kernel": "FP64 tiled Cholesky", "bound": "fp64", "achieved": B * n ** 3 / 3.0 /

@@ -107,6 +107,7 @@ def library():
     L.cg_noise_matrix_from_sims.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp, _dp]
     L.cg_selftest_wait_timeout.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]
     L.cg_probe_tf32_rate.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp]
+    L.cg_probe_fp32_rate.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp, _dp]
     L.cg_plan_memory.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
     L.cg_get_memory_plan.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
     L.cg_tune_set.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.c_int]
@@ -449,6 +450,12 @@ class Context:
         f = ctypes.c_int(0)
         self._check(self._L.cg_tune_load(self._h, str(path).encode(), ctypes.byref(f)))
         return bool(f.value)
+
+    def probe_fp32_rate(self, iters=1 << 14, reps=5):
+        """FP32 rate (TFLOP/s) of packed two-lane FMAs, and the mean launch time (cg_probe_fp32_rate)."""
+        tf, ms = ctypes.c_double(0), ctypes.c_double(0)
+        self._check(self._L.cg_probe_fp32_rate(self._h, int(iters), int(reps), ctypes.byref(tf), ctypes.byref(ms)))
+        return tf.value, ms.value
 
     def probe_tf32_rate(self, iters=1 << 16, reps=5):
         """TF32 tensor-core rate (TFLOP/s) of the MMA form the factorisation kernels issue, and

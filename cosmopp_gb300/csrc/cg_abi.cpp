@@ -819,6 +819,14 @@ extern "C" int cg_selftest_wait_timeout(cg_ctx* ctx, int* status)
     return cg::selftest_wait_timeout(ctx, status);
 }
 
+extern "C" int cg_probe_fp32_rate(cg_ctx* ctx, int iters, int reps, double* tflops, double* ms)
+{
+    if (!ctx || !tflops || !ms) return CG_ERR_BAD_ARG;
+    if (iters > (1 << 24) || reps > 10000) { ctx->err = "cg_probe_fp32_rate: iters <= 2^24, reps <= 10000"; return CG_ERR_BAD_ARG; }
+    CG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    return cg::probe_fp32_rate(ctx, iters, reps, tflops, ms);
+}
+
 extern "C" int cg_probe_tf32_rate(cg_ctx* ctx, int iters, int reps, double* tflops, double* ms)
 {
     if (!ctx || !tflops || !ms) return CG_ERR_BAD_ARG;

@@ -237,6 +237,8 @@ int contract_fwd_tc_launch(cg_ctx* ctx, int B, int nt, int lp, const float* U, c
 int selftest_wait_timeout(cg_ctx* ctx, int* host_status);
 // achieved rate of the factorisation kernels' MMA form (kind::tf32 M128 N128 K8, A in tensor memory)
 int probe_tf32_rate(cg_ctx* ctx, int iters, int reps, double* tflops, double* ms_per_launch);
+// achieved FP32 rate of packed two-lane FMAs (fma.rn.f32x2), the FP32 contraction's instruction
+int probe_fp32_rate(cg_ctx* ctx, int iters, int reps, double* tflops, double* ms_per_launch);
 // mixed path (k_mixed.cu)
 int mixed_prepare_reference(cg_ctx* ctx, const double* cl_ref_host);
 int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, const double* d_d, int d_stride,

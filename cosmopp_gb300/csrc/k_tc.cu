@@ -1738,7 +1738,65 @@ __global__ void __launch_bounds__(128) mma_rate_probe(int iters, int* err)
     if (warp == 0) tmem_dealloc(tm, 256);
 }
 
+// FP32-pipe probe: 8 independent packed two-lane FMA chains (fma.rn.f32x2, the form the FP32
+// contraction issues) per thread, 8 warps per CTA, 4 CTAs per SM; the chains stay bounded
+// (a += c m with |c m| = 1e-7) and the result is kept live by a store that never happens
+__global__ void __launch_bounds__(256) fma2_rate_probe(int iters, float seed, float* sink)
+{
+    float a[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) a[i] = seed * (float)(threadIdx.x + i);
+    const float m0 = 0.999f, m1 = 1.0001f, c0 = 1e-7f, c1 = -1e-7f;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int r = 0; r < 2; ++r)
+#pragma unroll
+            for (int i = 0; i < 16; i += 2) fma2(a[i], a[i + 1], c0, c1, m0, m1);
+    }
+    float s = 0.f;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) s += a[i];
+    if (s == 12345.678f) sink[threadIdx.x] = s;
+}
+
 }  // namespace
+
+int probe_fp32_rate(cg_ctx* ctx, int iters, int reps, double* tflops, double* ms_per_launch)
+{
+    if (iters <= 0 || reps <= 0) { ctx->err = "probe: iters and reps must be positive"; return CG_ERR_BAD_ARG; }
+    float* sink = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CG_CUDA_TRY(ctx, cudaMalloc((void**)&sink, 256 * sizeof(float)));
+    cudaError_t e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    const int grid = 4 * ctx->sm_count;
+    if (e == cudaSuccess) {
+        fma2_rate_probe<<<grid, 256, 0, ctx->stream>>>(iters, 1e-3f, sink);  // warm-up
+        count_launch(ctx);
+        e = cudaEventRecord(e0, ctx->stream);
+    }
+    for (int r = 0; r < reps && e == cudaSuccess; ++r) {
+        fma2_rate_probe<<<grid, 256, 0, ctx->stream>>>(iters, 1e-3f, sink);
+        count_launch(ctx);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(e1, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    float ms = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+    int rc = CG_OK;
+    if (e != cudaSuccess) { ctx->err = cudaGetErrorString(e); rc = CG_ERR_CUDA; }
+    else {
+        // 16 packed FMAs (32 lane-FMAs, 64 flops) per thread and iteration
+        const double flops = 64.0 * iters * 256.0 * grid * reps;
+        *tflops = flops / (ms * 1e-3) / 1e12;
+        *ms_per_launch = ms / reps;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(sink);
+    return rc;
+}
 
 int probe_tf32_rate(cg_ctx* ctx, int iters, int reps, double* tflops, double* ms_per_launch)
 {

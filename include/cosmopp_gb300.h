@@ -226,6 +226,10 @@ int cg_selftest_wait_timeout(cg_ctx* ctx, int* status);
    rate achieved (2 M N K per MMA), *ms = the mean launch time.  The FP32-accurate (3xTF32)
    peak of the factorisation kernels is a third of it.  No counterpart in the reference. */
 int cg_probe_tf32_rate(cg_ctx* ctx, int iters, int reps, double* tflops, double* ms);
+/* FP32-pipe rate probe: 4 CTAs x 256 threads per SM, each thread 16 packed two-lane FMAs
+   (fma.rn.f32x2, the FP32 contraction's instruction) per iteration on 8 independent chains;
+   *tflops counts 2 flops per lane-FMA.  No counterpart in the reference. */
+int cg_probe_fp32_rate(cg_ctx* ctx, int iters, int reps, double* tflops, double* ms);
 /* kernels this context has launched so far */
 long long cg_launch_count(const cg_ctx* ctx);
 /* record CUDA events between the stages of each cg_loglike* call */
