@@ -41,12 +41,13 @@ def test_pol_likelihood_matches_the_reference_itself():
     """Against the reference's own compiled LikelihoodPolarization (fixture from make_golden.py,
     part pol: its constructor fed n_inv.txt, calculate run with a zero TT a_lm, so the E-mode
     template is zero): chi2 and the raw ln det of three maps."""
-    import hashlib
     from conftest import load_golden
     g = load_golden("pol_nside4_reference")
     _, npix, good, c_packed, ninv = _case(int(g["seed"]))
     ninv = np.ascontiguousarray(ninv)
-    assert hashlib.sha256(c_packed.tobytes() + ninv.tobytes() + good.tobytes()).hexdigest() == str(g["inputs_sha256"])
+    # the inputs come from the seeded draws; their products round alike to the last bits on each
+    # machine's BLAS only, so the kept pixels (integers) are compared and the values by the bar
+    assert np.array_equal(good, g["good"])
     lik = cg.LikelihoodPolarization(c_packed, npix, good, ninv)
     for v, chi2_r, ld_r in zip(g["v"], g["chi2"], g["logdet_ref"]):
         like, chi2, logdet = lik.calculate(v, np.zeros_like(v))
