@@ -514,7 +514,7 @@ def run_ours(args):
                       "host_share": 1.0 - (nev / hmc_s) / bare, "accept_rate": float(acc.mean()),
                       "ess_min": float(ess.min()), "ess_median": float(np.median(ess)),
                       "ess_per_s_min": float(ess.min() / hmc_s), "wall_s": hmc_s,
-                      "reference_point": "fiducial, re-centred automatically beyond |ln C/C_ref| = 1"}
+                      "reference_point": "fiducial, fixed"}
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(wl, d)
     ctx.close()

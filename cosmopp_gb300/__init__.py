@@ -117,6 +117,8 @@ def library():
     L.cg_tune_load.argtypes = [ctypes.c_void_p, ctypes.c_char_p, _ip]
     L.cg_launch_count.restype = ctypes.c_longlong
     L.cg_launch_count.argtypes = [ctypes.c_void_p]
+    L.cg_graph_replays.restype = ctypes.c_longlong
+    L.cg_graph_replays.argtypes = [ctypes.c_void_p]
     L.cg_set_profiling.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.cg_stage_times.argtypes = [ctypes.c_void_p, _dp]
     L.cg_likelihood_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, _dp, _dp, _dp, _dp, ctypes.c_int]
@@ -419,7 +421,7 @@ class Context:
         self._check(self._L.cg_selftest_wait_timeout(self._h, ctypes.byref(st)))
         return st.value
 
-    TUNE_KNOBS = ("fwd", "fwd_ctas", "chol_ctas", "panel_ctas", "adj", "diag_sq", "table_bf16")
+    TUNE_KNOBS = ("fwd", "fwd_ctas", "chol_ctas", "panel_ctas", "adj", "diag_sq", "table_bf16", "graph")
     ACCURACY_KNOBS = ("fwd", "diag_sq", "table_bf16")   # never changed by autotune
 
     def tune_set(self, knob, value):
@@ -463,6 +465,10 @@ class Context:
         tf, ms = ctypes.c_double(0), ctypes.c_double(0)
         self._check(self._L.cg_probe_tf32_rate(self._h, int(iters), int(reps), ctypes.byref(tf), ctypes.byref(ms)))
         return tf.value, ms.value
+
+    def graph_replays(self):
+        """Mixed calls replayed from a captured CUDA graph so far (cg_graph_replays)."""
+        return int(self._L.cg_graph_replays(self._h))
 
     def launch_count(self):
         """Kernels this context has launched so far."""

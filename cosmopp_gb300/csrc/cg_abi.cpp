@@ -88,6 +88,8 @@ extern "C" void cg_destroy(cg_ctx* ctx)
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (cg_ctx::Graph& gr : ctx->graphs)
+        if (gr.exec) cudaGraphExecDestroy(gr.exec);
     cg::fp64_free(ctx);
     cg::mixed_free(ctx);
     cudaFree(ctx->d_xyz); cudaFree(ctx->d_noise); cudaFree(ctx->d_lega); cudaFree(ctx->d_legb);
@@ -470,6 +472,9 @@ extern "C" int cg_noise_matrix_from_sims(cg_ctx* ctx, int nsims, int n, const do
 
 // ---- likelihood ------------------------------------------------------------
 
+static int loglike_chunks(cg_ctx* ctx, int B, const double* d_cl, const double* d_d, int d_stride, double* d_m2lnl,
+                          double* d_chi2, double* d_logdet, double* d_grad, int* d_status, cudaStream_t s);
+
 extern "C" int cg_loglike_device(cg_ctx* ctx, int B, const double* d_cl, const double* d_d, int d_stride,
                                  double* d_m2lnl, double* d_chi2, double* d_logdet, double* d_grad, int* d_status,
                                  void* stream)
@@ -482,7 +487,76 @@ extern "C" int cg_loglike_device(cg_ctx* ctx, int B, const double* d_cl, const d
     CG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
     ctx->nmarks = 0;
-    // the batch in pieces of the admitted chunk (one piece when the whole batch fits)
+    // A mixed call with a fixed reference point makes no host decision that depends on the data, so
+    // its ~80 launches are captured once into a CUDA graph and replayed with one launch while the
+    // arguments, the knobs and the workspace stay the same.  Anything that stops a capture (the
+    // caller's stream already capturing, the legacy stream, profiling marks) runs the launches
+    // directly instead.
+    if (ctx->precision == CG_PREC_MIXED && ctx->tune.graph && ctx->recenter == CG_RECENTER_FIXED &&
+        ctx->wmx.have_ref && !ctx->profiling && s != cudaStreamLegacy && s != cudaStreamPerThread) {
+        cg::GraphKey key;
+        key.B = B;
+        key.d_stride = d_stride;
+        key.stream = s;
+        const void* p[8] = {d_cl, d_d, d_m2lnl, d_chi2, d_logdet, d_grad, d_status, nullptr};
+        for (int i = 0; i < 8; ++i) key.ptr[i] = p[i];
+        ++ctx->graph_uses;
+        cg_ctx::Graph* slot = nullptr;
+        for (cg_ctx::Graph& gr : ctx->graphs)
+            if (gr.exec && gr.epoch == ctx->epoch && gr.key == key) slot = &gr;
+        if (slot) {
+            slot->last_use = ctx->graph_uses;
+            CG_CUDA_TRY(ctx, cudaGraphLaunch(slot->exec, s));
+            cg::count_launch(ctx, slot->launches);
+            ++ctx->graph_replays;
+            return CG_OK;
+        }
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusNone) {
+            const int rc0 = cg::mixed_ensure(ctx, std::min(B, ctx->chunk > 0 ? ctx->chunk : B));
+            if (rc0) return rc0;
+            // relaxed: a kernel's module may still be loaded lazily on its first launch
+            if (cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed) == cudaSuccess) {
+                const long long l0 = ctx->launches;
+                const int rc = loglike_chunks(ctx, B, d_cl, d_d, d_stride, d_m2lnl, d_chi2, d_logdet, d_grad,
+                                              d_status, s);
+                cudaGraph_t g = nullptr;
+                const cudaError_t ec = cudaStreamEndCapture(s, &g);
+                cudaGraphExec_t ex = nullptr;
+                if (!rc && ec == cudaSuccess && g && cudaGraphInstantiate(&ex, g, 0) == cudaSuccess) {
+                    cudaGraphDestroy(g);
+                    // the stale or least recently used slot takes it
+                    cg_ctx::Graph* victim = &ctx->graphs[0];
+                    for (cg_ctx::Graph& gr : ctx->graphs) {
+                        if (!gr.exec || gr.epoch != ctx->epoch) { victim = &gr; break; }
+                        if (gr.last_use < victim->last_use) victim = &gr;
+                    }
+                    if (victim->exec) cudaGraphExecDestroy(victim->exec);
+                    victim->exec = ex;
+                    victim->key = key;
+                    victim->epoch = ctx->epoch;
+                    victim->launches = ctx->launches - l0;
+                    victim->last_use = ctx->graph_uses;
+                    CG_CUDA_TRY(ctx, cudaGraphLaunch(ex, s));
+                    return CG_OK;
+                }
+                // the capture did not take: forget it and run the launches directly
+                if (g) cudaGraphDestroy(g);
+                cudaGetLastError();
+                ctx->launches = l0;
+                if (rc && rc != CG_ERR_CUDA) return rc;
+            } else {
+                cudaGetLastError();
+            }
+        }
+    }
+    return loglike_chunks(ctx, B, d_cl, d_d, d_stride, d_m2lnl, d_chi2, d_logdet, d_grad, d_status, s);
+}
+
+// the batch in pieces of the admitted chunk (one piece when the whole batch fits)
+static int loglike_chunks(cg_ctx* ctx, int B, const double* d_cl, const double* d_d, int d_stride, double* d_m2lnl,
+                          double* d_chi2, double* d_logdet, double* d_grad, int* d_status, cudaStream_t s)
+{
     const int chunk = ctx->chunk > 0 ? ctx->chunk : B;
     const size_t L1 = (size_t)ctx->lmax + 1;
     for (int b0 = 0; b0 < B; b0 += chunk) {
@@ -550,6 +624,8 @@ extern "C" int cg_set_reference(cg_ctx* ctx, const double* cl_ref)
 extern "C" int cg_reference_count(const cg_ctx* ctx) { return ctx ? ctx->wmx.ref_count : 0; }
 
 extern "C" long long cg_launch_count(const cg_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+extern "C" long long cg_graph_replays(const cg_ctx* ctx) { return ctx ? ctx->graph_replays : 0; }
 
 extern "C" int cg_set_profiling(cg_ctx* ctx, int enable)
 {

@@ -115,6 +115,21 @@ struct Tune {
     int diag_sq = 1;      // Cholesky diagonal blocks: row sums of squares on the CUDA cores (accuracy, not speed)
     int table_bf16 = 0;   // the whitened Legendre table rounded to BF16 (8-bit significand) when it is built:
                           // the BF16 table variant, for its measured error; storage stays FP32
+    int graph = 1;        // mixed calls with a fixed reference point replayed as one CUDA graph
+};
+
+// the argument set a captured mixed call was recorded for
+struct GraphKey {
+    int B = 0, d_stride = 0;
+    const void* ptr[8] = {};
+    cudaStream_t stream = nullptr;
+    bool operator==(const GraphKey& o) const
+    {
+        if (B != o.B || d_stride != o.d_stride || stream != o.stream) return false;
+        for (int i = 0; i < 8; ++i)
+            if (ptr[i] != o.ptr[i]) return false;
+        return true;
+    }
 };
 
 }  // namespace cg
@@ -144,6 +159,18 @@ struct cg_ctx {
     cg::Fp64Work w64;
     cg::MixedWork wmx;
     cg::Tune tune;
+    // one captured mixed call (cg_loglike_device), replayed while its arguments, the knobs and the
+    // workspace stay the same; epoch counts changes to the latter two
+    struct Graph {
+        cudaGraphExec_t exec = nullptr;
+        cg::GraphKey key;
+        long long epoch = -1;
+        long long launches = 0;     // kernels in the captured call
+        long long last_use = 0;
+    };
+    static constexpr int kGraphs = 8;  // argument sets kept (a caller cycling a few buffers)
+    Graph graphs[kGraphs];
+    long long epoch = 0, graph_uses = 0, graph_replays = 0;
     // memory admission (cg_plan_memory): a call's batch runs in pieces of `chunk` elements
     int chunk = 0;
     cg_memory_plan plan = {};
@@ -244,6 +271,8 @@ int mixed_prepare_reference(cg_ctx* ctx, const double* cl_ref_host);
 int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, const double* d_d, int d_stride,
                   double* d_m2lnl, double* d_chi2, double* d_logdet, double* d_grad, int* d_status, cudaStream_t s);
 void mixed_free(cg_ctx* ctx);
+// the mixed path's per-element workspace for B elements (allocated before a graph capture)
+int mixed_ensure(cg_ctx* ctx, int B);
 void fp64_free(cg_ctx* ctx);
 // small FP64 launchers used by the Likelihood drop-in (k_fp64.cu)
 void fp64_packed_to_tiled(int n, int nt, const double* c, const double* f, const double* nz, double* A, cudaStream_t s);

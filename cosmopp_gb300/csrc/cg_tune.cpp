@@ -33,6 +33,7 @@ const Knob kKnobs[] = {
     {"adj", &cg::Tune::adj},
     {"diag_sq", &cg::Tune::diag_sq},
     {"table_bf16", &cg::Tune::table_bf16},
+    {"graph", &cg::Tune::graph},
 };
 
 const Knob* find_knob(const char* name)
@@ -60,7 +61,8 @@ bool valid_value(const cg_ctx* ctx, const Knob& k, int v)
 {
     if (k.field == &cg::Tune::fwd) return v == 0 || v == 1;
     if (k.field == &cg::Tune::adj) return v >= 0 && v <= 2;
-    if (k.field == &cg::Tune::diag_sq || k.field == &cg::Tune::table_bf16) return v == 0 || v == 1;
+    if (k.field == &cg::Tune::diag_sq || k.field == &cg::Tune::table_bf16 || k.field == &cg::Tune::graph)
+        return v == 0 || v == 1;
     return v >= 0 && v <= 64 * std::max(1, ctx->sm_count);  // CTA counts; 0 = one per SM
 }
 
@@ -153,6 +155,7 @@ extern "C" int cg_tune_set(cg_ctx* ctx, const char* knob, int value)
     if (!k || !valid_value(ctx, *k, value)) { ctx->err = std::string("cg_tune_set: bad knob or value: ") + (knob ? knob : "NULL"); return CG_ERR_BAD_ARG; }
     const int old = ctx->tune.*(k->field);
     ctx->tune.*(k->field) = value;
+    if (old != value) ++ctx->epoch;  // a captured call baked the old launch shapes in
     // the table is built at the reference point: rebuild it in the new precision
     if (k->field == &cg::Tune::table_bf16 && old != value && ctx->precision == CG_PREC_MIXED && ctx->wmx.have_ref) {
         CG_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
@@ -196,7 +199,10 @@ extern "C" int cg_tune_load(cg_ctx* ctx, const char* path, int* found)
             hit = true;
         }
     }
-    if (hit) ctx->tune = best;
+    if (hit) {
+        ctx->tune = best;
+        ++ctx->epoch;
+    }
     if (found) *found = hit ? 1 : 0;
     return CG_OK;
 }
@@ -219,6 +225,7 @@ extern "C" int cg_autotune(cg_ctx* ctx, int B, const char* path, double* best_ms
     CG_CUDA_TRY(ctx, cudaMemcpy(ctx->d_cl, cl.data(), sizeof(double) * cl.size(), cudaMemcpyHostToDevice));
     CG_CUDA_TRY(ctx, cudaMemcpy(o_d, d.data(), sizeof(double) * d.size(), cudaMemcpyHostToDevice));
     const cg::Tune saved = ctx->tune;
+    ++ctx->epoch;
     const bool prof = ctx->profiling;
     ctx->profiling = false;
     const int reps = 3;
@@ -233,6 +240,7 @@ extern "C" int cg_autotune(cg_ctx* ctx, int B, const char* path, double* best_ms
         for (int v : candidates(ctx, k)) {
             if (v == keep) continue;
             ctx->tune.*(k.field) = v;
+            ++ctx->epoch;
             double ms = 0;
             if ((rc = time_calls(ctx, B, reps, &ms))) break;
             if (ms < best * 0.995) {  // a change must win by more than the timing noise
@@ -241,10 +249,12 @@ extern "C" int cg_autotune(cg_ctx* ctx, int B, const char* path, double* best_ms
             }
         }
         ctx->tune.*(k.field) = pick;
+        ++ctx->epoch;
     }
     ctx->profiling = prof;
     if (rc) {
         ctx->tune = saved;
+        ++ctx->epoch;
         return rc;
     }
     if (best_ms) *best_ms = best;

@@ -230,7 +230,11 @@ __global__ void init_status(int B, const double* __restrict__ cl, int lmax, int*
 
 // Forward contraction: A_b[t][e] = [e on the diagonal] + sum_l Ubar[t][l][e] eps[l][b], written
 // to A.  A CTA covers BB batch elements and FWD_NBLK consecutive blocks of EB = 16384 / BB entries
-// (blocks never straddle a tile); thread (te, tb) computes 8 entries x 8 batch elements.  The
+// (blocks never straddle a tile); thread (te, tb) computes 8 entries x 8 batch elements: entries
+// 4 te .. 4 te + 3 and EB/2 + 4 te .. + 3, so that the threads of a warp read 16-byte pieces that
+// are 16 bytes apart (conflict-free 128-bit shared-memory loads; 8-entry runs 32 bytes apart were a
+// two-way conflict on every load, which made the loop shared-memory bound).  Rows l = 0, 1 are zero
+// in the table and in eps (C_0, C_1 do not enter) and are skipped.  The
 // next block's table rows (lp rows of EB floats, 4096 floats apart) arrive by bulk copies into a
 // double buffer while the current block is computed; eps is staged once.  A bounded wait that
 // gives up sets *err (reported as CG_ERR_TIMEOUT).
@@ -270,7 +274,7 @@ __global__ void __launch_bounds__(256) contract_fwd(int B, int lp, const float* 
     }
     __syncthreads();
     const int te = threadIdx.x % TE, tb = threadIdx.x / TE;
-    const int e0 = te * 8, b0 = tb * 8;
+    const int e0 = te * 4, e1 = EB / 2 + te * 4, b0 = tb * 8;
     bool ok = true;
     for (int i = 0; i < FWD_NBLK; ++i) {
         if (ok && !tc::mbar_wait(&full[i & 1], (i >> 1) & 1, 1u << 22, err)) {
@@ -284,9 +288,10 @@ __global__ void __launch_bounds__(256) contract_fwd(int B, int lp, const float* 
 #pragma unroll
             for (int q = 0; q < 8; ++q) acc[a][q] = 0.f;
         if (b_begin + b0 < B) {
-            for (int l = 0; l < lp; ++l) {
+#pragma unroll 2
+            for (int l = 2; l < lp; ++l) {
                 const float4 u0 = *reinterpret_cast<const float4*>(&bu[l * EB + e0]);
-                const float4 u1 = *reinterpret_cast<const float4*>(&bu[l * EB + e0 + 4]);
+                const float4 u1 = *reinterpret_cast<const float4*>(&bu[l * EB + e1]);
                 const float4 w0 = *reinterpret_cast<const float4*>(&sE[l * BB + b0]);
                 const float4 w1 = *reinterpret_cast<const float4*>(&sE[l * BB + b0 + 4]);
                 const float u[8] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
@@ -302,7 +307,7 @@ __global__ void __launch_bounds__(256) contract_fwd(int B, int lp, const float* 
         const size_t e_begin = (blk0 + i) * EB;
         int I, J;
         tile_coords((int)(e_begin / TILE_ELEMS), I, J);
-        const int ein = (int)(e_begin % TILE_ELEMS) + e0;  // entry offset within the tile
+        const int eoff = (int)(e_begin % TILE_ELEMS);  // the block's entry offset within the tile
 #pragma unroll
         for (int q = 0; q < 8; ++q) {
             const int bb = b_begin + b0 + q;
@@ -310,13 +315,13 @@ __global__ void __launch_bounds__(256) contract_fwd(int B, int lp, const float* 
             float v[8];
 #pragma unroll
             for (int a = 0; a < 8; ++a) {
-                const int e = ein + a;
+                const int e = eoff + (a < 4 ? e0 + a : e1 + a - 4);
                 const bool dg = (I == J) && (e % TS == e / TS);
                 v[a] = acc[a][q] + (dg ? 1.f : 0.f);
             }
-            float4* pa = reinterpret_cast<float4*>(A + (size_t)bb * strideA + e_begin + e0);
-            pa[0] = make_float4(v[0], v[1], v[2], v[3]);
-            pa[1] = make_float4(v[4], v[5], v[6], v[7]);
+            float* pb = A + (size_t)bb * strideA + e_begin;
+            *reinterpret_cast<float4*>(pb + e0) = make_float4(v[0], v[1], v[2], v[3]);
+            *reinterpret_cast<float4*>(pb + e1) = make_float4(v[4], v[5], v[6], v[7]);
         }
     }
 }
@@ -619,6 +624,7 @@ static int ensure_batch_bufs(cg_ctx* ctx, int B)
 {
     MixedWork& w = ctx->wmx;
     if (w.cap >= B) return CG_OK;
+    ++ctx->epoch;  // a captured call refers to the buffers freed below
     cudaFree(w.A); cudaFree(w.V); cudaFree(w.Ls); cudaFree(w.Ms); cudaFree(w.Linv); cudaFree(w.diag); cudaFree(w.eps);
     cudaFree(w.y); cudaFree(w.x); cudaFree(w.r); cudaFree(w.part); cudaFree(w.gpart); cudaFree(w.st); cudaFree(w.ld);
     cudaFree(w.proj); cudaFree(w.Lc); cudaFree(w.Mc);
@@ -649,6 +655,8 @@ static int ensure_batch_bufs(cg_ctx* ctx, int B)
     w.cap = B;
     return CG_OK;
 }
+
+int mixed_ensure(cg_ctx* ctx, int B) { return ensure_batch_bufs(ctx, B); }
 
 int mixed_prepare_reference(cg_ctx* ctx, const double* cl_ref_host)
 {

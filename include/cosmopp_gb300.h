@@ -230,8 +230,15 @@ int cg_probe_tf32_rate(cg_ctx* ctx, int iters, int reps, double* tflops, double*
    (fma.rn.f32x2, the FP32 contraction's instruction) per iteration on 8 independent chains;
    *tflops counts 2 flops per lane-FMA.  No counterpart in the reference. */
 int cg_probe_fp32_rate(cg_ctx* ctx, int iters, int reps, double* tflops, double* ms);
-/* kernels this context has launched so far */
+/* kernels this context has launched so far (a replayed graph counts its kernels) */
 long long cg_launch_count(const cg_ctx* ctx);
+/* Mixed calls with a fixed reference point (CG_RECENTER_FIXED, reference set) are captured into a
+   CUDA graph on their first call with a given argument set (batch size, pointers, stream) and
+   replayed with one graph launch on later calls with the same set; up to 8 sets are kept, and a
+   knob change or a larger batch re-captures.  Calls from a stream that is already capturing, the
+   legacy or per-thread default stream, or with profiling on, launch their kernels directly.  The
+   knob "graph" = 0 turns replays off.  Returns the replays so far. */
+long long cg_graph_replays(const cg_ctx* ctx);
 /* record CUDA events between the stages of each cg_loglike* call */
 int cg_set_profiling(cg_ctx* ctx, int enable);
 /* per-stage device milliseconds of the last profiled call: ms[7] =
@@ -248,7 +255,8 @@ int cg_stage_times(cg_ctx* ctx, double* ms);
    a factor e from the reference point), "diag_sq" (1, the default: the Cholesky's diagonal
    blocks take their row sums of squares from the CUDA cores rather than the tensor core),
    "table_bf16" (0, the default; 1 rounds the whitened Legendre table to BF16 and rebuilds it at
-   the current reference point: the BF16 table variant, whose error is measured, not a fast path). */
+   the current reference point: the BF16 table variant, whose error is measured, not a fast path).
+   "graph" (1, the default: fixed-reference mixed calls replayed as one CUDA graph; 0 = direct launches). */
 int cg_tune_set(cg_ctx* ctx, const char* knob, int value);
 int cg_tune_get(const cg_ctx* ctx, const char* knob, int* value);
 /* "fwd=1 fwd_ctas=0 ..." of the knobs in effect */

@@ -276,3 +276,34 @@ def test_bf16_table_variant_error_is_measured():
     print("BF16 table: max |d(-2lnL)| %.3e (FP32 table %.3e), gradient error / max|g| %.2e" % (e16, e32, g16))
     assert e32 <= TOL_M2LNL
     assert np.array_equal(back["m2lnl"], r32["m2lnl"]) and np.array_equal(back["grad"], r32["grad"])
+
+
+def test_fixed_reference_calls_replay_one_cuda_graph():
+    """With a fixed reference point a mixed call is captured into a CUDA graph on its first call and
+    replayed afterwards: the replayed results equal the direct launches' bit for bit, a knob change
+    re-captures, and an automatically re-centring context launches directly."""
+    g = load_golden("nside8_lmax24")
+    B = 16
+    cls = W.lognormal_batch(g["cls"][0], B, 31)
+    cls2 = W.lognormal_batch(g["cls"][0], B, 32)
+    with _ctx(g, "mixed", B, cl_ref=g["cls"][0], recenter="fixed") as direct:
+        direct.tune_set("graph", 0)
+        want = [direct.loglike(c, g["d"], grad=True) for c in (cls, cls2, cls)]
+        assert direct.graph_replays() == 0
+    with _ctx(g, "mixed", B, cl_ref=g["cls"][0], recenter="fixed") as ctx:
+        got = [ctx.loglike(c, g["d"], grad=True) for c in (cls, cls2, cls)]
+        assert ctx.graph_replays() == 2      # the host entry point stages into the same buffers
+        n0 = ctx.launch_count()
+        ctx.loglike(cls, g["d"], grad=True)
+        assert ctx.graph_replays() == 3 and ctx.launch_count() > n0
+        ctx.tune_set("adj", 2)               # a knob change: captured again, same numbers
+        again = ctx.loglike(cls, g["d"], grad=True)
+        assert ctx.graph_replays() == 3
+    for a, b in zip(got, want):
+        for k in ("m2lnl", "chi2", "logdet", "grad", "status"):
+            assert np.array_equal(a[k], b[k]), k
+    assert np.abs(again["m2lnl"] - want[0]["m2lnl"]).max() <= 1e-6
+    with _ctx(g, "mixed", B, cl_ref=g["cls"][0], recenter="auto") as auto:
+        auto.loglike(cls, g["d"])
+        auto.loglike(cls, g["d"])
+        assert auto.graph_replays() == 0
