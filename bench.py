@@ -480,6 +480,38 @@ def run_ours(args):
                              "measured for the record, not the benchmarked path"}
         ctx.tune_set("table_bf16", 0)
         c64.close()
+    if rank == 0 and path == "mixed" and args.workload == WORKLOAD and nfp > 0:
+        # The plain FP64 workload: 100 lognormal C_l vectors at nside 16 (the same sky, beam, mask and
+        # map as the fixture tests/golden/config2_nside16.npz, which holds the reference's own -2lnL of
+        # each), through the FP64 path with its stage split, against the reference's values.
+        g2 = np.load(os.path.join(ROOT, "tests", "golden", "config2_nside16.npz"))
+        n100 = len(g2["cls"])
+        c2 = cg.Context(lmax=int(g2["lmax"]), fwhm_deg=float(g2["fwhm_deg"]), nside=int(g2["nside"]),
+                        good_pixels=g2["nest_good"], scheme="NEST", noise_sigma=float(g2["sigma"]),
+                        max_batch=n100, precision="fp64", device=local)
+        cl2 = torch.tensor(g2["cls"], dtype=torch.float64, device=dev)
+        d2 = torch.tensor(g2["d"], dtype=torch.float64, device=dev)
+        m2b = torch.empty(n100, dtype=torch.float64, device=dev)
+        c2.loglike_device(4, cl2.data_ptr(), d2.data_ptr(), 0, m2b.data_ptr(), None, None, None, None, sp)
+        torch.cuda.synchronize()
+        c2.set_profiling(True)
+        q0 = torch.cuda.Event(enable_timing=True)
+        q1 = torch.cuda.Event(enable_timing=True)
+        q0.record(stream)
+        c2.loglike_device(n100, cl2.data_ptr(), d2.data_ptr(), 0, m2b.data_ptr(), None, None, None, None, sp)
+        q1.record(stream)
+        torch.cuda.synchronize()
+        st2 = c2.stage_times()
+        c2.set_profiling(False)
+        c2.close()
+        got = m2b.cpu().numpy()
+        out["plain_fp64_100"] = {"workload": "nside16_lmax47 (100 lognormal C_l vectors, likelihood only)",
+                                 "evals_per_s": n100 / (q0.elapsed_time(q1) / 1000.0),
+                                 "stages_ms": {k: round(v, 3) for k, v in st2.items() if k not in ("end", "adjoint")},
+                                 "max_abs_delta_vs_reference": float(np.abs(got - g2["m2lnl"]).max()),
+                                 "max_abs_delta_vs_extended_precision": float(np.abs(got - g2["m2lnl_ext"]).max()),
+                                 "reference_own_max_abs_delta_vs_extended": float(np.abs(g2["m2lnl"] -
+                                                                                         g2["m2lnl_ext"]).max())}
     if rank == 0 and path == "mixed" and args.hmc_iters > 0:
         # gradient + HMC: 64 chains on ln C_l (l = 2..lmax), 20 leapfrog steps of 0.05, unit masses,
         # starts at the fiducial +-10% (seeded); every leapfrog step is one batched evaluation
