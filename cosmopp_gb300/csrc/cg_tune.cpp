@@ -53,14 +53,14 @@ std::vector<int> candidates(const cg_ctx* ctx, const Knob& k)
     if (k.field == &cg::Tune::fwd_ctas) return {0, sm * 3 / 4, sm / 2};
     if (k.field == &cg::Tune::chol_ctas) return {0, sm / 2, 2 * sm};
     if (k.field == &cg::Tune::panel_ctas) return {0, sm / 2, 2 * sm};
-    if (k.field == &cg::Tune::adj) return {0, 1, 2};
+    if (k.field == &cg::Tune::adj) return {0, 1, 2, 3};
     return {ctx->tune.*(k.field)};  // accuracy knobs (fwd, diag_sq, table_bf16) are not searched
 }
 
 bool valid_value(const cg_ctx* ctx, const Knob& k, int v)
 {
     if (k.field == &cg::Tune::fwd) return v == 0 || v == 1;
-    if (k.field == &cg::Tune::adj) return v >= 0 && v <= 2;
+    if (k.field == &cg::Tune::adj) return v >= 0 && v <= 3;
     if (k.field == &cg::Tune::diag_sq || k.field == &cg::Tune::table_bf16 || k.field == &cg::Tune::graph)
         return v == 0 || v == 1;
     return v >= 0 && v <= 64 * std::max(1, ctx->sm_count);  // CTA counts; 0 = one per SM

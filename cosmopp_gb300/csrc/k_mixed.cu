@@ -472,19 +472,25 @@ __global__ void __launch_bounds__(256, 2) contract_adj(int B, int lp, const floa
 
 // proj[b][h] = sum_i Z[h][i] x_b[i] (FP32); 64 x 64 output per CTA, 4 x 4 per thread;
 // grid (nharm_pad / 64, ceil(B / 64))
-__global__ void __launch_bounds__(256) project_x(int B, int N, int nhp, const float* __restrict__ Zf,
-                                                 const double* __restrict__ x, float* __restrict__ proj)
+// Z^T x_b in K slices: slice z = blockIdx.z covers pixels [z ks, (z + 1) ks) and writes
+// proj_part[z][b][h]; project_reduce sums the slices in order (deterministic).  One 64 x 64 output
+// tile per CTA over all N pixels gave only nhp / 64 x B / 64 CTAs (144 at the benchmark point, fewer
+// than the SMs), each walking 80 K steps alone.
+constexpr int PROJ_KSPLIT = 4;
+__global__ void __launch_bounds__(256) project_x(int B, int N, int nhp, int ks, const float* __restrict__ Zf,
+                                                 const double* __restrict__ x, float* __restrict__ proj_part)
 {
     __shared__ float sx[64][33], sz[64][33];
     const int h_begin = blockIdx.x * 64, b_begin = blockIdx.y * 64;
     const int th = threadIdx.x % 16, tb = threadIdx.x / 16;
+    const int kb = blockIdx.z * ks, ke = min(N, kb + ks);
     float acc[4][4] = {};
-    for (int k0 = 0; k0 < N; k0 += 32) {
+    for (int k0 = kb; k0 < ke; k0 += 32) {
         __syncthreads();
         for (int k = threadIdx.x; k < 64 * 32; k += 256) {
             const int row = k / 32, kk = k % 32, b = b_begin + row;
-            sx[row][kk] = (b < B && k0 + kk < N) ? (float)x[(size_t)b * N + k0 + kk] : 0.f;
-            sz[row][kk] = (k0 + kk < N) ? Zf[(size_t)(h_begin + row) * N + k0 + kk] : 0.f;
+            sx[row][kk] = (b < B && k0 + kk < ke) ? (float)x[(size_t)b * N + k0 + kk] : 0.f;
+            sz[row][kk] = (k0 + kk < ke) ? Zf[(size_t)(h_begin + row) * N + k0 + kk] : 0.f;
         }
         __syncthreads();
 #pragma unroll 8
@@ -498,12 +504,23 @@ __global__ void __launch_bounds__(256) project_x(int B, int N, int nhp, const fl
                 for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(xv[i], zv[j], acc[i][j]);
         }
     }
+    float* out = proj_part + (size_t)blockIdx.z * B * nhp;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const int b = b_begin + tb + 16 * i;
         if (b >= B) continue;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) proj[(size_t)b * nhp + h_begin + th + 16 * j] = acc[i][j];
+        for (int j = 0; j < 4; ++j) out[(size_t)b * nhp + h_begin + th + 16 * j] = acc[i][j];
+    }
+}
+
+__global__ void project_reduce(size_t n, const float* __restrict__ part, float* __restrict__ proj)
+{
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        float v = part[i];
+#pragma unroll
+        for (int z = 1; z < PROJ_KSPLIT; ++z) v += part[(size_t)z * n + i];
+        proj[i] = v;
     }
 }
 
@@ -593,7 +610,7 @@ void mixed_bytes(const cg_ctx* ctx, size_t* fixed, size_t* per_element)
     *fixed = sizeof(double) * (2 * tiled + nt * TILE_ELEMS + N + 2 * nhp * N) + sizeof(float) * (tiled * lp + nhp * N) +
              sizeof(double) * ((size_t)ctx->lmax + 2) + sizeof(int) * (1 + (size_t)tc_queue_slots(ctx->nt));
     *per_element = sizeof(float) * (2 * tiled + 2 * tc_split_elems(ctx->nt) + tc_linv_elems(ctx->nt) +
-                                    2 * tc_c1_elems(ctx->nt) + N + lp + ntile * lp + nhp) +
+                                    2 * tc_c1_elems(ctx->nt) + N + lp + ntile * lp + (1 + PROJ_KSPLIT) * nhp) +
                    sizeof(double) * (3 * N + ntile * 2 * TS + 1) + sizeof(int);
 }
 
@@ -648,7 +665,7 @@ static int ensure_batch_bufs(cg_ctx* ctx, int B)
     if (!rc) rc = dalloc(ctx, &w.r, (size_t)B * N);
     if (!rc) rc = dalloc(ctx, &w.part, (size_t)B * ntile * 2 * TS);
     if (!rc) rc = dalloc(ctx, &w.gpart, (size_t)ntile * B * lp);
-    if (!rc) rc = dalloc(ctx, &w.proj, (size_t)B * nharm_pad(ctx->lmax));
+    if (!rc) rc = dalloc(ctx, &w.proj, (size_t)(1 + PROJ_KSPLIT) * B * nharm_pad(ctx->lmax));  // + K-slice partials
     if (!rc) rc = dalloc(ctx, &w.st, (size_t)B);
     if (!rc) rc = dalloc(ctx, &w.ld, (size_t)B);
     if (rc) return rc;
@@ -787,13 +804,19 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
     }
     // A_b = I + sum_l eps_bl Ubar_l; small batches use 32-element CTA tiles (more entries per block)
     // when the double-buffered table rows fit in shared memory
+    // (64-element tiles where the 32-element tile's buffers do not fit, e.g. lp = 96)
     const size_t smem32 = sizeof(float) * lp * (32 + 2 * 512), smem128 = sizeof(float) * lp * (128 + 2 * 128);
+    const size_t smem64 = sizeof(float) * lp * (64 + 2 * 256);
     if (ctx->tune.fwd == 1 && contract_fwd_tc_ok(lp)) {
         if ((rc = contract_fwd_tc_launch(ctx, B, nt, lp, w.U, w.eps, w.A, tiled, w.tcerr, ctx->tune.fwd_ctas, s)))
             return rc;
     } else if (B <= 48 && smem32 <= 200 * 1024) {
         CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_fwd<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32));
         contract_fwd<32><<<dim3((unsigned)(tiled / (512 * FWD_NBLK)), (B + 31) / 32), 256, smem32, s>>>(
+            B, lp, w.U, w.eps, w.A, tiled, w.tcerr);
+    } else if (B <= 64 && smem64 <= 224 * 1024) {
+        CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_fwd<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem64));
+        contract_fwd<64><<<dim3((unsigned)(tiled / (256 * FWD_NBLK)), (B + 63) / 64), 256, smem64, s>>>(
             B, lp, w.U, w.eps, w.A, tiled, w.tcerr);
     } else {
         CG_CUDA_TRY(ctx, cudaFuncSetAttribute(contract_fwd<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem128));
@@ -835,9 +858,13 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
             count_launch(ctx);
         }
         const int nhp = nharm_pad(lmax);
-        project_x<<<dim3(nhp / 64, (B + 63) / 64), 256, 0, s>>>(B, N, nhp, w.Zf, w.x, w.proj);
+        const int ks = ((N + PROJ_KSPLIT * 32 - 1) / (PROJ_KSPLIT * 32)) * 32;
+        float* proj_part = w.proj + (size_t)B * nhp;
+        project_x<<<dim3(nhp / 64, (B + 63) / 64, PROJ_KSPLIT), 256, 0, s>>>(B, N, nhp, ks, w.Zf, w.x, proj_part);
+        project_reduce<<<(unsigned)std::min<size_t>(((size_t)B * nhp + 255) / 256, 4096), 256, 0, s>>>(
+            (size_t)B * nhp, proj_part, w.proj);
         adj_finish<<<B, 256, 0, s>>>(B, ntile, lmax, lp, nhp, w.gpart, w.proj, w.cref, d_grad);
-        count_launch(ctx, 2);
+        count_launch(ctx, 3);
     }
     merge_tc_status<<<(B + 127) / 128, 128, 0, s>>>(B, w.tcerr, w.st);
     count_launch(ctx);

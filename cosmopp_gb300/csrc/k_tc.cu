@@ -1938,6 +1938,7 @@ int adjoint_contract_tc(cg_ctx* ctx, int B, int nt, int lp, const float* U, cons
     if (lp <= 48)
         rc = v == 1   ? launch_adj_tc<24, 2, 3>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)
              : v == 2 ? launch_adj_tc<24, 1, 4>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)
+             : v == 3 ? launch_adj_tc<24, 4, 2>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)  // 512-byte row runs
                       : launch_adj_tc<24, 2, 4>(ctx, grid, B, lp, U, V, strideA, part, d_err, s);
     else if (lp <= 64)
         rc = v == 2 ? launch_adj_tc<32, 1, 4>(ctx, grid, B, lp, U, V, strideA, part, d_err, s)

@@ -226,7 +226,7 @@ def test_tuning_knobs_autotune_and_file(tmp_path):
     path = tmp_path / "tune.txt"
     with _ctx(g, "mixed", B, cl_ref=g["cls"][0], recenter="fixed") as ctx:
         base = ctx.loglike(cls, g["d"], grad=True)
-        for knob, vals in (("fwd", (0, 1)), ("chol_ctas", (8, 300)), ("panel_ctas", (5, 300)), ("adj", (1, 2)),
+        for knob, vals in (("fwd", (0, 1)), ("chol_ctas", (8, 300)), ("panel_ctas", (5, 300)), ("adj", (1, 2, 3)),
                            ("fwd_ctas", (7,))):
             keep = ctx.tune_get(knob)
             for v in vals:
