@@ -116,6 +116,9 @@ struct Tune {
     int table_bf16 = 0;   // the whitened Legendre table rounded to BF16 (8-bit significand) when it is built:
                           // the BF16 table variant, for its measured error; storage stays FP32
     int graph = 1;        // mixed calls with a fixed reference point replayed as one CUDA graph
+    int lauum = 2;        // lauum: one CTA per block with the A operand from the FP32 copy, split on chip (2),
+                          // or from the split copy (0); persistent CTAs over a work queue (1)
+    int trtri = 0;        // 0 = one CTA per trtri block, 1 = persistent CTAs over a work queue (same results)
 };
 
 // the argument set a captured mixed call was recorded for

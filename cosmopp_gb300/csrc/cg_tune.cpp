@@ -34,6 +34,8 @@ const Knob kKnobs[] = {
     {"diag_sq", &cg::Tune::diag_sq},
     {"table_bf16", &cg::Tune::table_bf16},
     {"graph", &cg::Tune::graph},
+    {"lauum", &cg::Tune::lauum},
+    {"trtri", &cg::Tune::trtri},
 };
 
 const Knob* find_knob(const char* name)
@@ -54,6 +56,8 @@ std::vector<int> candidates(const cg_ctx* ctx, const Knob& k)
     if (k.field == &cg::Tune::chol_ctas) return {0, sm / 2, 2 * sm};
     if (k.field == &cg::Tune::panel_ctas) return {0, sm / 2, 2 * sm};
     if (k.field == &cg::Tune::adj) return {0, 1, 2, 3};
+    if (k.field == &cg::Tune::lauum) return {0, 1, 2};
+    if (k.field == &cg::Tune::trtri) return {0, 1};
     return {ctx->tune.*(k.field)};  // accuracy knobs (fwd, diag_sq, table_bf16) are not searched
 }
 
@@ -61,7 +65,9 @@ bool valid_value(const cg_ctx* ctx, const Knob& k, int v)
 {
     if (k.field == &cg::Tune::fwd) return v == 0 || v == 1;
     if (k.field == &cg::Tune::adj) return v >= 0 && v <= 3;
-    if (k.field == &cg::Tune::diag_sq || k.field == &cg::Tune::table_bf16 || k.field == &cg::Tune::graph)
+    if (k.field == &cg::Tune::lauum) return v >= 0 && v <= 2;
+    if (k.field == &cg::Tune::diag_sq || k.field == &cg::Tune::table_bf16 || k.field == &cg::Tune::graph ||
+        k.field == &cg::Tune::trtri)
         return v == 0 || v == 1;
     return v >= 0 && v <= 64 * std::max(1, ctx->sm_count);  // CTA counts; 0 = one per SM
 }

@@ -330,15 +330,17 @@ constexpr uint32_t kMaxIter = 1u << 22;  // try_wait attempts before a wait give
 // tensor-memory stage g % NAST, then one arrival per warp on the stage's a_full barrier
 // ssq (nullable, B_FROM_A only): the chunk's sum of squares of this thread's 16 values, summed in
 // FP32 (round to nearest) and added to the double-float (ssq->x, ssq->y) by an exact two-sum
+// ga (>= 0): the chunk's place in the A ring's own sequence, where not every chunk passes the ring
 template <int AMODE, int BMODE = B_COPY, int NX, class W>
 __device__ __forceinline__ void put_a(int g, float4 (&qx)[NX], W& wait, const float* sa_f, TcCtl& ctl, uint32_t tm,
-                                      float2* ssq = nullptr)
+                                      float2* ssq = nullptr, int ga = -1)
 {
     const int r = threadIdx.x % 128, h = threadIdx.x / 128, lane = threadIdx.x % 32, st = g % NAST;
     if constexpr (AMODE == A_SMEM_C1 || AMODE == A_SMEM_PRE) {
         // this thread's 16 values of the staged chunk (row r, K columns 16h .. 16h+15)
-        const int si = g % NSTA;
-        if constexpr (AMODE == A_SMEM_C1) wait(&ctl.as_full[si], (g / NSTA) & 1);
+        const int gi = ga >= 0 ? ga : g;
+        const int si = gi % NSTA;
+        if constexpr (AMODE == A_SMEM_C1) wait(&ctl.as_full[si], (gi / NSTA) & 1);
         const float* p = sa_f + si * (STA_BYTES / 4) + (r >> 3) * 256 + (r & 7) * 4 + 4 * h * 32;
 #pragma unroll
         for (int i = 0; i < 4; ++i) qx[i] = *reinterpret_cast<const float4*>(p + i * 32);
@@ -679,6 +681,174 @@ __device__ bool tc_stream(int nitems, int* queue, GEO geo, FA fa, FB fb, FE epi,
             enter(q);
             for (int g = 0; q.gm.n; ++g) {
                 copy_a<AMODE>(g, wait, ctl, sb, [&](auto& top, auto& bot, auto& kc) { fa(q.gm, q.c, top, bot, kc); });
+                next(q, REL_ONE);
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---- B copies: this thread takes the items and publishes them
+        if (lane == 0) {
+            int g = 0;
+            for (int k = 0;; ++k) {
+                const int slot = k % NIQ;
+                if (k >= NIQ) wait(&ctl.iq_empty[slot], ((k / NIQ) - 1) & 1);
+                const int got = ok ? atomicAdd(queue, 1) : -1;
+                const int it = (got >= 0 && got < nitems) ? got : -1;
+                ctl.iq[slot] = it;
+                mbar_arrive(&ctl.iq_full[slot]);
+                if (it < 0) break;
+                const Geo gm = geo(it);
+                for (int c = 0; c < gm.n; ++c, ++g)
+                    copy_b<B_COPY>(g, wait, ctl, sb, [&](uint32_t dst, uint64_t* bar) { fb(gm, c, dst, bar); });
+            }
+        }
+        __syncwarp();
+    }
+    return ok;
+}
+
+// ---- a stream of chained items ---------------------------------------------------------------
+
+// Chunks g .. g + 3 of a chained item: the A operand is the item's first product, held in R (this
+// thread: row t % 128, K columns 64 h + j of the four chunks' 128, i.e. chunks 2 h and 2 h + 1),
+// split into hi and lo as put_a splits (so the result is the one a ring round trip would give) and
+// stored to the tensor-memory stages (g + q) % NAST, which the caller freed by retiring every earlier
+// chunk.  Every producer warp arrives once on each of the four stages' a_full.
+__device__ __forceinline__ void put_chain(int g, const float (&R)[64], TcCtl& ctl, uint32_t tm)
+{
+    const int h = threadIdx.x / 128, lane = threadIdx.x % 32;
+#pragma unroll
+    for (int qq = 0; qq < 2; ++qq) {
+        const int st = (g + 2 * h + qq) % NAST;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            float4 x[4], qh[4], ql[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int j = 32 * qq + 16 * half + 4 * i;
+                x[i] = make_float4(R[j], R[j + 1], R[j + 2], R[j + 3]);
+            }
+            split4(x, qh, ql);
+            tmem_st16(tm + lane_base() + col_a_hi(st) + 16 * half, qh);
+            tmem_st16(tm + lane_base() + col_a_lo(st) + 16 * half, ql);
+        }
+    }
+    tmem_wait_st();
+    fence_before();
+    __syncwarp();
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) mbar_arrive(&ctl.a_full[(g + q) % NAST]);
+}
+
+// tc_stream for items that are two chained products, R1 = sum over its first n1 chunks (A from the
+// FP32 canonical ring, A_SMEM_C1) and R = R1 x (four more chunks of B): the last four chunks' A is
+// R1 itself, which the producers move from their registers to tensor memory (put_chain) once every
+// chunk of the first product is folded in, so the intermediate product never leaves the SM and the
+// CTA goes on to the next item without a barrier or a pipeline restart.  geo(it) gives a struct with
+// members n (all chunks, n1 + 4) and n1 (even, >= 2); fa(gm, c, top, bot, kc) names chunk c < n1's
+// A tiles; fb(gm, c, dst, bar) issues the B copies of every chunk; epi(gm, R) as for tc_stream.
+template <class GEO, class FA, class FB, class FE>
+__device__ bool tc_stream_chain(int nitems, int* queue, GEO geo, FA fa, FB fb, FE epi, unsigned char* sbuf,
+                                TcCtl& ctl, uint32_t tm, float (&R)[64], int* err)
+{
+    bool ok = true;
+    auto wait = [&](uint64_t* bar, uint32_t parity) {
+        if (!ok) return;
+        ok = mbar_wait(bar, parity, kMaxIter, err);
+        if (!ok) atomicExch(err, 1);
+    };
+    using Geo = decltype(geo(0));
+    struct Cur {
+        int k, c;
+        Geo gm;
+    };
+    auto enter = [&](Cur& q) {
+        wait(&ctl.iq_full[q.k % NIQ], (q.k / NIQ) & 1);
+        const int it = ctl.iq[q.k % NIQ];
+        q.c = 0;
+        if (ok && it >= 0 && it < nitems) {
+            q.gm = geo(it);
+        } else {
+            q.gm.n = 0;
+        }
+    };
+    enum { REL_NONE, REL_WARP, REL_ONE };
+    auto next = [&](Cur& q, int release) {
+        if (++q.c < q.gm.n) return;
+        if (release == REL_WARP) {
+            __syncwarp();
+            if ((threadIdx.x % 32) == 0) mbar_arrive(&ctl.iq_empty[q.k % NIQ]);
+        } else if (release == REL_ONE) {
+            mbar_arrive(&ctl.iq_empty[q.k % NIQ]);
+        }
+        ++q.k;
+        enter(q);
+    };
+    const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const uint32_t sb = smem_u32(sbuf);
+    const float* sa_f = reinterpret_cast<const float*>(sbuf + NSTB * STB_BYTES);
+#pragma unroll
+    for (int j = 0; j < 64; ++j) R[j] = 0.f;
+    if (warp < NPROD / 32) {
+        // ---- producers: chunks put (np), retired (nr), taken from the A ring (ga), in stream order
+        Cur pq{}, dq{};
+        enter(pq);
+        enter(dq);
+        int np = 0, nr = 0, ga = 0;
+        float4 qx[4];
+        auto retire = [&](bool last) {
+            const bool item_end = dq.c == dq.gm.n - 1;
+            retire_acc(nr, last, (nr & 1) || item_end, wait, ok, err, ctl, tm, R);
+            if (item_end) {
+                epi(dq.gm, R);
+#pragma unroll
+                for (int j = 0; j < 64; ++j) R[j] = 0.f;
+            }
+            ++nr;
+            next(dq, REL_WARP);
+        };
+        while (pq.gm.n) {
+            if (pq.c < pq.gm.n1) {
+                // a ring chunk into tensor-memory stage np % NAST, once chunk np - NAST has retired
+                while (nr <= np - NAST) retire(false);
+                put_a<A_SMEM_C1>(np, qx, wait, sa_f, ctl, tm, nullptr, ga);
+                ++ga;
+                ++np;
+                next(pq, REL_NONE);
+            } else {
+                // the item's first product complete in R: the four chained chunks from it
+                while (nr < np) retire(false);
+                put_chain(np, R, ctl, tm);
+#pragma unroll
+                for (int j = 0; j < 64; ++j) R[j] = 0.f;
+                np += 4;
+                for (int q = 0; q < 4; ++q) next(pq, REL_NONE);
+            }
+        }
+        while (nr < np) retire(true);
+    } else if (warp == NPROD / 32 || warp == NPROD / 32 + 2) {
+        // ---- MMA issue: chunk pairs 0, 2, 4, ... of the stream from warp 8, pairs 1, 3, ... from warp 10
+        const int par = (warp == NPROD / 32) ? 0 : 1;
+        if (lane == 0) {
+            Cur q{};
+            enter(q);
+            for (int g = 0; q.gm.n; ++g) {
+                if (((g >> 1) & 1) == par) issue_chunk(g, wait, ctl, tm, sb);
+                next(q, REL_ONE);
+            }
+        }
+        __syncwarp();
+    } else if (warp == NPROD / 32 + 3) {
+        // ---- A copies of the ring chunks, following the published items
+        if (lane == 0) {
+            Cur q{};
+            enter(q);
+            for (int ga = 0; q.gm.n;) {
+                if (q.c < q.gm.n1) {
+                    copy_a<A_SMEM_C1>(ga, wait, ctl, sb, [&](auto& top, auto& bot, auto& kc) { fa(q.gm, q.c, top, bot, kc); });
+                    ++ga;
+                }
                 next(q, REL_ONE);
             }
         }
@@ -1238,13 +1408,69 @@ __global__ void __launch_bounds__(NTH, 1) trtri_tc_row(int I2, int nt, const flo
     tc_end(tm);
 }
 
+// Row block I2 of M = L^-1 as a stream of items it = b * I2 + J2 (J2 < I2) taken in order from the
+// work queue by persistent CTAs: each item is trtri_tc_row's two products, S^T = sum_k M_kJ^T L_Ik^T
+// (A from M^T's FP32 canonical copy through the ring) and (M_IJ)^T = -S^T Linv_I^T, chained on chip
+// (tc_stream_chain), with the same operands, splits and summation order, so the same results.  The
+// items of one batch element share its L row panel I in L2.
+__global__ void __launch_bounds__(NTH, 1) trtri_tc_stream(int I2, int nt, int B, const float* __restrict__ Ls,
+                                                          const float* __restrict__ Linv, float* __restrict__ Ms,
+                                                          float* __restrict__ Mc, int* __restrict__ queue,
+                                                          int* __restrict__ err)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ TcCtl ctl;
+    const int nt2 = nt / 2;
+    const size_t ntile = (size_t)ntiles_lower(nt);
+    const uint32_t tm = tc_begin(ctl);
+    struct Item {
+        int n, n1, J2, b;
+    };
+    auto geo = [&](int it) {
+        const int J2 = it % I2, n1 = (2 * I2 - 2 * J2) * (TS / KC);
+        return Item{n1 + 128 / KC, n1, J2, it / I2};
+    };
+    // A(c, m) = M_kJ(m, c): C1 tiles (k, 2 J2), (k, 2 J2 + 1) of M^T, k >= 2 J2 (zero above the diagonal)
+    auto fa = [&](const Item& q, int c, const float*& top, const float*& bot, int& kc) {
+        const float* Mcb = Mc + (size_t)q.b * ntile * C1_TILE;
+        const int k = 2 * q.J2 + c / 2;
+        top = Mcb + (size_t)tile_index(k, 2 * q.J2) * C1_TILE;
+        bot = (k >= 2 * q.J2 + 1) ? Mcb + (size_t)tile_index(k, 2 * q.J2 + 1) * C1_TILE : nullptr;
+        kc = c % 2;
+    };
+    // B: L_Ik (SC tiles (2 I2, k), (2 I2 + 1, k)) for the first product, then Linv_I's four chunks
+    auto fb = [&](const Item& q, int c, uint32_t dst, uint64_t* bar) {
+        if (c < q.n1) {
+            const float* Lb = Ls + (size_t)q.b * ntile * SC_TILE;
+            const int k = 2 * q.J2 + c / 2;
+            bulk_tiles(Lb + (size_t)tile_index(2 * I2, k) * SC_TILE, Lb + (size_t)tile_index(2 * I2 + 1, k) * SC_TILE,
+                       c % 2, dst, bar);
+        } else {
+            bulk_linv(Linv + ((size_t)q.b * nt2 + I2) * LINV_SC, c - q.n1, dst, bar);
+        }
+    };
+    auto epi = [&](const Item& q, float (&R)[64]) {
+        const int row = threadIdx.x % 128, h = threadIdx.x / 128;
+        const size_t tix = (size_t)q.b * ntile + tile_index(2 * I2 + h, 2 * q.J2 + row / 64);
+        st_sc_row(Ms + tix * SC_TILE, row % 64, R, -1.f);
+        st_c1_row(Mc + tix * C1_TILE, row % 64, R, -1.f);
+    };
+    float R[64];
+    tc_stream_chain(I2 * B, queue, geo, fa, fb, epi, smem_raw, ctl, tm, R, err);
+    tc_end(tm);
+}
+
 // V_IJ (128x128 supertile, lower) = sum over k of M_k,I^T M_k,J from the M^T storage; V in FP32
-// column-major tiles.  grid (supertiles of the lower triangle, B).  One CTA per supertile: lauum's
-// A operands are loaded by the producers (a persistent stream costs them the registers for it),
-// and the hardware's in-order CTA dispatch keeps the CTAs running together on one batch element,
-// whose M stays in L2.
-__global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restrict__ Ms, float* __restrict__ V,
-                                                   int* __restrict__ err)
+// column-major tiles.  grid (supertiles of the lower triangle, B).  One CTA per supertile: the
+// hardware's in-order CTA dispatch keeps the CTAs running together on one batch element, whose M
+// stays in L2 (a persistent stream over a work queue, lauum_tc_stream, measured slower at nside 16
+// and level at nside 32).
+// AM = A_SMEM_C1 (the default): the A operand from the FP32 canonical copy Mc through the
+// shared-memory ring, split on chip, its low parts left unrounded for the tensor core; A_REG_SC: from
+// the split copy Ms, low parts rounded to TF32 when it was written.
+template <int AM>
+__global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restrict__ Ms, const float* __restrict__ Mc,
+                                                   float* __restrict__ V, int* __restrict__ err)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ TcCtl ctl;
@@ -1256,9 +1482,10 @@ __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restri
     const uint32_t tm = tc_begin(ctl);
     const int k0 = 2 * I2;  // first tile row with a non-zero M_k,I
     const int nchunks = (nt - k0) * (TS / KC);
-    // A(r, m) = M_{k, 2I2 + r/64}(m, r%64); B(c, m) = M_{k, 2J2 + c/64}(m, c%64); zero above the diagonal
-    // (A from the split copy: lauum's operands are shared by many CTAs and stay in L2, so the
-    // extra bytes cost less than splitting in the producers)
+    // A(r, m) = M_{k, 2I2 + r/64}(m, r%64); B(c, m) = M_{k, 2J2 + c/64}(m, c%64); zero above the diagonal.
+    // AM = A_REG_SC: A loaded pre-split by the producers, two chunks ahead in registers; A_SMEM_C1:
+    // A from the FP32 copy through the four-stage ring (half the bytes, further ahead), split on
+    // chip: 5.85 against 6.19 ms at nside 16, batch 256.
     auto fa = [&](int c, int r, int h, float4 (&x)[8]) {
         const int k = k0 + c / 2, col = 2 * I2 + r / 64;
         if (k < col) {
@@ -1281,8 +1508,62 @@ __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restri
         bulk_tiles(top, bot, c % 2, dst, bar);
     };
     float R[64];
-    tc_kloop<A_REG_SC>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
+    if constexpr (AM == A_SMEM_C1) {
+        const float* Mcb = Mc + (size_t)b * ntile * C1_TILE;
+        auto fa1 = [&](int c, const float*& top, const float*& bot, int& kc) {
+            const int k = k0 + c / 2;
+            top = Mcb + (size_t)tile_index(k, 2 * I2) * C1_TILE;
+            bot = (k >= 2 * I2 + 1) ? Mcb + (size_t)tile_index(k, 2 * I2 + 1) * C1_TILE : nullptr;
+            kc = c % 2;
+        };
+        tc_kloop<A_SMEM_C1>(nchunks, fa1, fb, smem_raw, ctl, tm, R, err);
+    } else {
+        tc_kloop<A_REG_SC>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
+    }
     store_block(R, V + (size_t)b * ntile * TILE_ELEMS, I2, J2, 1.f);
+    tc_end(tm);
+}
+
+// lauum_tc as a stream of items it = b * (supertiles) + t (t in tile_coords order) taken in order
+// from the work queue by persistent CTAs, so that a CTA's set-up and the first loads of an item
+// overlap the previous item's MMAs.  The A operand (M^T's column panel I) comes from the FP32
+// canonical copy through the shared-memory ring and is split on chip (its low part left unrounded
+// for the tensor core to truncate, where lauum_tc reads the split copy's rounded one: the two differ
+// by under 2^-22 of an entry); the B operand from the split copy, as in lauum_tc.
+__global__ void __launch_bounds__(NTH, 1) lauum_tc_stream(int nt, int B, const float* __restrict__ Ms,
+                                                          const float* __restrict__ Mc, float* __restrict__ V,
+                                                          int* __restrict__ queue, int* __restrict__ err)
+{
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    __shared__ TcCtl ctl;
+    const int nt2 = nt / 2, nsup = nt2 * (nt2 + 1) / 2;
+    const size_t ntile = (size_t)ntiles_lower(nt);
+    const uint32_t tm = tc_begin(ctl);
+    struct Item {
+        int n, I2, J2;
+        size_t boff;  // the batch element's first tile
+    };
+    auto geo = [&](int it) {
+        int I2, J2;
+        tile_coords(it % nsup, I2, J2);
+        return Item{(nt - 2 * I2) * (TS / KC), I2, J2, (size_t)(it / nsup) * ntile};
+    };
+    // A(r, m) = M_{k, 2I2 + r/64}(m, r%64): C1 tiles (k, 2 I2), (k, 2 I2 + 1) of M^T, k >= 2 I2
+    auto fa = [&](const Item& q, int c, const float*& top, const float*& bot, int& kc) {
+        const int k = 2 * q.I2 + c / 2;
+        top = Mc + (q.boff + tile_index(k, 2 * q.I2)) * C1_TILE;
+        bot = (k >= 2 * q.I2 + 1) ? Mc + (q.boff + tile_index(k, 2 * q.I2 + 1)) * C1_TILE : nullptr;
+        kc = c % 2;
+    };
+    auto fb = [&](const Item& q, int c, uint32_t dst, uint64_t* bar) {
+        const int k = 2 * q.I2 + c / 2;
+        const float* top = (k >= 2 * q.J2) ? Ms + (q.boff + tile_index(k, 2 * q.J2)) * SC_TILE : nullptr;
+        const float* bot = (k >= 2 * q.J2 + 1) ? Ms + (q.boff + tile_index(k, 2 * q.J2 + 1)) * SC_TILE : nullptr;
+        bulk_tiles(top, bot, c % 2, dst, bar);
+    };
+    auto epi = [&](const Item& q, float (&R)[64]) { store_block(R, V + q.boff * TILE_ELEMS, q.I2, q.J2, 1.f); };
+    float R[64];
+    tc_stream<A_SMEM_C1>(nsup * B, queue, geo, fa, fb, epi, smem_raw, ctl, tm, R, err);
     tc_end(tm);
 }
 
@@ -1854,8 +2135,10 @@ static int set_smem(cg_ctx* ctx, K kern)
 size_t tc_split_elems(int nt) { return (size_t)ntiles_lower(nt) * SC_TILE; }
 size_t tc_c1_elems(int nt) { return (size_t)ntiles_lower(nt) * C1_TILE; }
 size_t tc_linv_elems(int nt) { return (size_t)(nt / 2) * LINV_SC; }
-// work-queue counters after the error flag: one per update and one per panel launch of the Cholesky
-int tc_queue_slots(int nt) { return nt; }
+// work-queue counters after the error flag: one per panel launch of the Cholesky (slots 0 .. nt/2 - 1),
+// one per update launch (nt/2 .. nt - 1), the streamed lauum's (nt), one per streamed trtri row
+// (nt + 1 + I2, I2 < nt/2)
+int tc_queue_slots(int nt) { return nt + 1 + nt / 2; }
 
 int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, float* Lc, float* Linv, float* Ms,
                       float* Mc, float* diag, int* status, int* d_err, cudaStream_t s)
@@ -1889,10 +2172,20 @@ int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* Ls, const float* Lin
 {
     if (nt % 2) { ctx->err = "tensor-core trtri needs an even tile count"; return CG_ERR_BAD_ARG; }
     int rc;
-    if ((rc = set_smem(ctx, trtri_tc_row))) return rc;
     const int nt2 = nt / 2;
+    if (ctx->tune.trtri == 1) {
+        if ((rc = set_smem(ctx, trtri_tc_stream))) return rc;
+    } else {
+        if ((rc = set_smem(ctx, trtri_tc_row))) return rc;
+    }
     for (int I2 = 1; I2 < nt2; ++I2) {  // the diagonal blocks M_II come from the Cholesky
-        trtri_tc_row<<<dim3(I2, B), NTH, tc_smem(), s>>>(I2, nt, Ls, Linv, Ms, Mc, d_err);
+        if (ctx->tune.trtri == 1) {
+            const int items = I2 * B;
+            trtri_tc_stream<<<items < ctx->sm_count ? items : ctx->sm_count, NTH, tc_smem(), s>>>(
+                I2, nt, B, Ls, Linv, Ms, Mc, d_err + 1 + nt + 1 + I2, d_err);
+        } else {
+            trtri_tc_row<<<dim3(I2, B), NTH, tc_smem(), s>>>(I2, nt, Ls, Linv, Ms, Mc, d_err);
+        }
         count_launch(ctx);
     }
     CG_CUDA_TRY(ctx, cudaGetLastError());
@@ -1904,9 +2197,19 @@ int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, const float* Mc,
 {
     if (nt % 2) { ctx->err = "tensor-core lauum needs an even tile count"; return CG_ERR_BAD_ARG; }
     int rc;
-    if ((rc = set_smem(ctx, lauum_tc))) return rc;
-    const int nt2 = nt / 2;
-    lauum_tc<<<dim3(nt2 * (nt2 + 1) / 2, B), NTH, tc_smem(), s>>>(nt, Ms, V, d_err);
+    const int nt2 = nt / 2, nsup = nt2 * (nt2 + 1) / 2;
+    if (ctx->tune.lauum == 1) {
+        if ((rc = set_smem(ctx, lauum_tc_stream))) return rc;
+        const int items = nsup * B;
+        lauum_tc_stream<<<items < ctx->sm_count ? items : ctx->sm_count, NTH, tc_smem(), s>>>(
+            nt, B, Ms, Mc, V, d_err + 1 + nt, d_err);
+    } else if (ctx->tune.lauum == 2) {
+        if ((rc = set_smem(ctx, lauum_tc<A_SMEM_C1>))) return rc;
+        lauum_tc<A_SMEM_C1><<<dim3(nsup, B), NTH, tc_smem(), s>>>(nt, Ms, Mc, V, d_err);
+    } else {
+        if ((rc = set_smem(ctx, lauum_tc<A_REG_SC>))) return rc;
+        lauum_tc<A_REG_SC><<<dim3(nsup, B), NTH, tc_smem(), s>>>(nt, Ms, Mc, V, d_err);
+    }
     count_launch(ctx);
     CG_CUDA_TRY(ctx, cudaGetLastError());
     return CG_OK;

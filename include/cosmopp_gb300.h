@@ -249,7 +249,11 @@ int cg_stage_times(cg_ctx* ctx, double* ms);
 /* Knobs, by name.  Launch shapes (results change only in rounding order): "fwd_ctas",
    "chol_ctas", "panel_ctas" (persistent CTA counts of the tensor-core contraction, the Cholesky's
    off-diagonal work queue and its panel solve; 0 = one per SM), "adj" (tensor-core adjoint
-   variant 0..3).  Accuracy choices, never changed by cg_autotune: "fwd" (forward contraction:
+   variant 0..3), "lauum" (2, the default: one CTA per block of C^-1 with the A operand split on
+   chip; 0: A read pre-split; 1: persistent CTAs over a work queue, A split on chip; 0 differs from
+   the others below 2^-22 of an entry), "trtri" (0, the default: one CTA per block of L^-1;
+   1: persistent CTAs over a work queue with each block's two products chained on chip, identical
+   results).  Accuracy choices, never changed by cg_autotune: "fwd" (forward contraction:
    0 = FP32 FMA, the default; 1 = tensor cores, faster, but its one-way accumulation rounding
    biases the whitened matrix by a few ulp of |A - I|, about 1e-3 in -2lnL at nside 16 for C_l
    a factor e from the reference point), "diag_sq" (1, the default: the Cholesky's diagonal

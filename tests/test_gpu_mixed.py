@@ -227,7 +227,7 @@ def test_tuning_knobs_autotune_and_file(tmp_path):
     with _ctx(g, "mixed", B, cl_ref=g["cls"][0], recenter="fixed") as ctx:
         base = ctx.loglike(cls, g["d"], grad=True)
         for knob, vals in (("fwd", (0, 1)), ("chol_ctas", (8, 300)), ("panel_ctas", (5, 300)), ("adj", (1, 2, 3)),
-                           ("fwd_ctas", (7,))):
+                           ("fwd_ctas", (7,)), ("lauum", (1, 2, 0)), ("trtri", (1, 0))):
             keep = ctx.tune_get(knob)
             for v in vals:
                 ctx.tune_set(knob, v)
@@ -307,3 +307,23 @@ def test_fixed_reference_calls_replay_one_cuda_graph():
         auto.loglike(cls, g["d"])
         auto.loglike(cls, g["d"])
         assert auto.graph_replays() == 0
+
+
+def test_work_queue_variants_of_trtri_and_lauum():
+    """The streamed triangular inverse (persistent CTAs, the two products of each block chained on
+    chip) computes the same operands in the same order as the one-CTA-per-block kernel: identical
+    results.  The streamed lauum splits its A operand on chip (low part unrounded): within rounding."""
+    g = load_golden("nside16_lmax47")
+    B = 40
+    cls = W.lognormal_batch(g["cls"][0], B, 31)
+    with _ctx(g, "mixed", B, cl_ref=g["cls"][0], recenter="fixed") as ctx:
+        base = ctx.loglike(cls, g["d"], grad=True)
+        ctx.tune_set("trtri", 1)
+        tr = ctx.loglike(cls, g["d"], grad=True)
+        ctx.tune_set("lauum", 1)
+        both = ctx.loglike(cls, g["d"], grad=True)
+    assert np.all(tr["status"] == 0) and np.all(both["status"] == 0)
+    assert np.array_equal(tr["m2lnl"], base["m2lnl"]) and np.array_equal(tr["grad"], base["grad"])
+    assert np.abs(both["m2lnl"] - base["m2lnl"]).max() <= 1e-6
+    dg = np.abs(both["grad"][:, 2:] - base["grad"][:, 2:]) / np.abs(base["grad"][:, 2:]).max(axis=1, keepdims=True)
+    assert dg.max() <= 1e-5
