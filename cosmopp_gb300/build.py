@@ -15,7 +15,7 @@ OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libcosmopp_gb300.so")
 
-CU_SOURCES = ["k_chol.cu", "k_fp64.cu", "k_mixed.cu", "k_noalloc.cu", "k_tc.cu"]
+CU_SOURCES = ["k_chol.cu", "k_fp64.cu", "k_hmc.cu", "k_mixed.cu", "k_noalloc.cu", "k_tc.cu"]
 CXX_SOURCES = ["cg_abi.cpp", "cg_geometry.cpp", "cg_hmc.cpp", "cg_mcmc.cpp", "cg_tune.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

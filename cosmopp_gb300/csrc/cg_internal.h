@@ -119,6 +119,7 @@ struct Tune {
     int lauum = 2;        // lauum: one CTA per block with the A operand from the FP32 copy, split on chip (2),
                           // or from the split copy (0); persistent CTAs over a work queue (1)
     int trtri = 0;        // 0 = one CTA per trtri block, 1 = persistent CTAs over a work queue (same results)
+    int hmc_device = 1;   // cg_hmc_run: 1 = leapfrog resident on the device, 0 = the host loop (same chains)
 };
 
 // the argument set a captured mixed call was recorded for
@@ -249,6 +250,17 @@ size_t tc_linv_elems(int nt);    // floats per matrix of the Linv blocks
 // The tensor-core entry points take d_err = [0] the error flag (set when a bounded wait gave up),
 // then tc_queue_slots(nt) work-queue counters, all zero before the call.
 int tc_queue_slots(int nt);
+
+// device-resident leapfrog of cg_hmc_run (k_hmc.cu): half kick + drift + C_l = exp(x); gradient in
+// ln C_l + half kick; dH per chain; accepted proposals into the chains' state
+int hmc_launch_drift(cg_ctx* ctx, int B, int np, double t, double* p, const double* g, double* x, const double* mass,
+                     const double* tmpl, double* cl, cudaStream_t s);
+int hmc_launch_kick(cg_ctx* ctx, int B, int np, double t, int kick, double* p, double* g, const double* gcl,
+                    const double* cl, const int* st, double* m2lnl, cudaStream_t s);
+int hmc_launch_energy(cg_ctx* ctx, int B, int np, const double* p, const double* mass, const double* un,
+                      const double* u, const double* kin0, double* dh, cudaStream_t s);
+int hmc_launch_accept(cg_ctx* ctx, int B, int np, const int* flag, const double* xn, const double* gn,
+                      const double* un, double* x, double* g, double* u, cudaStream_t s);
 int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, float* Lc, float* Linv, float* Ms,
                       float* Mc, float* diag, int* status, int* d_err, cudaStream_t s);
 int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* Ls, const float* Linv, float* Ms, float* Mc,

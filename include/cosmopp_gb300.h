@@ -164,7 +164,12 @@ int cg_reference_count(const cg_ctx* ctx);
    derivative of -2lnL (halved, as the reference does), and accepts with
    exp(-dH/2), dH of -2lnL + p^2/m.  jitter != 0 draws tau in (0, tau] and
    ceil(nleap U) steps each iteration like the reference.  Every leapfrog step is
-   one batched cg_loglike call over all chains.  chain receives
+   one batched -2lnL + gradient call over all chains.  The leapfrog is resident on the
+   device: positions, momenta and gradients stay in device memory through a trajectory,
+   whose steps are launches only; per iteration the momenta go to the device and the
+   proposals' dH, -2lnL and x come back for the acceptance draws.  Knob "hmc_device" = 0
+   runs the same likelihood through cg_hmc_sample's host loop; the chains are the same
+   bit for bit (C_l = exp(x) by one routine on both sides).  chain receives
    [niter+1][nchains][lmax]: -2lnL then x for every chain after every iteration
    (row 0 = the start); accept_rate [nchains] (nullable). */
 int cg_hmc_run(cg_ctx* ctx, const double* map, int nchains, const double* x0, const double* cl_template,
