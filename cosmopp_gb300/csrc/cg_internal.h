@@ -266,7 +266,7 @@ int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, flo
 int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* Ls, const float* Linv, float* Ms, float* Mc,
                    int* d_err, cudaStream_t s);
 int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, const float* Mc, float* V, int* d_err,
-                   cudaStream_t s);
+                   const double* y, int ystride, float2* part, cudaStream_t s);
 // part[t][b][l] = sum_e w_e V_b[e] Ubar_l[e] over lower tile t (k_tc.cu), for lp % 16 == 0, lp <= 96
 bool adjoint_tc_ok(int lp);
 int adjoint_contract_tc(cg_ctx* ctx, int B, int nt, int lp, const float* U, const float* V, size_t strideA,

@@ -829,19 +829,25 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
     count_launch(ctx);
     stage_mark(ctx, ST_TRTRI, s);
     if ((rc = tiled_trtri_tc(ctx, B, nt, w.Ls, w.Linv, w.Ms, w.Mc, w.tcerr, s))) return rc;
-    stage_mark(ctx, ST_LAUUM, s);
-    if ((rc = tiled_lauum_tc(ctx, B, nt, w.Ms, w.Mc, w.V, w.tcerr, s))) return rc;
-    stage_mark(ctx, ST_SOLVE, s);
-    // x = V y; r = y - A x; x += V r  (the partials buffer holds double-float pairs here)
+    // x = V y; r = y - A x; x += V r  (the partials buffer holds double-float pairs here); the first
+    // pass's tile partials come from lauum's epilogue, which still holds each block of V in registers
+    // (not from the work-queue lauum, whose epilogues run beside the next block's K loop)
     float2* pf = reinterpret_cast<float2*>(w.part);
-    symv_partials<false><<<dim3((ntile + SYMV_TPB - 1) / SYMV_TPB, B), 256, 0, s>>>(nt, w.V, tiled, w.y, N, pf);
+    const bool fused = ctx->tune.lauum != 1;
+    stage_mark(ctx, ST_LAUUM, s);
+    if ((rc = tiled_lauum_tc(ctx, B, nt, w.Ms, w.Mc, w.V, w.tcerr, fused ? w.y : nullptr, N, pf, s))) return rc;
+    stage_mark(ctx, ST_SOLVE, s);
+    if (!fused) {
+        symv_partials<false><<<dim3((ntile + SYMV_TPB - 1) / SYMV_TPB, B), 256, 0, s>>>(nt, w.V, tiled, w.y, N, pf);
+        count_launch(ctx);
+    }
     symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, pf, w.x, N, nullptr, 1.0);
     symv_partials<true><<<dim3((ntile + SYMV_TPB - 1) / SYMV_TPB, B), 256, 0, s>>>(nt, w.A, tiled, w.x, N, pf);
     symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, pf, w.r, N, w.y, -1.0);
     symv_partials<false><<<dim3((ntile + SYMV_TPB - 1) / SYMV_TPB, B), 256, 0, s>>>(nt, w.V, tiled, w.r, N, pf);
     symv_reduce<<<dim3(nt, B), 64, 0, s>>>(nt, pf, w.x, N, w.x, 1.0);
     chi2_mixed<<<B, 256, 0, s>>>(n, N, N, w.y, w.x, w.ld, d_m2lnl, d_chi2, d_logdet);
-    count_launch(ctx, 7);
+    count_launch(ctx, 6);
     stage_mark(ctx, ST_ADJOINT, s);
     if (d_grad) {
         if (adjoint_tc_ok(lp)) {

@@ -1468,12 +1468,18 @@ __global__ void __launch_bounds__(NTH, 1) trtri_tc_stream(int I2, int nt, int B,
 // AM = A_SMEM_C1 (the default): the A operand from the FP32 canonical copy Mc through the
 // shared-memory ring, split on chip, its low parts left unrounded for the tensor core; A_REG_SC: from
 // the split copy Ms, low parts rounded to TF32 when it was written.
+// y (nullable): the solve's first pass x = V y folded into the epilogue, from the block still in
+// registers: for each stored 64x64 tile (I, J) of V, part[t][0][r] = (V_IJ y_J)[r] and, for I != J,
+// part[t][1][c] = (V_IJ^T y_I)[c] (zero on diagonal tiles), as FP32 sums with a zero low word: the
+// layout and meaning of tile::symv_partials<false>, whose read of V it saves.
 template <int AM>
 __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restrict__ Ms, const float* __restrict__ Mc,
-                                                   float* __restrict__ V, int* __restrict__ err)
+                                                   float* __restrict__ V, int* __restrict__ err,
+                                                   const double* __restrict__ y, int ystride, float2* __restrict__ part)
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ TcCtl ctl;
+    __shared__ float ys[2][128];  // y at the block's columns (J) and rows (I), fused solve pass
     int I2, J2;
     tile_coords(blockIdx.x, I2, J2);
     const int b = blockIdx.y;
@@ -1521,6 +1527,44 @@ __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restri
         tc_kloop<A_REG_SC>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
     }
     store_block(R, V + (size_t)b * ntile * TILE_ELEMS, I2, J2, 1.f);
+    if (y) {
+        if (threadIdx.x < 256) {
+            const int w = threadIdx.x / 128, k = threadIdx.x % 128;
+            ys[w][k] = (float)y[(size_t)b * ystride + (w == 0 ? 2 * J2 : 2 * I2) * TS + k];
+        }
+        __syncthreads();  // every MMA and copy of the K loop is done: the ring is free for the column sums
+        float* red = reinterpret_cast<float*>(smem_raw);  // [h][row half][column][65]
+        float2* pb = part + (size_t)b * ntile * 2 * TS;
+        if (threadIdx.x < NPROD) {
+            const int row = threadIdx.x % 128, h = threadIdx.x / 128;
+            const int ti = 2 * I2 + row / 64, tj = 2 * J2 + h;
+            if (tj <= ti) {
+                float a = 0.f;
+#pragma unroll
+                for (int j = 0; j < 64; ++j) a = fmaf(R[j], ys[0][64 * h + j], a);
+                pb[(size_t)tile_index(ti, tj) * 2 * TS + row % 64] = make_float2(a, 0.f);
+                if (ti != tj) {
+                    const float yr = ys[1][row];
+                    float* rr = red + (size_t)((h * 2 + row / 64) * 64) * 65 + row % 64;
+#pragma unroll
+                    for (int j = 0; j < 64; ++j) rr[j * 65] = R[j] * yr;
+                }
+            }
+        }
+        __syncthreads();
+        if (threadIdx.x < NPROD) {
+            const int hh = threadIdx.x / 128, half = (threadIdx.x / 64) % 2, c = threadIdx.x % 64;
+            const int ti = 2 * I2 + half, tj = 2 * J2 + hh;
+            if (tj <= ti) {
+                float sum = 0.f;
+                if (ti != tj) {
+                    const float* rc = red + (size_t)((hh * 2 + half) * 64 + c) * 65;
+                    for (int r = 0; r < 64; ++r) sum += rc[r];
+                }
+                pb[(size_t)tile_index(ti, tj) * 2 * TS + TS + c] = make_float2(sum, 0.f);
+            }
+        }
+    }
     tc_end(tm);
 }
 
@@ -2193,7 +2237,7 @@ int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* Ls, const float* Lin
 }
 
 int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, const float* Mc, float* V, int* d_err,
-                   cudaStream_t s)
+                   const double* y, int ystride, float2* part, cudaStream_t s)
 {
     if (nt % 2) { ctx->err = "tensor-core lauum needs an even tile count"; return CG_ERR_BAD_ARG; }
     int rc;
@@ -2205,10 +2249,10 @@ int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, const float* Mc,
             nt, B, Ms, Mc, V, d_err + 1 + nt, d_err);
     } else if (ctx->tune.lauum == 2) {
         if ((rc = set_smem(ctx, lauum_tc<A_SMEM_C1>))) return rc;
-        lauum_tc<A_SMEM_C1><<<dim3(nsup, B), NTH, tc_smem(), s>>>(nt, Ms, Mc, V, d_err);
+        lauum_tc<A_SMEM_C1><<<dim3(nsup, B), NTH, tc_smem(), s>>>(nt, Ms, Mc, V, d_err, y, ystride, part);
     } else {
         if ((rc = set_smem(ctx, lauum_tc<A_REG_SC>))) return rc;
-        lauum_tc<A_REG_SC><<<dim3(nsup, B), NTH, tc_smem(), s>>>(nt, Ms, Mc, V, d_err);
+        lauum_tc<A_REG_SC><<<dim3(nsup, B), NTH, tc_smem(), s>>>(nt, Ms, Mc, V, d_err, y, ystride, part);
     }
     count_launch(ctx);
     CG_CUDA_TRY(ctx, cudaGetLastError());
