@@ -1485,6 +1485,9 @@ __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restri
     const int b = blockIdx.y;
     const size_t ntile = (size_t)ntiles_lower(nt);
     const float* Mb = Ms + (size_t)b * ntile * SC_TILE;
+    float ypre = 0.f;  // this thread's y entry for the epilogue, loaded before the K loop hides its latency
+    if (y && threadIdx.x < 256)
+        ypre = (float)__ldg(y + (size_t)b * ystride + (threadIdx.x < 128 ? 2 * J2 : 2 * I2) * TS + threadIdx.x % 128);
     const uint32_t tm = tc_begin(ctl);
     const int k0 = 2 * I2;  // first tile row with a non-zero M_k,I
     const int nchunks = (nt - k0) * (TS / KC);
@@ -1528,10 +1531,7 @@ __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restri
     }
     store_block(R, V + (size_t)b * ntile * TILE_ELEMS, I2, J2, 1.f);
     if (y) {
-        if (threadIdx.x < 256) {
-            const int w = threadIdx.x / 128, k = threadIdx.x % 128;
-            ys[w][k] = (float)y[(size_t)b * ystride + (w == 0 ? 2 * J2 : 2 * I2) * TS + k];
-        }
+        if (threadIdx.x < 256) ys[threadIdx.x / 128][threadIdx.x % 128] = ypre;
         __syncthreads();  // every MMA and copy of the K loop is done: the ring is free for the column sums
         float* red = reinterpret_cast<float*>(smem_raw);  // [h][row half][column][65]
         float2* pb = part + (size_t)b * ntile * 2 * TS;
