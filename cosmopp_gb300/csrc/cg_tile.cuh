@@ -145,18 +145,30 @@ __global__ void __launch_bounds__(256) symv_partials(int nt, const float* __rest
         }
         __syncthreads();
         float ah = 0.f, al = 0.f, th = 0.f, tl = 0.f;
-        for (int c = q; c < TS; c += 4) {
-            const float va = s[c][r], vt = s[r][c];
-            if (DF) {
-                const float p = va * svh[0][c];
+        if (DF) {
+            // two interleaved double-float chains per direction (columns q + 8i and q + 8i + 4), merged
+            // at the end: half the dependent additions in a row
+            float bh = 0.f, bl = 0.f, uh = 0.f, ul = 0.f;
+#pragma unroll
+            for (int c = q; c < TS; c += 8) {
+                const float va = s[c][r], vt = s[r][c], wa = s[c + 4][r], wt = s[r][c + 4];
+                const float p = va * svh[0][c], pw = wa * svh[0][c + 4];
                 df_add(ah, al, p);
+                df_add(bh, bl, pw);
                 al += fmaf(va, svh[0][c], -p) + va * svl[0][c];
-                const float pt = vt * svh[1][c];
+                bl += fmaf(wa, svh[0][c + 4], -pw) + wa * svl[0][c + 4];
+                const float pt = vt * svh[1][c], ptw = wt * svh[1][c + 4];
                 df_add(th, tl, pt);
+                df_add(uh, ul, ptw);
                 tl += fmaf(vt, svh[1][c], -pt) + vt * svl[1][c];
-            } else {
-                ah = fmaf(va, svh[0][c], ah);
-                th = fmaf(vt, svh[1][c], th);
+                ul += fmaf(wt, svh[1][c + 4], -ptw) + wt * svl[1][c + 4];
+            }
+            df_merge(ah, al, bh, bl);
+            df_merge(th, tl, uh, ul);
+        } else {
+            for (int c = q; c < TS; c += 4) {
+                ah = fmaf(s[c][r], svh[0][c], ah);
+                th = fmaf(s[r][c], svh[1][c], th);
             }
         }
         redh[q][0][r] = ah;
