@@ -1238,7 +1238,6 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
     // a diagonal block
     const int I2 = J2, b = blockIdx.x;
     const float* Ab = A + (size_t)b * ntile * TILE_ELEMS;
-    float* Lb = Ls + (size_t)b * ntile * SC_TILE;
     float* Lcb = Lc + (size_t)b * ntile * C1_TILE;
     const uint32_t tm = tc_begin(ctl);
     auto fa = [&](int c, const float*& top, const float*& bot, int& kc) {
@@ -1277,15 +1276,8 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
     __syncthreads();
     factor_block128(s, inv, tmp, &ctl.bad);
     float v[64];
-    if (prod) {   // L_JJ into the three lower SC tiles, strict upper of the diagonal tiles zeroed
-        const int ti = 2 * J2 + row / 64, tj = 2 * J2 + h;
-        if (tj <= ti) {
-#pragma unroll
-            for (int j = 0; j < 64; ++j) v[j] = (row >= 64 * h + j) ? s[(64 * h + j) * 129 + row] : 0.f;
-            st_sc_row(Lb + (size_t)tile_index(ti, tj) * SC_TILE, row % 64, v, 1.f);
-            st_c1_row(Lcb + (size_t)tile_index(ti, tj) * C1_TILE, row % 64, v, 1.f);
-        }
-    }
+    // L_JJ itself is not stored: no later step reads L's diagonal blocks (the updates and trtri
+    // take L's off-diagonal panels, the panel solves and trtri the inverse Linv_J)
     if (threadIdx.x < 128) diag[(size_t)b * nt * TS + J2 * 128 + row] = s[row * 129 + row];
     if (prod) {   // Linv_J: row `row`, K columns 64h .. 64h+63 (chunks 2h, 2h+1)
         float* li = Linv + ((size_t)b * nt2 + J2) * LINV_SC;
