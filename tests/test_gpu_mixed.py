@@ -1,5 +1,5 @@
 """Parity of the batched mixed-precision path: every -2lnL within the
-spec bar |delta| <= 1e-3 of the FP64 reference values (golden fixtures
+mixed-path bar |delta| <= 1e-3 of the FP64 reference values (golden fixtures
 from the reference's own code, and the FP64 CUDA path, itself pinned to the
 reference to 1e-6), every gradient component within 1e-4 of the FP64 adjoint
 relative to max(|g_l|, s_l), s_l the gradient's minimum statistical scatter
