@@ -362,9 +362,9 @@ def run_ours(args):
                 "peak_note": "measured TF32 rate of the kernel's MMA form / 3 (three MMAs per FP32-accurate "
                              "product); bf16-derived alternative %.1f" % (peaks["bf16_tflops_sustained"] / 6.0),
                 # ncu dram__bytes_read + dram__bytes_write of one batch-32 Cholesky, x B / 32 (traffic grows
-                # with the batch): the 20 update launches measured (4.154 GB), the 19 panel launches from one
+                # with the batch): the 20 update launches measured (4.146 GB), the 19 panel launches from one
                 # launch's bytes per block times the block count (0.849 GB); profiles/tc_kernels_nside16_b32.md
-                "traffic": 5.003e9 * B / 32.0 if args.workload == WORKLOAD else None,
+                "traffic": 4.995e9 * B / 32.0 if args.workload == WORKLOAD else None,
                 "traffic_unit": "bytes per step (whole Cholesky stage)"}
         roof["frac"] = roof["achieved"] / roof["peak"]
         # the forward contraction A_b = I + sum_l eps_bl Ubar_l: reads the FP32 table once
