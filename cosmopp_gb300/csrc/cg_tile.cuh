@@ -96,6 +96,55 @@ __device__ __forceinline__ void df_merge(float& hi, float& lo, float h2, float l
     hi = t;
 }
 
+// Packed two-lane FP32 operations (each lane rounded to nearest on its own, as the scalar operation
+// would be, and never contracted into a fused operation): the residual pass keeps its row and
+// column double-float sums as the two lanes of one pair, so each operation serves both.
+__device__ __forceinline__ float2 pk_add(float2 a, float2 b)
+{
+    asm("{\n\t.reg .b64 ra, rb;\n\tmov.b64 ra, {%0, %1};\n\tmov.b64 rb, {%2, %3};\n\t"
+        "add.rn.f32x2 ra, ra, rb;\n\tmov.b64 {%0, %1}, ra;\n\t}"
+        : "+f"(a.x), "+f"(a.y)
+        : "f"(b.x), "f"(b.y));
+    return a;
+}
+__device__ __forceinline__ float2 pk_sub(float2 a, float2 b)
+{
+    asm("{\n\t.reg .b64 ra, rb;\n\tmov.b64 ra, {%0, %1};\n\tmov.b64 rb, {%2, %3};\n\t"
+        "sub.rn.f32x2 ra, ra, rb;\n\tmov.b64 {%0, %1}, ra;\n\t}"
+        : "+f"(a.x), "+f"(a.y)
+        : "f"(b.x), "f"(b.y));
+    return a;
+}
+__device__ __forceinline__ float2 pk_mul(float2 a, float2 b)
+{
+    asm("{\n\t.reg .b64 ra, rb;\n\tmov.b64 ra, {%0, %1};\n\tmov.b64 rb, {%2, %3};\n\t"
+        "mul.rn.f32x2 ra, ra, rb;\n\tmov.b64 {%0, %1}, ra;\n\t}"
+        : "+f"(a.x), "+f"(a.y)
+        : "f"(b.x), "f"(b.y));
+    return a;
+}
+// a * b + c, one rounding per lane
+__device__ __forceinline__ float2 pk_fma(float2 a, float2 b, float2 c)
+{
+    asm("{\n\t.reg .b64 ra, rb, rc;\n\tmov.b64 ra, {%0, %1};\n\tmov.b64 rb, {%2, %3};\n\t"
+        "mov.b64 rc, {%4, %5};\n\tfma.rn.f32x2 ra, ra, rb, rc;\n\tmov.b64 {%0, %1}, ra;\n\t}"
+        : "+f"(a.x), "+f"(a.y)
+        : "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return a;
+}
+// (hi, lo) += a * (bh + bl) in double-float arithmetic: the product a bh exactly as p + (a bh - p)
+// (one fused operation), p added to hi by Knuth's two-sum, every error term folded into lo
+__device__ __forceinline__ void pk_df_madd(float2& hi, float2& lo, float2 a, float2 bh, float2 bl)
+{
+    const float2 p = pk_mul(a, bh);
+    const float2 t = pk_add(hi, p);
+    const float2 z = pk_sub(t, hi);
+    const float2 e = pk_add(pk_sub(hi, pk_sub(t, z)), pk_sub(p, z));
+    const float2 perr = pk_fma(a, bh, make_float2(-p.x, -p.y));
+    lo = pk_add(lo, pk_add(e, pk_fma(a, bl, perr)));
+    hi = t;
+}
+
 // One CTA walks SYMV_TPB consecutive tiles of one batch element: 128-bit loads, the next tile
 // prefetched into registers while the current one is reduced.  grid (ceil(tiles / SYMV_TPB), B).
 // The four partial sums of a row are combined in FP32 (double-float for DF) and converted to FP64
@@ -146,25 +195,19 @@ __global__ void __launch_bounds__(256) symv_partials(int nt, const float* __rest
         __syncthreads();
         float ah = 0.f, al = 0.f, th = 0.f, tl = 0.f;
         if (DF) {
-            // two interleaved double-float chains per direction (columns q + 8i and q + 8i + 4), merged
-            // at the end: half the dependent additions in a row
-            float bh = 0.f, bl = 0.f, uh = 0.f, ul = 0.f;
+            // row (lane x) and column (lane y) sums as packed pairs, in two interleaved chains
+            // (columns q + 8i and q + 8i + 4) merged at the end: half the dependent additions in a row
+            float2 H1 = make_float2(0.f, 0.f), L1 = H1, H2 = H1, L2 = H1;
 #pragma unroll
             for (int c = q; c < TS; c += 8) {
-                const float va = s[c][r], vt = s[r][c], wa = s[c + 4][r], wt = s[r][c + 4];
-                const float p = va * svh[0][c], pw = wa * svh[0][c + 4];
-                df_add(ah, al, p);
-                df_add(bh, bl, pw);
-                al += fmaf(va, svh[0][c], -p) + va * svl[0][c];
-                bl += fmaf(wa, svh[0][c + 4], -pw) + wa * svl[0][c + 4];
-                const float pt = vt * svh[1][c], ptw = wt * svh[1][c + 4];
-                df_add(th, tl, pt);
-                df_add(uh, ul, ptw);
-                tl += fmaf(vt, svh[1][c], -pt) + vt * svl[1][c];
-                ul += fmaf(wt, svh[1][c + 4], -ptw) + wt * svl[1][c + 4];
+                pk_df_madd(H1, L1, make_float2(s[c][r], s[r][c]), make_float2(svh[0][c], svh[1][c]),
+                           make_float2(svl[0][c], svl[1][c]));
+                pk_df_madd(H2, L2, make_float2(s[c + 4][r], s[r][c + 4]),
+                           make_float2(svh[0][c + 4], svh[1][c + 4]), make_float2(svl[0][c + 4], svl[1][c + 4]));
             }
-            df_merge(ah, al, bh, bl);
-            df_merge(th, tl, uh, ul);
+            ah = H1.x; al = L1.x; th = H1.y; tl = L1.y;
+            df_merge(ah, al, H2.x, L2.x);
+            df_merge(th, tl, H2.y, L2.y);
         } else {
             for (int c = q; c < TS; c += 4) {
                 ah = fmaf(s[c][r], svh[0][c], ah);
