@@ -209,10 +209,12 @@ __global__ void __launch_bounds__(256) symv_partials(int nt, const float* __rest
             df_merge(ah, al, H2.x, L2.x);
             df_merge(th, tl, H2.y, L2.y);
         } else {
-            for (int c = q; c < TS; c += 4) {
-                ah = fmaf(s[c][r], svh[0][c], ah);
-                th = fmaf(s[r][c], svh[1][c], th);
-            }
+            float2 H = make_float2(0.f, 0.f);  // (row, column) sums, one packed FMA per column
+#pragma unroll
+            for (int c = q; c < TS; c += 4)
+                H = pk_fma(make_float2(s[c][r], s[r][c]), make_float2(svh[0][c], svh[1][c]), H);
+            ah = H.x;
+            th = H.y;
         }
         redh[q][0][r] = ah;
         redl[q][0][r] = al;
