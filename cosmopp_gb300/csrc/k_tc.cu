@@ -122,8 +122,10 @@ __device__ __forceinline__ void drain(uint32_t tm, uint32_t col, float (&R)[64])
 struct TcCtl {
     uint64_t mma_bar[NAST];   // stage: the MMAs of its chunk completed (its A and B stages are free)
     uint64_t acc_free[2];     // pair parity: the pair's accumulator was drained (one arrival per producer warp)
-    uint64_t a_full[NAST];    // A stage: the chunk's A is in tensor memory (one arrival per producer warp)
-    uint64_t b_full[NSTB];    // B stage landed
+    uint64_t a_full[NAST];    // stage: the chunk's A is in tensor memory (one arrival per producer warp) and,
+                              // where a copy thread fills the B stage, its B landed (that thread's arrival
+                              // with the copies' bytes), so the issuer polls one barrier per chunk
+    uint64_t b_full[NSTB];    // (unused: the B copies complete on a_full)
     uint64_t b_empty[NSTB];   // B stage's MMAs completed
     uint64_t as_full[NSTA];   // A shared-memory stage landed
     uint64_t as_empty[NSTA];  // A shared-memory stage read by every producer warp
@@ -134,11 +136,12 @@ struct TcCtl {
     int bad;
 };
 
-__device__ __forceinline__ void init_bars(TcCtl& ctl)
+// bcopy: a copy thread fills the B stages (B_COPY), so a_full also counts its arrival
+__device__ __forceinline__ void init_bars(TcCtl& ctl, bool bcopy = true)
 {
     for (int i = 0; i < NAST; ++i) mbar_init(&ctl.mma_bar[i], 1);
     for (int i = 0; i < 2; ++i) mbar_init(&ctl.acc_free[i], NPROD / 32);
-    for (int i = 0; i < NAST; ++i) mbar_init(&ctl.a_full[i], NPROD / 32);
+    for (int i = 0; i < NAST; ++i) mbar_init(&ctl.a_full[i], NPROD / 32 + (bcopy ? 1 : 0));
     for (int i = 0; i < NSTB; ++i) {
         mbar_init(&ctl.b_full[i], 1);
         mbar_init(&ctl.b_empty[i], 1);
@@ -155,11 +158,11 @@ __device__ __forceinline__ void init_bars(TcCtl& ctl)
     fence_mbar_init();
 }
 
-__device__ __forceinline__ uint32_t tc_begin(TcCtl& ctl)
+__device__ __forceinline__ uint32_t tc_begin(TcCtl& ctl, bool bcopy = true)
 {
     if (threadIdx.x < 32) tmem_alloc(&ctl.tbase, TMEM_COLS);
     if (threadIdx.x == 0) {
-        init_bars(ctl);
+        init_bars(ctl, bcopy);
         ctl.bad = 0;
     }
     fence_before();
@@ -422,8 +425,7 @@ template <int BMODE = B_COPY, class W>
 __device__ __forceinline__ void issue_chunk(int g, W& wait, TcCtl& ctl, uint32_t tm, uint32_t sb)
 {
     const int st = g % NAST, sbi = g % NSTB, pr = g >> 1;
-    wait(&ctl.a_full[st], (g / NAST) & 1);
-    if constexpr (BMODE == B_COPY) wait(&ctl.b_full[sbi], (g / NSTB) & 1);
+    wait(&ctl.a_full[st], (g / NAST) & 1);  // A put and (B_COPY) B landed: one barrier
     if ((g & 1) == 0 && pr >= 2) wait(&ctl.acc_free[pr & 1], ((pr - 2) >> 1) & 1);
     fence_after();
     const uint32_t bh = sb + sbi * STB_BYTES, bl = bh + STB_BYTES / 2;
@@ -461,7 +463,7 @@ __device__ __forceinline__ void copy_b(int g, W& wait, TcCtl& ctl, uint32_t sb, 
     if constexpr (BMODE == B_COPY) {
         const int sbi = g % NSTB;
         if (g >= NSTB) wait(&ctl.b_empty[sbi], ((g / NSTB) - 1) & 1);
-        fb(sb + sbi * STB_BYTES, &ctl.b_full[sbi]);
+        fb(sb + sbi * STB_BYTES, &ctl.a_full[sbi]);  // stage sbi == the chunk's A stage (NSTB == NAST)
     }
 }
 
@@ -1239,7 +1241,7 @@ __global__ void __launch_bounds__(NTH, 1) chol_tc_update(int J2, int nt, int B, 
     const int I2 = J2, b = blockIdx.x;
     const float* Ab = A + (size_t)b * ntile * TILE_ELEMS;
     float* Lcb = Lc + (size_t)b * ntile * C1_TILE;
-    const uint32_t tm = tc_begin(ctl);
+    const uint32_t tm = tc_begin(ctl, false);  // B_FROM_A: the producers fill the B stages themselves
     auto fa = [&](int c, const float*& top, const float*& bot, int& kc) {
         top = Lcb + (size_t)tile_index(2 * I2, c / 2) * C1_TILE;
         bot = Lcb + (size_t)tile_index(2 * I2 + 1, c / 2) * C1_TILE;
