@@ -1473,7 +1473,7 @@ __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restri
 {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     __shared__ TcCtl ctl;
-    __shared__ float ys[2][128];  // y at the block's columns (J) and rows (I), fused solve pass
+    __shared__ __align__(16) float ys[2][128];  // y at the block's columns (J) and rows (I), fused solve pass
     int I2, J2;
     tile_coords(blockIdx.x, I2, J2);
     const int b = blockIdx.y;
@@ -1527,21 +1527,41 @@ __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restri
     if (y) {
         if (threadIdx.x < 256) ys[threadIdx.x / 128][threadIdx.x % 128] = ypre;
         __syncthreads();  // every MMA and copy of the K loop is done: the ring is free for the column sums
-        float* red = reinterpret_cast<float*>(smem_raw);  // [h][row half][column][65]
+        float(*red)[64] = reinterpret_cast<float(*)[64]>(smem_raw);  // [producer warp][column]: warp column sums
         float2* pb = part + (size_t)b * ntile * 2 * TS;
         if (threadIdx.x < NPROD) {
-            const int row = threadIdx.x % 128, h = threadIdx.x / 128;
-            const int ti = 2 * I2 + row / 64, tj = 2 * J2 + h;
+            const int row = threadIdx.x % 128, h = threadIdx.x / 128, lane = threadIdx.x % 32;
+            const int ti = 2 * I2 + row / 64, tj = 2 * J2 + h;  // the same for the whole warp
             if (tj <= ti) {
-                float a = 0.f;
+                // row sum V_IJ(row, :) y_J in four interleaved chains
+                float a[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-                for (int j = 0; j < 64; ++j) a = fmaf(R[j], ys[0][64 * h + j], a);
-                pb[(size_t)tile_index(ti, tj) * 2 * TS + row % 64] = make_float2(a, 0.f);
+                for (int j = 0; j < 64; j += 4) {
+                    const float4 yv = *reinterpret_cast<const float4*>(&ys[0][64 * h + j]);
+                    a[0] = fmaf(R[j], yv.x, a[0]);
+                    a[1] = fmaf(R[j + 1], yv.y, a[1]);
+                    a[2] = fmaf(R[j + 2], yv.z, a[2]);
+                    a[3] = fmaf(R[j + 3], yv.w, a[3]);
+                }
+                pb[(size_t)tile_index(ti, tj) * 2 * TS + row % 64] = make_float2((a[0] + a[1]) + (a[2] + a[3]), 0.f);
                 if (ti != tj) {
+                    // column sums y_I(rows)^T V_IJ over the warp's 32 rows: five halving exchange steps,
+                    // after which lane L holds the sums of columns 2L and 2L + 1
                     const float yr = ys[1][row];
-                    float* rr = red + (size_t)((h * 2 + row / 64) * 64) * 65 + row % 64;
 #pragma unroll
-                    for (int j = 0; j < 64; ++j) rr[j * 65] = R[j] * yr;
+                    for (int j = 0; j < 64; ++j) R[j] *= yr;
+#pragma unroll
+                    for (int st = 0; st < 5; ++st) {
+                        const int H = 32 >> st, xm = 16 >> st;
+                        const bool up = (lane & xm) != 0;  // keeps the upper half of the columns
+#pragma unroll
+                        for (int i = 0; i < H; ++i) {
+                            const float send = up ? R[i] : R[H + i];
+                            const float keep = up ? R[H + i] : R[i];
+                            R[i] = keep + __shfl_xor_sync(0xffffffffu, send, xm);
+                        }
+                    }
+                    *reinterpret_cast<float2*>(&red[threadIdx.x / 32][2 * lane]) = make_float2(R[0], R[1]);
                 }
             }
         }
@@ -1550,11 +1570,8 @@ __global__ void __launch_bounds__(NTH, 1) lauum_tc(int nt, const float* __restri
             const int hh = threadIdx.x / 128, half = (threadIdx.x / 64) % 2, c = threadIdx.x % 64;
             const int ti = 2 * I2 + half, tj = 2 * J2 + hh;
             if (tj <= ti) {
-                float sum = 0.f;
-                if (ti != tj) {
-                    const float* rc = red + (size_t)((hh * 2 + half) * 64 + c) * 65;
-                    for (int r = 0; r < 64; ++r) sum += rc[r];
-                }
+                // the tile's 64 rows are producer warps 4 hh + 2 half and 4 hh + 2 half + 1
+                const float sum = (ti != tj) ? red[4 * hh + 2 * half][c] + red[4 * hh + 2 * half + 1][c] : 0.f;
                 pb[(size_t)tile_index(ti, tj) * 2 * TS + TS + c] = make_float2(sum, 0.f);
             }
         }
