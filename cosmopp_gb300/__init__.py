@@ -421,7 +421,7 @@ class Context:
         self._check(self._L.cg_selftest_wait_timeout(self._h, ctypes.byref(st)))
         return st.value
 
-    TUNE_KNOBS = ("fwd", "fwd_ctas", "chol_ctas", "panel_ctas", "adj", "diag_sq", "table_bf16", "graph", "lauum", "trtri", "hmc_device")
+    TUNE_KNOBS = ("fwd", "fwd_ctas", "chol_ctas", "panel_ctas", "adj", "diag_sq", "table_bf16", "graph", "lauum", "trtri", "hmc_device", "overlap")
     ACCURACY_KNOBS = ("fwd", "diag_sq", "table_bf16")   # never changed by autotune
 
     def tune_set(self, knob, value):

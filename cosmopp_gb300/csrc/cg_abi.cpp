@@ -96,6 +96,12 @@ extern "C" void cg_destroy(cg_ctx* ctx)
     cudaFree(ctx->d_beam); cudaFree(ctx->d_cl); cudaFree(ctx->d_out);
     for (cudaEvent_t e : ctx->marks)
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_col, ctx->ev_join})
+        if (e) cudaEventDestroy(e);
+    if (ctx->hi) {
+        cudaStreamSynchronize(ctx->hi);
+        cudaStreamDestroy(ctx->hi);
+    }
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -523,7 +529,9 @@ extern "C" int cg_loglike_device(cg_ctx* ctx, int B, const double* d_cl, const d
                 cudaGraph_t g = nullptr;
                 const cudaError_t ec = cudaStreamEndCapture(s, &g);
                 cudaGraphExec_t ex = nullptr;
-                if (!rc && ec == cudaSuccess && g && cudaGraphInstantiate(&ex, g, 0) == cudaSuccess) {
+                // node priorities: the overlapped Cholesky's launches keep their stream's priority
+                if (!rc && ec == cudaSuccess && g &&
+                    cudaGraphInstantiate(&ex, g, cudaGraphInstantiateFlagUseNodePriority) == cudaSuccess) {
                     cudaGraphDestroy(g);
                     // the stale or least recently used slot takes it
                     cg_ctx::Graph* victim = &ctx->graphs[0];

@@ -120,6 +120,8 @@ struct Tune {
                           // or from the split copy (0); persistent CTAs over a work queue (1)
     int trtri = 0;        // 0 = one CTA per trtri block, 1 = persistent CTAs over a work queue (same results)
     int hmc_device = 1;   // cg_hmc_run: 1 = leapfrog resident on the device, 0 = the host loop (same chains)
+    int overlap = 1;      // 1 = trtri's row launches run beside the Cholesky (which moves to a high-priority
+                          // stream of the context), row I2 once column I2's update is done; 0 = after it
 };
 
 // the argument set a captured mixed call was recorded for
@@ -149,6 +151,10 @@ struct cg_ctx {
     double recenter_radius = 1.0;
     int sm_count = 0;
     cudaStream_t stream = nullptr;
+    // the overlapped Cholesky + trtri (Tune::overlap): the Cholesky's stream, at the device's highest
+    // priority, and the events that fork it from the caller's stream, hand each column to trtri and join
+    cudaStream_t hi = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_col = nullptr, ev_join = nullptr;
     std::vector<double> xyz;     // [n][3]
     std::vector<double> noise;   // [n]
     cg::LegConsts leg;
@@ -263,6 +269,10 @@ int hmc_launch_accept(cg_ctx* ctx, int B, int np, const int* flag, const double*
                       const double* un, double* x, double* g, double* u, cudaStream_t s);
 int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, float* Lc, float* Linv, float* Ms,
                       float* Mc, float* diag, int* status, int* d_err, cudaStream_t s);
+// the tensor-core Cholesky with trtri's row launches beside it (Tune::overlap = 1): the Cholesky on
+// ctx->hi, forked from s; row I2 on s once column I2's update is done; s joins the Cholesky at the end
+int tiled_chol_trtri_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, float* Lc, float* Linv, float* Ms,
+                        float* Mc, float* diag, int* status, int* d_err, cudaStream_t s);
 int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* Ls, const float* Linv, float* Ms, float* Mc,
                    int* d_err, cudaStream_t s);
 int tiled_lauum_tc(cg_ctx* ctx, int B, int nt, const float* Ms, const float* Mc, float* V, int* d_err,

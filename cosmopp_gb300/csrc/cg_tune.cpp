@@ -37,6 +37,7 @@ const Knob kKnobs[] = {
     {"lauum", &cg::Tune::lauum},
     {"trtri", &cg::Tune::trtri},
     {"hmc_device", &cg::Tune::hmc_device},
+    {"overlap", &cg::Tune::overlap},
 };
 
 const Knob* find_knob(const char* name)
@@ -59,6 +60,7 @@ std::vector<int> candidates(const cg_ctx* ctx, const Knob& k)
     if (k.field == &cg::Tune::adj) return {0, 1, 2, 3};
     if (k.field == &cg::Tune::lauum) return {0, 1, 2};
     if (k.field == &cg::Tune::trtri) return {0, 1};
+    if (k.field == &cg::Tune::overlap) return {1, 0};
     return {ctx->tune.*(k.field)};  // accuracy knobs (fwd, diag_sq, table_bf16) and switches (graph, hmc_device): not searched
 }
 
@@ -68,7 +70,7 @@ bool valid_value(const cg_ctx* ctx, const Knob& k, int v)
     if (k.field == &cg::Tune::adj) return v >= 0 && v <= 3;
     if (k.field == &cg::Tune::lauum) return v >= 0 && v <= 2;
     if (k.field == &cg::Tune::diag_sq || k.field == &cg::Tune::table_bf16 || k.field == &cg::Tune::graph ||
-        k.field == &cg::Tune::trtri || k.field == &cg::Tune::hmc_device)
+        k.field == &cg::Tune::trtri || k.field == &cg::Tune::hmc_device || k.field == &cg::Tune::overlap)
         return v == 0 || v == 1;
     return v >= 0 && v <= 64 * std::max(1, ctx->sm_count);  // CTA counts; 0 = one per SM
 }

@@ -824,11 +824,20 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
             B, lp, w.U, w.eps, w.A, tiled, w.tcerr);
     }
     stage_mark(ctx, ST_CHOL, s);
-    if ((rc = tiled_cholesky_tc(ctx, B, nt, w.A, w.Ls, w.Lc, w.Linv, w.Ms, w.Mc, w.diag, w.st, w.tcerr, s))) return rc;
-    logdet_mixed<<<B, 256, 0, s>>>(n, N, w.diag, w.ldref, w.ld);
-    count_launch(ctx);
-    stage_mark(ctx, ST_TRTRI, s);
-    if ((rc = tiled_trtri_tc(ctx, B, nt, w.Ls, w.Linv, w.Ms, w.Mc, w.tcerr, s))) return rc;
+    if (ctx->tune.overlap) {
+        // trtri's rows beside the Cholesky (which marks the trtri stage's start where it ends)
+        if ((rc = tiled_chol_trtri_tc(ctx, B, nt, w.A, w.Ls, w.Lc, w.Linv, w.Ms, w.Mc, w.diag, w.st, w.tcerr, s)))
+            return rc;
+        logdet_mixed<<<B, 256, 0, s>>>(n, N, w.diag, w.ldref, w.ld);
+        count_launch(ctx);
+    } else {
+        if ((rc = tiled_cholesky_tc(ctx, B, nt, w.A, w.Ls, w.Lc, w.Linv, w.Ms, w.Mc, w.diag, w.st, w.tcerr, s)))
+            return rc;
+        logdet_mixed<<<B, 256, 0, s>>>(n, N, w.diag, w.ldref, w.ld);
+        count_launch(ctx);
+        stage_mark(ctx, ST_TRTRI, s);
+        if ((rc = tiled_trtri_tc(ctx, B, nt, w.Ls, w.Linv, w.Ms, w.Mc, w.tcerr, s))) return rc;
+    }
     // x = V y; r = y - A x; x += V r  (the partials buffer holds double-float pairs here); the first
     // pass's tile partials come from lauum's epilogue, which still holds each block of V in registers
     // (not from the work-queue lauum, whose epilogues run beside the next block's K loop)

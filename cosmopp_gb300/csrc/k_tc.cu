@@ -2195,28 +2195,61 @@ size_t tc_linv_elems(int nt) { return (size_t)(nt / 2) * LINV_SC; }
 // (nt + 1 + I2, I2 < nt/2)
 int tc_queue_slots(int nt) { return nt + 1 + nt / 2; }
 
+// the Cholesky's column block J2: the update (with the diagonal blocks' factorisation) and the panel solve
+static void chol_column(cg_ctx* ctx, int J2, int B, int nt, const float* A, float* Ls, float* Lc, float* Linv,
+                        float* Ms, float* Mc, float* diag, int* status, int* d_err, cudaStream_t s)
+{
+    const int nt2 = nt / 2;
+    // diagonal CTAs, then one CTA per off-diagonal block (J2 = 0) or persistent CTAs
+    const int noff = (nt2 - J2 - 1) * B;
+    const int cap = J2 == 0 ? 4 * ctx->sm_count : (ctx->tune.chol_ctas > 0 ? ctx->tune.chol_ctas : ctx->sm_count);
+    const int grid = B + (noff < cap ? noff : cap);
+    chol_tc_update<<<grid, NTH, tc_smem(), s>>>(J2, nt, B, A, Ls, Lc, Linv, Ms, Mc, diag, status,
+                                                d_err + 1 + nt2 + J2, d_err, ctx->tune.diag_sq);
+    count_launch(ctx);
+}
+
+static void chol_panel(cg_ctx* ctx, int J2, int B, int nt, float* Ls, float* Lc, const float* Linv, int* d_err,
+                       cudaStream_t s)
+{
+    const int nt2 = nt / 2;
+    if (J2 + 1 >= nt2) return;
+    const int items = (nt2 - J2 - 1) * B;
+    const int pc = ctx->tune.panel_ctas > 0 ? ctx->tune.panel_ctas : ctx->sm_count;
+    chol_tc_panel<<<items < pc ? items : pc, NTH, tc_smem(), s>>>(J2, nt, B, Ls, Lc, Linv, d_err + 1 + J2, d_err);
+    count_launch(ctx);
+}
+
+// trtri's row block I2 >= 1 (the diagonal blocks M_II come from the Cholesky): its blocks J2 < I2
+// read L's row panel I2 (final once the Cholesky's panel I2 - 1 is done), Linv_I2 (from column I2's
+// update) and M's rows above I2 (earlier rows), and write M's row I2, which no later Cholesky step reads
+static void trtri_row(cg_ctx* ctx, int I2, int B, int nt, const float* Ls, const float* Linv, float* Ms, float* Mc,
+                      int* d_err, cudaStream_t s)
+{
+    if (ctx->tune.trtri == 1) {
+        const int items = I2 * B;
+        trtri_tc_stream<<<items < ctx->sm_count ? items : ctx->sm_count, NTH, tc_smem(), s>>>(
+            I2, nt, B, Ls, Linv, Ms, Mc, d_err + 1 + nt + 1 + I2, d_err);
+    } else {
+        trtri_tc_row<<<dim3(I2, B), NTH, tc_smem(), s>>>(I2, nt, Ls, Linv, Ms, Mc, d_err);
+    }
+    count_launch(ctx);
+}
+
+static int trtri_smem(cg_ctx* ctx)
+{
+    return ctx->tune.trtri == 1 ? set_smem(ctx, trtri_tc_stream) : set_smem(ctx, trtri_tc_row);
+}
+
 int tiled_cholesky_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, float* Lc, float* Linv, float* Ms,
                       float* Mc, float* diag, int* status, int* d_err, cudaStream_t s)
 {
     if (nt % 2) { ctx->err = "tensor-core Cholesky needs an even tile count"; return CG_ERR_BAD_ARG; }
     int rc;
     if ((rc = set_smem(ctx, chol_tc_update)) || (rc = set_smem(ctx, chol_tc_panel))) return rc;
-    const int nt2 = nt / 2;
-    for (int J2 = 0; J2 < nt2; ++J2) {
-        // diagonal CTAs, then one CTA per off-diagonal block (J2 = 0) or persistent CTAs
-        const int noff = (nt2 - J2 - 1) * B;
-        const int cap = J2 == 0 ? 4 * ctx->sm_count : (ctx->tune.chol_ctas > 0 ? ctx->tune.chol_ctas : ctx->sm_count);
-        const int grid = B + (noff < cap ? noff : cap);
-        chol_tc_update<<<grid, NTH, tc_smem(), s>>>(J2, nt, B, A, Ls, Lc, Linv, Ms, Mc, diag, status,
-                                                    d_err + 1 + nt2 + J2, d_err, ctx->tune.diag_sq);
-        count_launch(ctx);
-        if (J2 + 1 < nt2) {
-            const int items = (nt2 - J2 - 1) * B;
-            const int pc = ctx->tune.panel_ctas > 0 ? ctx->tune.panel_ctas : ctx->sm_count;
-            chol_tc_panel<<<items < pc ? items : pc, NTH, tc_smem(), s>>>(
-                J2, nt, B, Ls, Lc, Linv, d_err + 1 + J2, d_err);
-            count_launch(ctx);
-        }
+    for (int J2 = 0; J2 < nt / 2; ++J2) {
+        chol_column(ctx, J2, B, nt, A, Ls, Lc, Linv, Ms, Mc, diag, status, d_err, s);
+        chol_panel(ctx, J2, B, nt, Ls, Lc, Linv, d_err, s);
     }
     CG_CUDA_TRY(ctx, cudaGetLastError());
     return CG_OK;
@@ -2227,22 +2260,44 @@ int tiled_trtri_tc(cg_ctx* ctx, int B, int nt, const float* Ls, const float* Lin
 {
     if (nt % 2) { ctx->err = "tensor-core trtri needs an even tile count"; return CG_ERR_BAD_ARG; }
     int rc;
-    const int nt2 = nt / 2;
-    if (ctx->tune.trtri == 1) {
-        if ((rc = set_smem(ctx, trtri_tc_stream))) return rc;
-    } else {
-        if ((rc = set_smem(ctx, trtri_tc_row))) return rc;
+    if ((rc = trtri_smem(ctx))) return rc;
+    for (int I2 = 1; I2 < nt / 2; ++I2) trtri_row(ctx, I2, B, nt, Ls, Linv, Ms, Mc, d_err, s);
+    CG_CUDA_TRY(ctx, cudaGetLastError());
+    return CG_OK;
+}
+
+// The Cholesky on the context's high-priority stream and trtri's rows on s, each row after its
+// column's update (the block scheduler then gives free SMs to the Cholesky's CTAs first, and
+// trtri's fill the rest: the panel solves' HBM-bound launches, the update's tails); s waits for
+// the whole Cholesky at the end.  Same launches, same results as tiled_cholesky_tc + tiled_trtri_tc.
+int tiled_chol_trtri_tc(cg_ctx* ctx, int B, int nt, const float* A, float* Ls, float* Lc, float* Linv, float* Ms,
+                        float* Mc, float* diag, int* status, int* d_err, cudaStream_t s)
+{
+    if (nt % 2) { ctx->err = "tensor-core Cholesky needs an even tile count"; return CG_ERR_BAD_ARG; }
+    int rc;
+    if ((rc = set_smem(ctx, chol_tc_update)) || (rc = set_smem(ctx, chol_tc_panel)) || (rc = trtri_smem(ctx)))
+        return rc;
+    if (!ctx->hi) {
+        int least = 0, greatest = 0;
+        CG_CUDA_TRY(ctx, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        CG_CUDA_TRY(ctx, cudaStreamCreateWithPriority(&ctx->hi, cudaStreamNonBlocking, greatest));
     }
-    for (int I2 = 1; I2 < nt2; ++I2) {  // the diagonal blocks M_II come from the Cholesky
-        if (ctx->tune.trtri == 1) {
-            const int items = I2 * B;
-            trtri_tc_stream<<<items < ctx->sm_count ? items : ctx->sm_count, NTH, tc_smem(), s>>>(
-                I2, nt, B, Ls, Linv, Ms, Mc, d_err + 1 + nt + 1 + I2, d_err);
-        } else {
-            trtri_tc_row<<<dim3(I2, B), NTH, tc_smem(), s>>>(I2, nt, Ls, Linv, Ms, Mc, d_err);
+    for (cudaEvent_t* e : {&ctx->ev_fork, &ctx->ev_col, &ctx->ev_join})
+        if (!*e) CG_CUDA_TRY(ctx, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    CG_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_fork, s));
+    CG_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->hi, ctx->ev_fork, 0));
+    for (int J2 = 0; J2 < nt / 2; ++J2) {
+        chol_column(ctx, J2, B, nt, A, Ls, Lc, Linv, Ms, Mc, diag, status, d_err, ctx->hi);
+        if (J2 >= 1) {
+            CG_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_col, ctx->hi));
+            CG_CUDA_TRY(ctx, cudaStreamWaitEvent(s, ctx->ev_col, 0));
+            trtri_row(ctx, J2, B, nt, Ls, Linv, Ms, Mc, d_err, s);
         }
-        count_launch(ctx);
+        chol_panel(ctx, J2, B, nt, Ls, Lc, Linv, d_err, ctx->hi);
     }
+    stage_mark(ctx, ST_TRTRI, ctx->hi);  // the Cholesky's end: the trtri stage is the rows left after it
+    CG_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_join, ctx->hi));
+    CG_CUDA_TRY(ctx, cudaStreamWaitEvent(s, ctx->ev_join, 0));
     CG_CUDA_TRY(ctx, cudaGetLastError());
     return CG_OK;
 }

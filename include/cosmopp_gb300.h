@@ -258,7 +258,9 @@ int cg_stage_times(cg_ctx* ctx, double* ms);
    chip; 0: A read pre-split; 1: persistent CTAs over a work queue, A split on chip; 0 differs from
    the others below 2^-22 of an entry), "trtri" (0, the default: one CTA per block of L^-1;
    1: persistent CTAs over a work queue with each block's two products chained on chip, identical
-   results).  Accuracy choices, never changed by cg_autotune: "fwd" (forward contraction:
+   results), "overlap" (1, the default: trtri's row launches run beside the Cholesky, which the
+   call moves to a high-priority stream of the context, each row once its column's update is done;
+   0: trtri after the Cholesky; identical results).  Accuracy choices, never changed by cg_autotune: "fwd" (forward contraction:
    0 = FP32 FMA, the default; 1 = tensor cores, faster, but its one-way accumulation rounding
    biases the whitened matrix by a few ulp of |A - I|, about 1e-3 in -2lnL at nside 16 for C_l
    a factor e from the reference point), "diag_sq" (1, the default: the Cholesky's diagonal

@@ -327,3 +327,33 @@ def test_work_queue_variants_of_trtri_and_lauum():
     assert np.abs(both["m2lnl"] - base["m2lnl"]).max() <= 1e-6
     dg = np.abs(both["grad"][:, 2:] - base["grad"][:, 2:]) / np.abs(base["grad"][:, 2:]).max(axis=1, keepdims=True)
     assert dg.max() <= 1e-5
+
+
+def test_trtri_beside_the_cholesky_gives_identical_results():
+    """Knob overlap = 1 runs trtri's row launches beside the Cholesky (the Cholesky on a high-priority
+    stream of the context, row I2 after column I2's update): the same launches on the same operands,
+    so the results equal the sequential order's bit for bit, through a captured graph and through
+    direct launches, with either trtri kernel, call after call."""
+    g = load_golden("nside16_lmax47")
+    B = 40
+    cls = W.lognormal_batch(g["cls"][0], B, 41)
+    with _ctx(g, "mixed", B, cl_ref=g["cls"][0], recenter="fixed") as ctx:
+        assert ctx.tune_get("overlap") == 1
+        ctx.tune_set("overlap", 0)
+        want = ctx.loglike(cls, g["d"], grad=True)
+        for graph in (1, 0):
+            ctx.tune_set("graph", graph)
+            for trtri in (0, 1):
+                ctx.tune_set("trtri", trtri)
+                ctx.tune_set("overlap", 1)
+                for _ in range(3):
+                    got = ctx.loglike(cls, g["d"], grad=True)
+                    for k in ("m2lnl", "chi2", "logdet", "grad", "status"):
+                        assert np.array_equal(got[k], want[k]), (graph, trtri, k)
+        ctx.tune_set("graph", 1)
+        ctx.tune_set("trtri", 0)
+        ctx.set_profiling(True)
+        ctx.loglike(cls, g["d"], grad=True)
+        st = ctx.stage_times()
+        ctx.set_profiling(False)
+    assert st["cholesky"] > 0 and st["trtri"] >= 0 and st["lauum"] > 0
