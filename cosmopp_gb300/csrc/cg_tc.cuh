@@ -192,6 +192,30 @@ __device__ __forceinline__ void tmem_st16(uint32_t taddr, const float4 (&v)[4])
         : "memory");
 }
 
+// Two 16-column pieces of a thread's row into tensor memory, then the wait for both, in one asm
+// statement: tcgen05.st is asynchronous, and with the wait in the same statement the source
+// registers stay reserved until the stores are complete (with a separate wait the compiler is free
+// to give them to other values in between)
+__device__ __forceinline__ void tmem_st16x2_wait(uint32_t a0, const float4 (&v0)[4], uint32_t a1, const float4 (&v1)[4])
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17};\n\t"
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%1], {%18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32, %33};\n\t"
+        "tcgen05.wait::st.sync.aligned;"
+        ::"r"(a0), "r"(a1),
+          "r"(__float_as_uint(v0[0].x)), "r"(__float_as_uint(v0[0].y)), "r"(__float_as_uint(v0[0].z)),
+          "r"(__float_as_uint(v0[0].w)), "r"(__float_as_uint(v0[1].x)), "r"(__float_as_uint(v0[1].y)),
+          "r"(__float_as_uint(v0[1].z)), "r"(__float_as_uint(v0[1].w)), "r"(__float_as_uint(v0[2].x)),
+          "r"(__float_as_uint(v0[2].y)), "r"(__float_as_uint(v0[2].z)), "r"(__float_as_uint(v0[2].w)),
+          "r"(__float_as_uint(v0[3].x)), "r"(__float_as_uint(v0[3].y)), "r"(__float_as_uint(v0[3].z)),
+          "r"(__float_as_uint(v0[3].w)), "r"(__float_as_uint(v1[0].x)), "r"(__float_as_uint(v1[0].y)),
+          "r"(__float_as_uint(v1[0].z)), "r"(__float_as_uint(v1[0].w)), "r"(__float_as_uint(v1[1].x)),
+          "r"(__float_as_uint(v1[1].y)), "r"(__float_as_uint(v1[1].z)), "r"(__float_as_uint(v1[1].w)),
+          "r"(__float_as_uint(v1[2].x)), "r"(__float_as_uint(v1[2].y)), "r"(__float_as_uint(v1[2].z)),
+          "r"(__float_as_uint(v1[2].w)), "r"(__float_as_uint(v1[3].x)), "r"(__float_as_uint(v1[3].y)),
+          "r"(__float_as_uint(v1[3].z)), "r"(__float_as_uint(v1[3].w))
+        : "memory");
+}
 __device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
 // ---- bulk (non-tensor) async copies global -> shared, completing on an mbarrier ----
@@ -230,12 +254,14 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-// registers -> 32 lanes x 32 consecutive 32-bit columns (the inverse of tmem_ld32)
+// registers -> 32 lanes x 32 consecutive 32-bit columns (the inverse of tmem_ld32), with the wait in
+// the same statement (see tmem_st16x2_wait)
 __device__ __forceinline__ void tmem_st32(uint32_t taddr, const float (&v)[32])
 {
     asm volatile(
         "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32};" ::"r"(taddr),
+        "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32};\n\t"
+        "tcgen05.wait::st.sync.aligned;" ::"r"(taddr),
         "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])), "r"(__float_as_uint(v[3])),
         "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])), "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])),
         "r"(__float_as_uint(v[8])), "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
@@ -247,10 +273,17 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const float (&v)[32])
         "r"(__float_as_uint(v[27])), "r"(__float_as_uint(v[28])), "r"(__float_as_uint(v[29])),
         "r"(__float_as_uint(v[30])), "r"(__float_as_uint(v[31]))
         : "memory");
-    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }
 
 // (r0, r1) += (m0, m1) as one packed two-lane FP32 add (round to nearest, like two FADDs)
+__device__ __forceinline__ void sub2(float& r0, float& r1, float m0, float m1)
+{
+    asm("{\n\t.reg .b64 ra, rb;\n\tmov.b64 ra, {%0, %1};\n\tmov.b64 rb, {%2, %3};\n\t"
+        "sub.rn.f32x2 ra, ra, rb;\n\tmov.b64 {%0, %1}, ra;\n\t}"
+        : "+f"(r0), "+f"(r1)
+        : "f"(m0), "f"(m1));
+}
+
 __device__ __forceinline__ void add2(float& r0, float& r1, float m0, float m1)
 {
     asm("{\n\t.reg .b64 ra, rb;\n\tmov.b64 ra, {%0, %1};\n\tmov.b64 rb, {%2, %3};\n\t"

@@ -378,8 +378,7 @@ __device__ __forceinline__ void put_a(int g, float4 (&qx)[NX], W& wait, const fl
     } else {
         split4(reinterpret_cast<const float4(&)[4]>(qx), qh, ql);
     }
-    tmem_st16(tm + lane_base() + col_a_hi(st) + 16 * h, qh);
-    tmem_st16(tm + lane_base() + col_a_lo(st) + 16 * h, ql);
+    tmem_st16x2_wait(tm + lane_base() + col_a_hi(st) + 16 * h, qh, tm + lane_base() + col_a_lo(st) + 16 * h, ql);
     if constexpr (BMODE == B_FROM_A) {
         // the same piece into B stage g % NSTB (free: the caller retired chunk g - 4), hi and lo planes
         float* stage = const_cast<float*>(sa_f) - (NSTB * STB_BYTES) / 4 + (g % NSTB) * (STB_BYTES / 4) +
@@ -391,7 +390,6 @@ __device__ __forceinline__ void put_a(int g, float4 (&qx)[NX], W& wait, const fl
         }
         fence_proxy_async();  // the MMA reads the stage through the async proxy
     }
-    tmem_wait_st();
     fence_before();
     __syncwarp();
     if (lane == 0) mbar_arrive(&ctl.a_full[st]);
@@ -631,13 +629,14 @@ __device__ bool tc_stream(int nitems, int* queue, GEO geo, FA fa, FB fb, FE epi,
             next(pq, REL_NONE);
         };
         auto retire = [&](int g, bool last) {
-            retire_acc(g, last, (g & 1) || dq.c == dq.gm.n - 1, wait, ok, err, ctl, tm, R);
-            if (dq.c == dq.gm.n - 1) {
-                epi(dq.gm, R);
+            const bool item_end = dq.c == dq.gm.n - 1;
+            retire_acc(g, last, (g & 1) || item_end, wait, ok, err, ctl, tm, R);
+            if (item_end) epi(dq.gm, R);
+            next(dq, REL_WARP);
+            if (item_end) {
 #pragma unroll
                 for (int j = 0; j < 64; ++j) R[j] = 0.f;
             }
-            next(dq, REL_WARP);
         };
         // chunks 0 and 1 into the empty stages 0 and 1; register modes load two chunks ahead of the store
         int nput = 0;  // chunks put so far; while any remain, chunk g + 2 is put at step g
@@ -731,11 +730,10 @@ __device__ __forceinline__ void put_chain(int g, const float (&R)[64], TcCtl& ct
                 x[i] = make_float4(R[j], R[j + 1], R[j + 2], R[j + 3]);
             }
             split4(x, qh, ql);
-            tmem_st16(tm + lane_base() + col_a_hi(st) + 16 * half, qh);
-            tmem_st16(tm + lane_base() + col_a_lo(st) + 16 * half, ql);
+            tmem_st16x2_wait(tm + lane_base() + col_a_hi(st) + 16 * half, qh, tm + lane_base() + col_a_lo(st) + 16 * half,
+                             ql);
         }
     }
-    tmem_wait_st();
     fence_before();
     __syncwarp();
     if (lane == 0)
@@ -1731,8 +1729,7 @@ __global__ void __launch_bounds__(ADJ_NTH, 1) contract_adj_tc(int B, int lp, con
                 }
             }
             split4(x, qh, ql);
-            tmem_st16(tm + lane_base() + col_a_hi(st) + 16 * h, qh);
-            tmem_st16(tm + lane_base() + col_a_lo(st) + 16 * h, ql);
+            tmem_st16x2_wait(tm + lane_base() + col_a_hi(st) + 16 * h, qh, tm + lane_base() + col_a_lo(st) + 16 * h, ql);
             unsigned char* stage = smem_raw + st * stb;
 #pragma unroll
             for (int p = 0; p < NBP; ++p) {
@@ -1750,7 +1747,6 @@ __global__ void __launch_bounds__(ADJ_NTH, 1) contract_adj_tc(int B, int lp, con
                 }
             }
             fence_proxy_async();
-            tmem_wait_st();
             fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive(&ab_full[st]);
