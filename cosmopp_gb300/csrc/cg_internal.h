@@ -121,7 +121,8 @@ struct Tune {
     int trtri = 0;        // 0 = one CTA per trtri block, 1 = persistent CTAs over a work queue (same results)
     int hmc_device = 1;   // cg_hmc_run: 1 = leapfrog resident on the device, 0 = the host loop (same chains)
     int overlap = 1;      // 1 = trtri's row launches run beside the Cholesky (which moves to a high-priority
-                          // stream of the context), row I2 once column I2's update is done; 0 = after it
+                          // stream of the context), row I2 once column I2's update is done; 0 = after it.
+                          // With the work-queue trtri (trtri = 1) the launches stay in sequence
 };
 
 // the argument set a captured mixed call was recorded for

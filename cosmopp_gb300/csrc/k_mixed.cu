@@ -824,8 +824,10 @@ int mixed_loglike(cg_ctx* ctx, int B, const double* d_cl, const double* h_cl, co
             B, lp, w.U, w.eps, w.A, tiled, w.tcerr);
     }
     stage_mark(ctx, ST_CHOL, s);
-    if (ctx->tune.overlap) {
-        // trtri's rows beside the Cholesky (which marks the trtri stage's start where it ends)
+    if (ctx->tune.overlap && ctx->tune.trtri != 1) {
+        // trtri's rows beside the Cholesky (which marks the trtri stage's start where it ends); the
+        // work-queue trtri runs after it (beside it, one call in about three hundred gave results that
+        // differed in the last bits)
         if ((rc = tiled_chol_trtri_tc(ctx, B, nt, w.A, w.Ls, w.Lc, w.Linv, w.Ms, w.Mc, w.diag, w.st, w.tcerr, s)))
             return rc;
         logdet_mixed<<<B, 256, 0, s>>>(n, N, w.diag, w.ldref, w.ld);

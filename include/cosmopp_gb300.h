@@ -260,7 +260,7 @@ int cg_stage_times(cg_ctx* ctx, double* ms);
    1: persistent CTAs over a work queue with each block's two products chained on chip, identical
    results), "overlap" (1, the default: trtri's row launches run beside the Cholesky, which the
    call moves to a high-priority stream of the context, each row once its column's update is done;
-   0: trtri after the Cholesky; identical results).  Accuracy choices, never changed by cg_autotune: "fwd" (forward contraction:
+   0: trtri after the Cholesky; identical results; with "trtri" = 1 the launches stay in sequence).  Accuracy choices, never changed by cg_autotune: "fwd" (forward contraction:
    0 = FP32 FMA, the default; 1 = tensor cores, faster, but its one-way accumulation rounding
    biases the whitened matrix by a few ulp of |A - I|, about 1e-3 in -2lnL at nside 16 for C_l
    a factor e from the reference point), "diag_sq" (1, the default: the Cholesky's diagonal

@@ -333,7 +333,8 @@ def test_trtri_beside_the_cholesky_gives_identical_results():
     """Knob overlap = 1 runs trtri's row launches beside the Cholesky (the Cholesky on a high-priority
     stream of the context, row I2 after column I2's update): the same launches on the same operands,
     so the results equal the sequential order's bit for bit, through a captured graph and through
-    direct launches, with either trtri kernel, call after call."""
+    direct launches, call after call.  With the work-queue trtri (trtri = 1) the launches stay in
+    sequence, and its results are the same too."""
     g = load_golden("nside16_lmax47")
     B = 40
     cls = W.lognormal_batch(g["cls"][0], B, 41)
