@@ -125,7 +125,7 @@ struct TcCtl {
     uint64_t a_full[NAST];    // stage: the chunk's A is in tensor memory (one arrival per producer warp) and,
                               // where a copy thread fills the B stage, its B landed (that thread's arrival
                               // with the copies' bytes), so the issuer polls one barrier per chunk
-    uint64_t b_full[NSTB];    // (unused: the B copies complete on a_full)
+    uint64_t b_full[NSTB];    // B_PRE: the stage's B, copied ahead of its K loop, landed (B_COPY copies complete on a_full)
     uint64_t b_empty[NSTB];   // B stage's MMAs completed
     uint64_t as_full[NSTA];   // A shared-memory stage landed
     uint64_t as_empty[NSTA];  // A shared-memory stage read by every producer warp
@@ -136,14 +136,15 @@ struct TcCtl {
     int bad;
 };
 
-// bcopy: a copy thread fills the B stages (B_COPY), so a_full also counts its arrival
-__device__ __forceinline__ void init_bars(TcCtl& ctl, bool bcopy = true)
+// bcopy: a copy thread fills the B stages (B_COPY), so a_full also counts its arrival; bfull: b_full
+// is initialised too (not when a second K loop's B copies may already be counting on it)
+__device__ __forceinline__ void init_bars(TcCtl& ctl, bool bcopy = true, bool bfull = true)
 {
     for (int i = 0; i < NAST; ++i) mbar_init(&ctl.mma_bar[i], 1);
     for (int i = 0; i < 2; ++i) mbar_init(&ctl.acc_free[i], NPROD / 32);
     for (int i = 0; i < NAST; ++i) mbar_init(&ctl.a_full[i], NPROD / 32 + (bcopy ? 1 : 0));
     for (int i = 0; i < NSTB; ++i) {
-        mbar_init(&ctl.b_full[i], 1);
+        if (bfull) mbar_init(&ctl.b_full[i], 1);
         mbar_init(&ctl.b_empty[i], 1);
     }
     for (int i = 0; i < NSTA; ++i) {
@@ -178,15 +179,18 @@ __device__ __forceinline__ void tc_end(uint32_t tm)
     if (threadIdx.x < 32) tmem_dealloc(tm, TMEM_COLS);
 }
 
-// re-arm the barriers for a second K loop in the same CTA (every MMA and copy of the first completed)
-__device__ __forceinline__ void tc_rearm(TcCtl& ctl)
+// re-arm the barriers for a second K loop in the same CTA whose B stages were filled ahead (B_PRE):
+// every MMA of the first loop completed; b_full, which the second loop's B copies (issued by the
+// first loop's B copy thread as the stages were freed) count on, is left as it is
+__device__ __forceinline__ void tc_rearm_pre(TcCtl& ctl)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
         uint64_t* all = &ctl.mma_bar[0];  // every barrier of TcCtl, contiguous
         for (int i = 0; i < 2 * NAST + 2 + 2 * NSTB + 2 * NSTA + 2 * NIQ; ++i)
-            asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(all + i)));
-        init_bars(ctl);
+            if (all + i < ctl.b_full || all + i >= ctl.b_full + NSTB)
+                asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(all + i)));
+        init_bars(ctl, false, false);
     }
     __syncthreads();
 }
@@ -323,7 +327,9 @@ enum { A_REG_SC = 0, A_REG_C1 = 1, A_SMEM_C1 = 2, A_SMEM_PRE = 3 };
 //   B_FROM_A  (A_SMEM_C1 only, fb unused) B is the same matrix as A (a diagonal block's L_J L_J^T):
 //             the producers write the A chunk they split into the B stage too, so the rows are read
 //             from memory once, in FP32, instead of twice.
-enum { B_COPY = 0, B_FROM_A = 1 };
+//   B_PRE     (at most NSTB chunks) the stages were filled before the loop, each copy completing on
+//             the stage's b_full (phase 0); the loop copies nothing.
+enum { B_COPY = 0, B_FROM_A = 1, B_PRE = 2 };
 
 // ---- pieces shared by the single-item K loop and the item stream -----------------------------
 
@@ -424,6 +430,7 @@ __device__ __forceinline__ void issue_chunk(int g, W& wait, TcCtl& ctl, uint32_t
 {
     const int st = g % NAST, sbi = g % NSTB, pr = g >> 1;
     wait(&ctl.a_full[st], (g / NAST) & 1);  // A put and (B_COPY) B landed: one barrier
+    if constexpr (BMODE == B_PRE) wait(&ctl.b_full[sbi], 0);
     if ((g & 1) == 0 && pr >= 2) wait(&ctl.acc_free[pr & 1], ((pr - 2) >> 1) & 1);
     fence_after();
     const uint32_t bh = sb + sbi * STB_BYTES, bl = bh + STB_BYTES / 2;
@@ -472,11 +479,17 @@ __device__ __forceinline__ void copy_b(int g, W& wait, TcCtl& ctl, uint32_t sb, 
 // product for row t % 128, column 64 (t / 128) + j (0 if nchunks == 0).  Returns false if an
 // mbarrier wait gave up; waits give up early once *err is set (by this or any other CTA), and a
 // thread whose wait gave up skips its later waits, so a failure ends the launch quickly.
-template <int AMODE, int BMODE = B_COPY, class FA, class FB>
+// tc_kloop's default `tail`: nothing after the B copy thread's last copy
+struct NoTail {
+    template <class W>
+    __device__ __forceinline__ void operator()(W&, TcCtl&, uint32_t) const {}
+};
+
+template <int AMODE, int BMODE = B_COPY, class FA, class FB, class FT = NoTail>
 __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& ctl, uint32_t tm, float (&R)[64],
-                         int* err, float2* ssq = nullptr)
+                         int* err, float2* ssq = nullptr, FT tail = FT())
 {
-    static_assert(BMODE == B_COPY || AMODE == A_SMEM_C1, "B_FROM_A needs the A chunk staged in shared memory");
+    static_assert(BMODE != B_FROM_A || AMODE == A_SMEM_C1, "B_FROM_A needs the A chunk staged in shared memory");
     bool ok = true;
     auto wait = [&](uint64_t* bar, uint32_t parity) {
         if (!ok) return;
@@ -530,10 +543,12 @@ __device__ bool tc_kloop(int nchunks, FA fa, FB fb, unsigned char* sbuf, TcCtl& 
             }
         __syncwarp();
     } else if (warp == NPROD / 32 + 1) {
-        // ---- B copies
-        if (lane == 0)
+        // ---- B copies, then tail(wait, ctl, sb) (e.g. a next loop's B copies as the stages free up)
+        if (lane == 0) {
             for (int c = 0; c < nchunks; ++c)
                 copy_b<BMODE>(c, wait, ctl, sb, [&](uint32_t dst, uint64_t* bar) { fb(c, dst, bar); });
+            tail(wait, ctl, sb);
+        }
         __syncwarp();
     } else {
         // ---- A copies
@@ -1373,8 +1388,17 @@ __global__ void __launch_bounds__(NTH, 1) trtri_tc_row(int I2, int nt, const flo
         bulk_tiles(Lb + (size_t)tile_index(2 * I2, k) * SC_TILE, Lb + (size_t)tile_index(2 * I2 + 1, k) * SC_TILE,
                    c % 2, dst, bar);
     };
+    // the second product's B, Linv_I's four chunks, copied into the B stages by the first loop's B copy
+    // thread as each stage's last MMAs complete, so that it lands while the first product finishes
+    auto tail = [&](auto& wait, TcCtl& c, uint32_t sb) {
+        for (int q = 0; q < NSTB; ++q) {
+            const int cq = nchunks - 1 - ((nchunks - 1 - q) % NSTB);  // the first loop's last chunk in stage q
+            wait(&c.b_empty[q], (cq / NSTB) & 1);
+            bulk_linv(li, q, sb + q * STB_BYTES, &c.b_full[q]);
+        }
+    };
     float R[64];
-    tc_kloop<A_SMEM_C1>(nchunks, fa, fb, smem_raw, ctl, tm, R, err);
+    tc_kloop<A_SMEM_C1>(nchunks, fa, fb, smem_raw, ctl, tm, R, err, nullptr, tail);
     // S^T stays on chip: into the A ring as the four FP32 canonical K chunks of the second product
     // (row = M's column, K = M's rows 64h .. 64h+63: chunks 2h, 2h+1).  Every producer's last ring
     // read came before the last chunk's MMAs, which any producer leaving the loop has waited for.
@@ -1387,11 +1411,12 @@ __global__ void __launch_bounds__(NTH, 1) trtri_tc_row(int I2, int nt, const flo
                                        (row & 7) * 4) = make_float4(R[4 * q], R[4 * q + 1], R[4 * q + 2], R[4 * q + 3]);
         }
     }
-    tc_rearm(ctl);  // its __syncthreads also makes the ring writes visible to all producers
-    // A(c, m) = S^T(c, m) from the ring; B(r, m) = Linv_I(r, m)
+    tc_rearm_pre(ctl);  // its __syncthreads also makes the ring writes visible to all producers
+    // A(c, m) = S^T(c, m) from the ring; B(r, m) = Linv_I(r, m), already in (or on its way to) the B stages
+    static_assert(128 / KC == NSTB, "the second product's B fills the B stages exactly");
     auto fa2 = [](int, const float*&, const float*&, int&) {};
-    auto fb2 = [&](int c, uint32_t dst, uint64_t* bar) { bulk_linv(li, c, dst, bar); };
-    tc_kloop<A_SMEM_PRE>(128 / KC, fa2, fb2, smem_raw, ctl, tm, R, err);
+    auto fb2 = [](int, uint32_t, uint64_t*) {};
+    tc_kloop<A_SMEM_PRE, B_PRE>(128 / KC, fa2, fb2, smem_raw, ctl, tm, R, err);
     if (threadIdx.x < NPROD) {
         const size_t tix = tile_index(2 * I2 + h, 2 * J2 + row / 64);
         st_sc_row(Mb + tix * SC_TILE, row % 64, R, -1.f);
