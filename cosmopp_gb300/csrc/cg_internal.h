@@ -110,7 +110,8 @@ struct Tune {
     int fwd = 0;
     int fwd_ctas = 0;     // persistent CTAs of the tensor-core contraction (0 = one per SM)
     int chol_ctas = 0;    // persistent CTAs of the Cholesky's off-diagonal work queue, column blocks J > 0 (0 = one per SM)
-    int panel_ctas = 0;   // persistent CTAs of the Cholesky's panel solve (0 = one per SM)
+    int panel_ctas = 0;   // persistent CTAs of the Cholesky's panel solve (0 = one per SM; 7/8 of them when
+                          // trtri's rows run beside the Cholesky)
     int adj = 0;          // tensor-core adjoint variant (fetch groups / buffers), 0 .. 3
     int diag_sq = 1;      // Cholesky diagonal blocks: row sums of squares on the CUDA cores (accuracy, not speed)
     int table_bf16 = 0;   // the whitened Legendre table rounded to BF16 (8-bit significand) when it is built:

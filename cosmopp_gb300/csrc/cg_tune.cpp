@@ -56,7 +56,7 @@ std::vector<int> candidates(const cg_ctx* ctx, const Knob& k)
     (void)lp;
     if (k.field == &cg::Tune::fwd_ctas) return {0, sm * 3 / 4, sm / 2};
     if (k.field == &cg::Tune::chol_ctas) return {0, sm / 2, 2 * sm};
-    if (k.field == &cg::Tune::panel_ctas) return {0, sm / 2, 2 * sm};
+    if (k.field == &cg::Tune::panel_ctas) return {0, sm / 2, sm, 2 * sm};
     if (k.field == &cg::Tune::adj) return {0, 1, 2, 3};
     if (k.field == &cg::Tune::lauum) return {0, 1, 2};
     if (k.field == &cg::Tune::trtri) return {0, 1};

@@ -253,7 +253,8 @@ int cg_stage_times(cg_ctx* ctx, double* ms);
 /* ---- launch-shape tuning of the mixed path (no counterpart in the reference) ---- */
 /* Knobs, by name.  Launch shapes (results change only in rounding order): "fwd_ctas",
    "chol_ctas", "panel_ctas" (persistent CTA counts of the tensor-core contraction, the Cholesky's
-   off-diagonal work queue and its panel solve; 0 = one per SM), "adj" (tensor-core adjoint
+   off-diagonal work queue and its panel solve; 0 = one per SM, for the panel 7/8 of them while
+   trtri runs beside the Cholesky), "adj" (tensor-core adjoint
    variant 0..3), "lauum" (2, the default: one CTA per block of C^-1 with the A operand split on
    chip; 0: A read pre-split; 1: persistent CTAs over a work queue, A split on chip; 0 differs from
    the others below 2^-22 of an entry), "trtri" (0, the default: one CTA per block of L^-1;
